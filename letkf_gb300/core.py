@@ -1,0 +1,203 @@
+"""Host-side mirror of the reference's letkf_core interface and the batched
+device entry points.
+
+``letkf_core`` keeps the argument list, meaning and error behaviour of
+SUBROUTINE letkf_core (common/common_letkf.f90:50): hdxb is (nobs, ne) with
+only the first nobsl rows used, parm_infl is updated, transm / pao are the
+optional outputs, rdiag_wloc and minfl the optional inputs.  Where the
+reference STOPs (common/common_mtx.f90:61-64,75-78) this raises LetkfError.
+
+The batched wrappers take torch CUDA tensors (device memory and streams are
+torch's; the arithmetic is the library's) and call the C ABI with raw device
+pointers.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from .lib import LETKF_ERR_ARG, LETKF_OK, LetkfError, check, lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def letkf_core(ne, nobs, nobsl, hdxb, rdiag, rloc, dep, parm_infl, transm=False, pao=False, rdiag_wloc=False,
+               minfl=None):
+    """One LETKF analysis on the GPU (FP64 plain form).
+
+    Returns ``(trans, transm, pao, parm_infl)``; ``transm`` / ``pao`` are None
+    unless requested.  ``trans[k, m]`` is the weight of background member k
+    in analysis member m (Fortran trans(k+1, m+1))."""
+    hdxb = np.asfortranarray(hdxb, dtype=np.float64)
+    if hdxb.shape != (nobs, ne):
+        raise LetkfError(LETKF_ERR_ARG, f"hdxb shape {hdxb.shape} != (nobs, ne) = ({nobs}, {ne})")
+    rdiag = np.ascontiguousarray(rdiag, dtype=np.float64)
+    rloc = np.ascontiguousarray(rloc, dtype=np.float64)
+    dep = np.ascontiguousarray(dep, dtype=np.float64)
+    infl = np.array([parm_infl], dtype=np.float64)
+    trans = np.zeros((ne, ne), dtype=np.float64, order="F")
+    tm = np.zeros(ne) if transm else None
+    pa = np.zeros((ne, ne), order="F") if pao else None
+    mf = float(minfl) if minfl is not None else 0.0
+    st = lib().letkf_core_c(ne, nobs, nobsl, _ptr(hdxb), _ptr(rdiag), _ptr(rloc), _ptr(dep), _ptr(infl),
+                            _ptr(trans), _ptr(tm), _ptr(pa), int(bool(rdiag_wloc)), mf)
+    check(st, "letkf_core")
+    return trans, tm, pa, float(infl[0])
+
+
+# ---------------------------------------------------------------- device side
+def _dptr(t):
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise ValueError("expected a CUDA tensor")
+    if not t.is_contiguous():
+        raise ValueError("expected a contiguous tensor")
+    return C.c_void_p(t.data_ptr())
+
+
+def _stream(stream):
+    import torch
+
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def core_batch_f64(ne, offs, rows, rdiag, rloc, dep, parm_infl, want_transm=False, want_pao=False,
+                   rdiag_wloc=False, minfl=0.0, stream=None):
+    """Batched FP64 plain form.  offs int64 [npts+1]; rows float64 [nrows, ne];
+    parm_infl float64 [npts] is updated in place.  Returns dict of tensors
+    (trans [npts, ne, ne] with trans[p, m, k] = trans_p(k, m), transm, pao,
+    status)."""
+    import torch
+
+    npts = offs.numel() - 1
+    dev = rows.device
+    trans = torch.empty((npts, ne, ne), dtype=torch.float64, device=dev)
+    tm = torch.empty((npts, ne), dtype=torch.float64, device=dev) if want_transm else None
+    pa = torch.empty((npts, ne, ne), dtype=torch.float64, device=dev) if want_pao else None
+    status = torch.empty(npts, dtype=torch.int32, device=dev)
+    st = lib().letkf_core_batch_f64(ne, npts, _dptr(offs), _dptr(rows), _dptr(rdiag), _dptr(rloc), _dptr(dep),
+                                    _dptr(parm_infl), _dptr(trans), _dptr(tm), _dptr(pa), int(bool(rdiag_wloc)),
+                                    float(minfl), _dptr(status), _stream(stream))
+    check(st, "letkf_core_batch_f64")
+    return dict(trans=trans, transm=tm, pao=pa, status=status, parm_infl=parm_infl)
+
+
+def core_batch_mixed(ne, offs, rows, rdiag, rloc, dep, parm_infl, want_transm=False, rdiag_wloc=False, minfl=0.0,
+                     stream=None):
+    """Batched mixed-precision core: float32 rows / rdiag / rloc / dep, float64
+    parm_infl (in place).  Returns dict of tensors (float32 trans, transm)."""
+    import torch
+
+    npts = offs.numel() - 1
+    dev = rows.device
+    trans = torch.empty((npts, ne, ne), dtype=torch.float32, device=dev)
+    tm = torch.empty((npts, ne), dtype=torch.float32, device=dev) if want_transm else None
+    status = torch.empty(npts, dtype=torch.int32, device=dev)
+    st = lib().letkf_core_batch_mixed(ne, npts, _dptr(offs), _dptr(rows), _dptr(rdiag), _dptr(rloc), _dptr(dep),
+                                      _dptr(parm_infl), _dptr(trans), _dptr(tm), int(bool(rdiag_wloc)), float(minfl),
+                                      _dptr(status), _stream(stream))
+    check(st, "letkf_core_batch_mixed")
+    return dict(trans=trans, transm=tm, status=status, parm_infl=parm_infl)
+
+
+def update_f64(xb, trans, transm=None, stream=None):
+    """xb float64 [nv, npts, ne] full members; trans [npts, ne, ne] (column-
+    major per point); returns xa like xb."""
+    import torch
+
+    nv, npts, ne = xb.shape
+    xa = torch.empty_like(xb)
+    st = lib().letkf_update_f64(ne, npts, nv, _dptr(xb), _dptr(trans), _dptr(transm), _dptr(xa), _stream(stream))
+    check(st, "letkf_update_f64")
+    return xa
+
+
+def exclusive_scan(counts, stream=None):
+    import torch
+
+    offs = torch.empty(counts.numel() + 1, dtype=torch.int64, device=counts.device)
+    check(lib().letkf_exclusive_scan(counts.numel(), _dptr(counts), _dptr(offs), _stream(stream)), "scan")
+    return offs
+
+
+def gather_rows(idx, ens, dep, stream=None):
+    """rows[r] = ens[idx[r]], dep_out[r] = dep[idx[r]] (same dtype as ens)."""
+    import torch
+
+    nrows = idx.numel()
+    ne = ens.shape[1]
+    rows = torch.empty((nrows, ne), dtype=ens.dtype, device=ens.device)
+    dout = torch.empty(nrows, dtype=ens.dtype, device=ens.device)
+    check(lib().letkf_gather_rows(ne, nrows, _dptr(idx), _dptr(ens), _dptr(dep), ens.element_size(), _dptr(rows),
+                                  _dptr(dout), _stream(stream)), "gather_rows")
+    return rows, dout
+
+
+SCALE_PARAM_ORDER = ("dx", "dy", "dlon_zero", "dlat_zero", "sigma_obs", "sigma_obsv", "sigma_obs_rain",
+                     "sigma_obsv_rain", "base_obsv_rain", "sigma_obs_radar", "sigma_obs_radar_noref",
+                     "sigma_obsz_radar", "radar_ref_thres_dbz", "sigma_obs_tc", "sigma_obsv_tc")
+
+
+def search_scale(nlon, nlat, nobsgrd, obs, pts, params, var_local_row=None, stream=None):
+    """SCALE Cartesian local search on device tensors.
+    obs: dict of tensors ri, rj, lev, dat, err (float64), cls, varloc (int32), sorted.
+    pts: dict ri, rj, rlev (float64) [, rz].  params: dict with SCALE_PARAM_ORDER keys.
+    Returns (offs int64 [npts+1], idx int32, rloc, rdiag float64)."""
+    import torch
+
+    dev = obs["ri"].device
+    npts = pts["ri"].numel()
+    nobs = obs["ri"].numel()
+    P = torch.tensor([float(params[k]) for k in SCALE_PARAM_ORDER] + [0.0], dtype=torch.float64)
+    vl = None if var_local_row is None else torch.as_tensor(var_local_row, dtype=torch.float64, device=dev)
+    nobsl = torch.empty(npts, dtype=torch.int32, device=dev)
+    args = (nlon, nlat, _dptr(nobsgrd), nobs, _dptr(obs["ri"]), _dptr(obs["rj"]), _dptr(obs["lev"]),
+            _dptr(obs["dat"]), _dptr(obs["err"]), _dptr(obs["cls"]), _dptr(obs["varloc"]), npts, _dptr(pts["ri"]),
+            _dptr(pts["rj"]), _dptr(pts["rlev"]), _dptr(pts.get("rz")), _dptr(vl), C.c_void_p(P.data_ptr()))
+    check(lib().letkf_search_scale(*args, None, _dptr(nobsl), None, None, None, _stream(stream)), "search_scale")
+    offs = exclusive_scan(nobsl, stream)
+    total = int(offs[-1].item())
+    idx = torch.empty(max(total, 1), dtype=torch.int32, device=dev)
+    rloc = torch.empty(max(total, 1), dtype=torch.float64, device=dev)
+    rdiag = torch.empty(max(total, 1), dtype=torch.float64, device=dev)
+    check(lib().letkf_search_scale(*args, _dptr(offs), _dptr(nobsl), _dptr(idx), _dptr(rloc), _dptr(rdiag),
+                                   _stream(stream)), "search_scale")
+    return offs, idx[:total], rloc[:total], rdiag[:total]
+
+
+def search_speedy(grid, obs, pts, params, var_local_row, stream=None):
+    """SPEEDY lat/lon local search on device tensors.
+    grid: dict lon, lat (float64), nobsgrd (int32 [nlat, nlon]).
+    obs: dict elm, lon, lat, lev, dat, err (float64), sorted.
+    pts: dict lon, lat, dlon_zero, logpfm (float64), ilev (int32, 1-based).
+    params: (dist_zero, dist_zerov, dlat_zero, sigma_obs, sigma_obsv)."""
+    import torch
+
+    dev = obs["lon"].device
+    npts = pts["lon"].numel()
+    P = torch.tensor([float(x) for x in params], dtype=torch.float64)
+    vl = torch.as_tensor(var_local_row, dtype=torch.float64, device=dev).contiguous()
+    nobsl = torch.empty(npts, dtype=torch.int32, device=dev)
+    nlat, nlon = grid["nobsgrd"].shape
+    args = (nlon, nlat, _dptr(grid["lon"]), _dptr(grid["lat"]), _dptr(grid["nobsgrd"]), obs["lon"].numel(),
+            _dptr(obs["elm"]), _dptr(obs["lon"]), _dptr(obs["lat"]), _dptr(obs["lev"]), _dptr(obs["dat"]),
+            _dptr(obs["err"]), npts, _dptr(pts["lon"]), _dptr(pts["lat"]), _dptr(pts["dlon_zero"]),
+            _dptr(pts["ilev"]), _dptr(pts["logpfm"]), _dptr(vl), C.c_void_p(P.data_ptr()))
+    check(lib().letkf_search_speedy(*args, None, _dptr(nobsl), None, None, None, _stream(stream)), "search_speedy")
+    offs = exclusive_scan(nobsl, stream)
+    total = int(offs[-1].item())
+    idx = torch.empty(max(total, 1), dtype=torch.int32, device=dev)
+    rloc = torch.empty(max(total, 1), dtype=torch.float64, device=dev)
+    rdiag = torch.empty(max(total, 1), dtype=torch.float64, device=dev)
+    check(lib().letkf_search_speedy(*args, _dptr(offs), _dptr(nobsl), _dptr(idx), _dptr(rloc), _dptr(rdiag),
+                                    _stream(stream)), "search_speedy")
+    return offs, idx[:total], rloc[:total], rdiag[:total]
+
+
+__all__ = ["letkf_core", "core_batch_f64", "core_batch_mixed", "update_f64", "exclusive_scan", "gather_rows",
+           "search_scale", "search_speedy", "LETKF_OK"]

@@ -1,0 +1,56 @@
+// letkf_common.cuh -- shared device helpers for the GB300 LETKF kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/letkf_gpu.h"
+
+namespace letkf {
+
+// launch bookkeeping shared by every translation unit (defined in abi.cu)
+void note_launch();
+int cuda_status(cudaError_t e);
+
+constexpr double kSigmaB = 0.04;  // common/common_letkf.f90:75 error stdev of parm_infl
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_max(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    T w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w > v ? w : v;
+  }
+  return v;
+}
+
+// Block-wide sum; `red` holds >= 32 elements of scratch.  All threads get the result.
+template <typename T, int NT>
+__device__ __forceinline__ T block_sum(T v, T* red) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  T s = T(0);
+  if (w == 0) {
+    s = lane < NT / 32 ? red[lane] : T(0);
+    s = warp_sum(s);
+    if (lane == 0) red[0] = s;
+  }
+  __syncthreads();
+  s = red[0];
+  return s;
+}
+
+// Fortran SIGN(a,b)
+__device__ __forceinline__ double fsign(double a, double b) { return copysign(fabs(a), b); }
+__device__ __forceinline__ float fsignf(float a, float b) { return copysignf(fabsf(a), b); }
+
+}  // namespace letkf

@@ -1,0 +1,372 @@
+// obs_search.cu -- local observation search kernels (bit-exact selection order).
+//
+// One thread per grid point scans its candidate bucket ranges in the
+// reference order and applies the reference's tests in FP64:
+//   SCALE  scale/letkf/letkf_tools.f90:853-1178 (+ obs_choose,
+//          scale/letkf/letkf_obs.f90:1054-1119), MEM_NP = 1
+//   SPEEDY speedy/letkf/letkf_tools.f90:272-603 (+ common/common.f90:401-424)
+// Count pass (idx == NULL) writes nobsl[p]; fill pass writes the rows at
+// offs[p].  The same predicate code runs in both passes.
+#include <math.h>
+
+#include "letkf_common.cuh"
+
+namespace letkf {
+
+// scale/letkf/letkf_obs.f90:29-30 keep these as default-real literals
+__device__ __forceinline__ double scale_dzf2() { return (double)13.33333333f; }
+
+struct ScaleParams {
+  double dx, dy, dlon_zero, dlat_zero, sigma_obs, sigma_obsv, sigma_obs_rain, sigma_obsv_rain, base_obsv_rain,
+      sigma_obs_radar, sigma_obs_radar_noref, sigma_obsz_radar, radar_ref_thres_dbz, sigma_obs_tc, sigma_obsv_tc;
+};
+
+__global__ void search_scale_kernel(int nlon, int nlat, const int* __restrict__ G, int nobs,
+                                    const double* __restrict__ ori, const double* __restrict__ orj,
+                                    const double* __restrict__ olev, const double* __restrict__ odat,
+                                    const double* __restrict__ oerr, const int* __restrict__ ocls,
+                                    const int* __restrict__ ovarloc, int npts, const double* __restrict__ pri,
+                                    const double* __restrict__ prj, const double* __restrict__ prlev,
+                                    const double* __restrict__ prz, const double* __restrict__ var_local,
+                                    ScaleParams P, const int64_t* __restrict__ offs, int* nobsl, int* idx,
+                                    double* rloc, double* rdiag) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npts) return;
+  const int ld = nlon + 1;
+  const double ri = pri[p], rj = prj[p], rlev = prlev[p], rz = prz ? prz[p] : 0.0;
+  const double logr = log(rlev);
+  int imin = (int)floor(ri - P.dlon_zero);
+  if (imin < 1) imin = 1;
+  int imax = (int)ceil(ri + P.dlon_zero);
+  if (imax > nlon) imax = nlon;
+  int jmin = (int)floor(rj - P.dlat_zero);
+  if (jmin < 1) jmin = 1;
+  int jmax = (int)ceil(rj + P.dlat_zero);
+  if (jmax > nlat) jmax = nlat;
+  const double dzf2 = scale_dzf2();
+  int cnt = 0;
+  const int64_t base = idx ? offs[p] : 0;
+  if (nobs > 0 && G[(size_t)(nlat - 1) * ld + nlon] > 0 && imin <= imax && jmin <= jmax) {
+    for (int j = jmin; j <= jmax; j++) {
+      const int ib = G[(size_t)(j - 1) * ld + imin - 1], ie = G[(size_t)(j - 1) * ld + imax];
+      for (int ob = ib; ob < ie; ob++) {
+        const int vl = ovarloc[ob];
+        if (var_local && var_local[vl] < 2.2250738585072014e-308) continue;
+        const double rdx = (ri - ori[ob]) * P.dx, rdy = (rj - orj[ob]) * P.dy;
+        double nd_h = sqrt(rdx * rdx + rdy * rdy), nd_v;
+        const int cls = ocls[ob];
+        if (cls == 1) {
+          nd_h = nd_h / P.sigma_obs;
+          nd_v = fabs(log(odat[ob]) - logr) / P.sigma_obsv;
+        } else if (cls == 2) {
+          nd_h = nd_h / P.sigma_obs_rain;
+          nd_v = fabs(log(P.base_obsv_rain) - logr) / P.sigma_obsv_rain;
+        } else if (cls >= 3 && cls <= 5) {
+          if (cls == 3 && odat[ob] <= P.radar_ref_thres_dbz + 1.0e-6)
+            nd_h = nd_h / P.sigma_obs_radar_noref;
+          else
+            nd_h = nd_h / P.sigma_obs_radar;
+          nd_v = fabs(olev[ob] - rz) / P.sigma_obsz_radar;
+        } else if (cls == 6) {
+          nd_h = nd_h / P.sigma_obs_tc;
+          nd_v = fabs(log(olev[ob]) - logr) / P.sigma_obsv_tc;
+        } else {
+          nd_h = nd_h / P.sigma_obs;
+          nd_v = fabs(log(olev[ob]) - logr) / P.sigma_obsv;
+        }
+        const double ndist = nd_h * nd_h + nd_v * nd_v;
+        if (ndist > dzf2) continue;
+        if (idx) {
+          double nrloc = exp(-0.5 * ndist);
+          if (var_local) nrloc = nrloc * var_local[vl];
+          idx[base + cnt] = ob;
+          rloc[base + cnt] = nrloc;
+          rdiag[base + cnt] = oerr[ob] * oerr[ob] / nrloc;
+        }
+        cnt++;
+      }
+    }
+  }
+  if (!idx) nobsl[p] = cnt;
+}
+
+// common/common.f90:401-424 (pi and re of common/common.f90:28,35)
+__device__ __forceinline__ double distll(double alon, double alat, double blon, double blat) {
+  const double pi = 3.1415926535, re = 6371.3e3, r180 = 1.0 / 180.0;
+  const double lon1 = alon * pi * r180, lon2 = blon * pi * r180;
+  const double lat1 = alat * pi * r180, lat2 = blat * pi * r180;
+  double cosd = sin(lat1) * sin(lat2) + cos(lat1) * cos(lat2) * cos(lon2 - lon1);
+  cosd = fmin(1.0, cosd);
+  cosd = fmax(-1.0, cosd);
+  return acos(cosd) * re;
+}
+
+__device__ __forceinline__ int first_below(double x, const double* axis, int lim) {
+  for (int i = 1; i <= lim; i++)
+    if (x < axis[i]) return i;
+  return lim + 1;
+}
+
+struct SpeedyCtx {
+  int nlon, nlat;
+  const double *lon, *lat;
+  const int* G;
+  const double *elm, *olon, *olat, *olev, *odat, *oerr, *var_local;
+  double dist_zero, dist_zerov, sigma_obs, sigma_obsv;
+};
+
+// Test candidates [ib, ie] (1-based, inclusive) for one point; appends.
+__device__ __forceinline__ void speedy_range(const SpeedyCtx& c, int ib, int ie, double lon1, double lat1, int ilev,
+                                             double logpfm, int* idx, double* rloc, double* rdiag, int64_t base,
+                                             int& cnt) {
+  for (int ip = ib; ip <= ie; ip++) {
+    const int ob = ip - 1;
+    const int elm = (int)llround(c.elm[ob]);
+    double dlev;
+    if (elm == 14593 && ilev > 1) dlev = fabs(log(c.odat[ob]) - logpfm);
+    else if (elm != 14593) dlev = fabs(log(c.olev[ob]) - logpfm);
+    else dlev = 0.0;
+    if (dlev > c.dist_zerov) continue;
+    const double dist = distll(c.olon[ob], c.olat[ob], lon1, lat1);
+    if (dist > c.dist_zero) continue;
+    int iobs;
+    switch (elm) {
+      case 2819: iobs = 1; break;
+      case 2820: iobs = 2; break;
+      case 3073: iobs = 3; break;
+      case 3330: iobs = 4; break;
+      case 3331: iobs = 5; break;
+      case 14593: iobs = 6; break;
+      default: iobs = 7; break;
+    }
+    const double vl = c.var_local[iobs - 1];
+    if (vl < 2.2250738585072014e-308) continue;
+    if (idx) {
+      const double a = dist / c.sigma_obs, b = dlev / c.sigma_obsv;
+      idx[base + cnt] = ob;
+      rdiag[base + cnt] = c.oerr[ob] * c.oerr[ob];
+      rloc[base + cnt] = exp(-0.5 * (a * a + b * b)) * vl;
+    }
+    cnt++;
+  }
+}
+
+// speedy/letkf/letkf_tools.f90:575-603
+__device__ __forceinline__ void speedy_sub(const SpeedyCtx& c, int imin, int imax, int jmin, int jmax, double lon1,
+                                           double lat1, int ilev, double logpfm, int* idx, double* rloc,
+                                           double* rdiag, int64_t base, int& cnt) {
+  const int nlon = c.nlon;
+  for (int j = jmin; j <= jmax; j++) {
+    int ib;
+    if (imin > 1) ib = c.G[(size_t)(j - 1) * nlon + imin - 2] + 1;
+    else if (j > 1) ib = c.G[(size_t)(j - 2) * nlon + nlon - 1] + 1;
+    else ib = 1;
+    const int ie = c.G[(size_t)(j - 1) * nlon + imax - 1];
+    if (ie - ib + 1 == 0) continue;
+    speedy_range(c, ib, ie, lon1, lat1, ilev, logpfm, idx, rloc, rdiag, base, cnt);
+  }
+}
+
+__global__ void search_speedy_kernel(SpeedyCtx c, int npts, const double* __restrict__ plon,
+                                     const double* __restrict__ plat, const double* __restrict__ pdlon,
+                                     const int* __restrict__ pilev, const double* __restrict__ plogp, double dlat_zero,
+                                     const int64_t* __restrict__ offs, int* nobsl, int* idx, double* rloc,
+                                     double* rdiag) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npts) return;
+  const int nlon = c.nlon, nlat = c.nlat;
+  const double lon1 = plon[p], lat1 = plat[p], logpfm = plogp[p];
+  const int ilev = pilev[p];
+  double minlon = lon1 - pdlon[p], maxlon = lon1 + pdlon[p];
+  const double minlat = lat1 - dlat_zero, maxlat = lat1 + dlat_zero;
+  if (maxlon - minlon >= 360.0) {
+    minlon = 0.0;
+    maxlon = 360.0;
+  }
+  const int jmin = first_below(minlat, c.lat, nlat - 2);
+  const int jmax = first_below(maxlat, c.lat, nlat - 2);
+  const int64_t base = idx ? offs[p] : 0;
+  int cnt = 0, imin, imax;
+#define SUB(a, b) speedy_sub(c, (a), (b), jmin, jmax, lon1, lat1, ilev, logpfm, idx, rloc, rdiag, base, cnt)
+  if (minlon >= 0 && maxlon <= 360.0) {
+    imin = first_below(minlon, c.lon, nlon - 1);
+    imax = first_below(maxlon, c.lon, nlon - 1);
+    SUB(imin, imax);
+  } else if (minlon >= 0 && maxlon > 360.0) {
+    imin = first_below(minlon, c.lon, nlon - 1);
+    maxlon = maxlon - 360.0;
+    if (maxlon > 360.0) {
+      SUB(1, nlon);
+    } else {
+      imax = first_below(maxlon, c.lon, nlon - 1);
+      if (imax > imin) {
+        SUB(1, nlon);
+      } else {
+        SUB(1, imax);
+        imin = first_below(minlon, c.lon, nlon - 1);
+        SUB(imin, nlon);
+      }
+    }
+  } else if (minlon < 0 && maxlon <= 360.0) {
+    imax = first_below(maxlon, c.lon, nlon - 1);
+    minlon = minlon + 360.0;
+    if (minlon < 0) {
+      SUB(1, nlon);
+    } else {
+      imin = first_below(minlon, c.lon, nlon - 1);
+      if (imin < imax) {
+        SUB(1, nlon);
+      } else {
+        SUB(1, imax);
+        imin = first_below(minlon, c.lon, nlon - 1);
+        SUB(imin, nlon);
+      }
+    }
+  } else {
+    maxlon = maxlon - 360.0;
+    minlon = minlon + 360.0;
+    if (maxlon > 360.0 || minlon < 0) {
+      SUB(1, nlon);
+    } else {
+      imin = first_below(minlon, c.lon, nlon - 1);
+      imax = first_below(maxlon, c.lon, nlon - 1);
+      if (imin > imax) SUB(1, nlon);
+      else SUB(imin, imax);
+    }
+  }
+#undef SUB
+  if (!idx) nobsl[p] = cnt;
+}
+
+int launch_search_scale(int nlon, int nlat, const int* G, int nobs, const double* ori, const double* orj,
+                        const double* olev, const double* odat, const double* oerr, const int* ocls,
+                        const int* ovarloc, int npts, const double* pri, const double* prj, const double* prlev,
+                        const double* prz, const double* var_local, const double* params, const int64_t* offs,
+                        int* nobsl, int* idx, double* rloc, double* rdiag, cudaStream_t stream) {
+  if (npts <= 0) return npts == 0 ? LETKF_OK : LETKF_ERR_ARG;
+  ScaleParams P;
+  double* f = &P.dx;
+  for (int i = 0; i < 15; i++) f[i] = params[i];
+  const int bs = 128;
+  search_scale_kernel<<<(npts + bs - 1) / bs, bs, 0, stream>>>(nlon, nlat, G, nobs, ori, orj, olev, odat, oerr,
+                                                                 ocls, ovarloc, npts, pri, prj, prlev, prz,
+                                                                 var_local, P, offs, nobsl, idx, rloc, rdiag);
+  note_launch();
+  return cuda_status(cudaGetLastError());
+}
+
+int launch_search_speedy(int nlon, int nlat, const double* lon, const double* lat, const int* G, int nobs,
+                         const double* elm, const double* olon, const double* olat, const double* olev,
+                         const double* odat, const double* oerr, int npts, const double* plon, const double* plat,
+                         const double* pdlon, const int* pilev, const double* plogp, const double* var_local,
+                         const double* params, const int64_t* offs, int* nobsl, int* idx, double* rloc,
+                         double* rdiag, cudaStream_t stream) {
+  if (npts <= 0) return npts == 0 ? LETKF_OK : LETKF_ERR_ARG;
+  SpeedyCtx c;
+  c.nlon = nlon;
+  c.nlat = nlat;
+  c.lon = lon;
+  c.lat = lat;
+  c.G = G;
+  c.elm = elm;
+  c.olon = olon;
+  c.olat = olat;
+  c.olev = olev;
+  c.odat = odat;
+  c.oerr = oerr;
+  c.var_local = var_local;
+  c.dist_zero = params[0];
+  c.dist_zerov = params[1];
+  c.sigma_obs = params[3];
+  c.sigma_obsv = params[4];
+  (void)nobs;
+  const int bs = 128;
+  search_speedy_kernel<<<(npts + bs - 1) / bs, bs, 0, stream>>>(c, npts, plon, plat, pdlon, pilev, plogp, params[2],
+                                                                  offs, nobsl, idx, rloc, rdiag);
+  note_launch();
+  return cuda_status(cudaGetLastError());
+}
+
+// ---- exclusive scan of int32 counts into int64 offsets (three-phase) ----
+constexpr int SCAN_BS = 1024;
+
+__global__ void scan_blocks_kernel(int n, const int* __restrict__ in, int64_t* out, int64_t* bsum) {
+  __shared__ int64_t s[SCAN_BS];
+  const int i = blockIdx.x * SCAN_BS + threadIdx.x;
+  s[threadIdx.x] = i < n ? (int64_t)in[i] : 0;
+  __syncthreads();
+  for (int o = 1; o < SCAN_BS; o <<= 1) {
+    int64_t v = threadIdx.x >= o ? s[threadIdx.x - o] : 0;
+    __syncthreads();
+    s[threadIdx.x] += v;
+    __syncthreads();
+  }
+  if (i < n) out[i + 1] = s[threadIdx.x];  // inclusive into out[i+1]
+  if (threadIdx.x == SCAN_BS - 1) bsum[blockIdx.x] = s[threadIdx.x];
+}
+
+__global__ void scan_sums_kernel(int nb, int64_t* bsum) {
+  // single thread: nb is small (n / 1024)
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    int64_t run = 0;
+    for (int b = 0; b < nb; b++) {
+      int64_t v = bsum[b];
+      bsum[b] = run;
+      run += v;
+    }
+  }
+}
+
+__global__ void scan_add_kernel(int n, int64_t* out, const int64_t* bsum) {
+  const int i = blockIdx.x * SCAN_BS + threadIdx.x;
+  if (i < n) out[i + 1] += bsum[blockIdx.x];
+  if (i == 0) out[0] = 0;
+}
+
+int launch_exclusive_scan(int n, const int* counts, int64_t* offs, int64_t* scratch, cudaStream_t stream) {
+  if (n <= 0) {
+    cudaMemsetAsync(offs, 0, sizeof(int64_t), stream);
+    return LETKF_OK;
+  }
+  const int nb = (n + SCAN_BS - 1) / SCAN_BS;
+  scan_blocks_kernel<<<nb, SCAN_BS, 0, stream>>>(n, counts, offs, scratch);
+  scan_sums_kernel<<<1, 32, 0, stream>>>(nb, scratch);
+  scan_add_kernel<<<nb, SCAN_BS, 0, stream>>>(n, offs, scratch);
+  note_launch();
+  note_launch();
+  note_launch();
+  return cuda_status(cudaGetLastError());
+}
+
+template <typename T>
+__global__ void gather_rows_kernel(int ne, int64_t nrows, const int* __restrict__ idx, const T* __restrict__ ens,
+                                   const T* __restrict__ dep, T* rows_out, T* dep_out) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t tot = nrows * ne;
+  if (t < tot) {
+    const int64_t r = t / ne;
+    const int m = (int)(t - r * ne);
+    rows_out[t] = ens[(size_t)idx[r] * ne + m];
+    if (m == 0 && dep) dep_out[r] = dep[idx[r]];
+  }
+}
+
+int launch_gather_rows(int ne, int64_t nrows, const int* idx, const void* ens, const void* dep, int elem_bytes,
+                       void* rows_out, void* dep_out, cudaStream_t stream) {
+  if (nrows <= 0) return LETKF_OK;
+  const int64_t tot = nrows * ne;
+  const int bs = 256;
+  const unsigned grid = (unsigned)((tot + bs - 1) / bs);
+  if (elem_bytes == 8)
+    gather_rows_kernel<double><<<grid, bs, 0, stream>>>(ne, nrows, idx, (const double*)ens, (const double*)dep,
+                                                        (double*)rows_out, (double*)dep_out);
+  else if (elem_bytes == 4)
+    gather_rows_kernel<float><<<grid, bs, 0, stream>>>(ne, nrows, idx, (const float*)ens, (const float*)dep,
+                                                       (float*)rows_out, (float*)dep_out);
+  else
+    return LETKF_ERR_ARG;
+  note_launch();
+  return cuda_status(cudaGetLastError());
+}
+
+}  // namespace letkf
