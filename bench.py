@@ -1,0 +1,401 @@
+#!/usr/bin/env python
+"""Benchmark: LETKF grid-point analyses per second on one GB300 (per rank).
+
+Workload (per rank): the regional configuration -- 256 x 256 x 40 grid at
+3 km, 6 variables updated per point, k = 64 members stored FP32, 1e6
+clustered observations (0-2000 local obs per point).  One step = one full
+analysis sweep: local search, letkf_core and the update of every grid point
+(scale/letkf/letkf_tools.f90:38-476 with relax_beta = 1), mixed precision,
+one persistent CUDA launch.
+
+  value     device-resident throughput (points/s), CUDA events on the launch
+            stream, inputs (4 GB background ensemble) larger than L2
+  e2e       the same sweep through the public C ABI with pinned host buffers:
+            per step H2D of the background and the observations (sorted on the
+            device), the sweep, D2H of the analysis
+  fp64      the FP64 plain form on a strided subset of the same points
+  cpu_baseline  the CPU oracle (restatement of the reference path) on a
+            bounded sample of points with all host threads
+  error     analysis mean / spread RMS error of the mixed form against the
+            FP64 oracle on that sample, relative to the background spread
+
+``--impl reference`` times the CPU oracle alone (the reference arm).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "grid-point analyses/s"
+UNIT = "points/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nlon", type=int, default=256)
+    ap.add_argument("--nlat", type=int, default=256)
+    ap.add_argument("--nlev", type=int, default=40)
+    ap.add_argument("--ne", type=int, default=64)
+    ap.add_argument("--nobs", type=int, default=1_000_000)
+    ap.add_argument("--nv", type=int, default=6)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
+    ap.add_argument("--fp64-stride", type=int, default=64, help="FP64 plain form on every n-th point")
+    ap.add_argument("--no-extras", action="store_true", help="skip e2e, fp64, cpu baseline (profiling runs)")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ helpers
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                mx = float(r[1])
+            except (ValueError, IndexError):
+                continue
+            for k, nm in enumerate(names):
+                if len(r) > 4 + k and r[4 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def algorithmic_flops(nobsl, ne, nv):
+    """Per sweep: sum over points of 2 L k^2 + 2 L k + 9 k^3 + 2 k^3 + 4 k^2
+    (letkf_core; L > 0) + 2 V k^2 (update)."""
+    L = nobsl.astype(np.float64)
+    k = float(ne)
+    core = np.where(L > 0, 2 * L * k * k + 2 * L * k + 11 * k ** 3 + 4 * k * k, 0.0)
+    return float(core.sum() + nobsl.size * 2 * nv * k * k)
+
+
+def algorithmic_bytes(npts, nv, ne, nobs):
+    """Per sweep: ensemble read + write (FP32), obs ensemble + records once, FP64 mean."""
+    return float(npts * nv * ne * 8 + nobs * ne * 4 + nobs * 48 + npts * nv * 8)
+
+
+def load_traffic():
+    p = os.path.join(ROOT, "profiles", "sweep_mixed_traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f)
+    except OSError:
+        return None
+
+
+# --------------------------------------------------------------- CPU oracle
+def cpu_oracle_setup(wl, obs):
+    from oracle import oracle as O
+
+    hdxf, dep, dat = obs
+    perm, grd = O.scale_sort_obs(wl.nlon, wl.nlat, wl.ri, wl.rj)
+    n = perm.size
+    prm = wl.params
+    so = O.ScaleObs(wl.nlon, wl.nlat, grd, wl.ri[perm], wl.rj[perm], wl.lev[perm], dat[perm], wl.err[perm],
+                    wl.cls[perm], np.zeros(n), np.zeros(n), np.zeros(n), 1, 1, prm["dx"], prm["dy"], prm["dlon_zero"],
+                    prm["dlat_zero"], prm["sigma_obs"], prm["sigma_obsv"])
+    return so, np.ascontiguousarray(hdxf[perm], dtype=np.float64), np.ascontiguousarray(dep[perm])
+
+
+def cpu_oracle_run(wl, so, hd, dp, idx, nthreads, infl=1.0):
+    i, j, p = wl.points(idx)
+    xb = wl.background_numpy(idx).astype(np.float64)
+    t = time.perf_counter()
+    xa, inf, nl = so.sweep(hd, dp, xb, i, j, p, np.full(idx.size, infl), nthreads=nthreads)
+    return time.perf_counter() - t, xb, xa, inf, nl
+
+
+def sample_points(wl, n, seed=1):
+    rng = np.random.default_rng(seed)
+    return np.sort(rng.choice(wl.npts, size=min(n, wl.npts), replace=False))
+
+
+def run_reference(args, rank, world):
+    """Reference arm: the CPU oracle of the path on the host cores."""
+    if rank != 0:
+        return None
+    from letkf_gb300.workload import RegionalWorkload
+
+    wl = RegionalWorkload(args.seed, args.nlon, args.nlat, args.nlev, args.ne, args.nobs, args.nv)
+    obs = wl.obs_numpy()
+    so, hd, dp = cpu_oracle_setup(wl, obs)
+    nthreads = os.cpu_count() or 1
+    # size each step's sample from a probe so that a step takes about 1 s
+    probe = sample_points(wl, 64, seed=99)
+    dt, *_ = cpu_oracle_run(wl, so, hd, dp, probe, nthreads)
+    per_step = int(max(64, min(wl.npts, 64 * 1.0 / max(dt, 1e-6))))
+    times, npts_done = [], 0
+    for s in range(args.warmup + args.steps):
+        idx = sample_points(wl, per_step, seed=1000 + s)
+        dt, *_ = cpu_oracle_run(wl, so, hd, dp, idx, nthreads)
+        if s >= args.warmup:
+            times.append(dt)
+            npts_done += idx.size
+    tot = sum(times)
+    val = npts_done / tot
+    line = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": config_block(args, wl),
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": nthreads, "kind": "port",
+                             "sample": f"{per_step} random grid points per step of the {wl.npts}-point sweep"},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    return line
+
+
+def config_block(args, wl):
+    return {"workload": f"regional {args.nlon}x{args.nlat}x{args.nlev} (3 km), {args.nv} vars, k={args.ne}, "
+                        f"{args.nobs} clustered obs, sigma_h={wl.sigma_obs:.0f} m, sigma_v={wl.sigma_obsv} ln p",
+            "points_per_sweep": wl.npts, "ensemble": args.ne, "variables": args.nv, "observations": args.nobs,
+            "local_obs": "0-2000 per point", "form": "mixed (FP32 ensemble / Gram / Jacobi, FP64 mean)",
+            "l2": "inputs larger than L2 (background ensemble %.1f GB)" % (wl.npts * args.nv * args.ne * 4 / 1e9),
+            "parallelism": f"dp{args.gpus} (independent domains per GPU)"}
+
+
+# ----------------------------------------------------------------- GPU arm
+def run_gpu(args, rank, world, dist):
+    import torch
+
+    from letkf_gb300 import lib as L
+    from letkf_gb300.sweep import PREC_F64, PREC_MIXED, Sweep
+    from letkf_gb300.workload import RegionalWorkload
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    wl = RegionalWorkload(args.seed + rank, args.nlon, args.nlat, args.nlev, args.ne, args.nobs, args.nv)
+    hdxf, dep, dat = wl.obs_torch(dev)
+    xb = wl.background_torch(dev)
+    ri, rj, plev = wl.points()
+    sw = Sweep(args.ne, args.nv, args.nlon, args.nlat, wl.npts, wl.params, precision=PREC_MIXED)
+    sw.set_points(ri, rj, plev, tile=4)
+    sw.set_obs(wl.ri, wl.rj, wl.lev, dat, wl.err, dep, wl.cls, hdxf)
+    sw.set_background_device(xb.data_ptr())
+    infl0 = np.ones(wl.npts)
+    sw.set_inflation(infl0)
+    stream = torch.cuda.Stream(device=dev)
+    for _ in range(args.warmup):
+        sw.run(stream.cuda_stream)
+    torch.cuda.synchronize()
+    dg = sw.diagnostics()
+    nobsl = dg["nobsl"]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n0 = L.launch_count()
+    with ClockSampler(dev.index) as clk:
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            for _ in range(args.steps):
+                sw.run(stream.cuda_stream)
+            ev1.record(stream)
+        torch.cuda.synchronize()
+    launches = L.launch_count() - n0
+    t = ev0.elapsed_time(ev1) / 1e3
+    if dist:
+        tt = torch.tensor([t], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    value = world * wl.npts * args.steps / t
+    ms = 1e3 * t / args.steps
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded smooth random fields, clustered obs)",
+           "config": config_block(args, wl), "gpu_launches": int(launches), "clocks": clk.summary()}
+    # roofline of the dominant (only) kernel: sweep_mixed_kernel
+    peaks, src = measured_peaks()
+    flops = algorithmic_flops(nobsl, args.ne, args.nv)
+    ach = flops / (t / args.steps) / 1e12
+    pk = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
+    trf = load_traffic()
+    traffic = None
+    if trf and trf.get("per_point_bytes"):
+        traffic = trf["per_point_bytes"] * wl.npts
+    out["roofline"] = {"bound": "tensor", "kernel": "sweep_mixed_kernel", "achieved": ach, "peak": pk,
+                       "unit": "TFLOP/s", "frac": ach / pk, "traffic": traffic,
+                       "peak_source": f"bf16 dense sustained ({src})",
+                       "algorithmic_flops_per_launch": flops,
+                       "algorithmic_bytes_per_launch": algorithmic_bytes(wl.npts, args.nv, args.ne, args.nobs)}
+    clkmhz = out["clocks"]["sm_mhz"] or 1900.0
+    nsm = torch.cuda.get_device_properties(dev).multi_processor_count
+    fp32_peak = nsm * 128 * 2 * clkmhz * 1e6 / 1e12
+    out["roofline_fp32_simt"] = {"achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak,
+                                 "peak_source": f"{nsm} SMs x 128 FP32 lanes x 2 x median SM clock under load"}
+    nl = nobsl.astype(np.float64)
+    out["local_obs"] = {"min": int(nl.min()), "mean": float(nl.mean()), "p50": float(np.median(nl)),
+                        "p99": float(np.percentile(nl, 99)), "max": int(nl.max()), "zero_frac": float((nl == 0).mean())}
+    out["jacobi_sweeps"] = {"mean": float(dg["sweeps"][nobsl > 0].mean()) if (nobsl > 0).any() else 0.0,
+                            "max": int(dg["sweeps"].max())}
+    if args.no_extras:
+        return out, sw
+    # ---- e2e: host buffers through the C ABI ----
+    xb_host = torch.empty(xb.shape, dtype=torch.float32, pin_memory=True)
+    xb_host.copy_(xb)
+    xa_host = torch.empty_like(xb_host, pin_memory=True)
+    from letkf_gb300.sweep import _L
+    import ctypes as C
+
+    obs_bytes = args.nobs * (6 * 8 + 4 + args.ne * 4)
+    e2e_steps = max(2, min(args.steps, 5))
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        L.check(_L().letkf_sweep_set_background(sw.h, C.c_void_p(xb_host.data_ptr()), 0), "set_background")
+        sw.set_obs(wl.ri, wl.rj, wl.lev, dat, wl.err, dep, wl.cls, hdxf)
+        sw.run(stream.cuda_stream)
+        torch.cuda.synchronize()
+        sw.analysis_into(xa_host.data_ptr())
+    torch.cuda.synchronize()
+    te = time.perf_counter() - t0
+    if dist:
+        tt = torch.tensor([te], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        te = float(tt.item())
+    out["e2e"] = {"value": world * wl.npts * e2e_steps / te, "unit": UNIT, "steps": e2e_steps,
+                  "h2d_bytes_per_step": int(xb.numel() * 4 + obs_bytes), "d2h_bytes_per_step": int(xb.numel() * 4)}
+    if rank != 0:
+        return out, sw
+    # ---- error vs the FP64 oracle on a sample, from a fresh inflation field ----
+    sw.set_background_device(xb.data_ptr())
+    sw.set_inflation(infl0)
+    sw.run(stream.cuda_stream)
+    torch.cuda.synchronize()
+    xa = sw.analysis()
+    so, hd, dp = cpu_oracle_setup(wl, (hdxf, dep, dat))
+    nthreads = os.cpu_count() or 1
+    probe = sample_points(wl, 64, seed=99)
+    dtp, *_ = cpu_oracle_run(wl, so, hd, dp, probe, nthreads)
+    nsample = int(max(256, min(16384, 64 * args.cpu_seconds / max(dtp, 1e-6))))
+    idx = sample_points(wl, nsample, seed=7)
+    dtc, xb_s, xa_ref, inf_ref, nl_ref = cpu_oracle_run(wl, so, hd, dp, idx, nthreads)
+    out["cpu_baseline"] = {"value": idx.size / dtc, "unit": UNIT, "cores": nthreads, "kind": "port",
+                           "sample": f"{idx.size} random grid points of the {wl.npts}-point sweep "
+                                     f"({dtc:.1f} s, OpenMP dynamic over points)"}
+    xg = xa[:, idx, :].astype(np.float64)
+    spread = np.sqrt(((xb_s - xb_s.mean(-1, keepdims=True)) ** 2).sum(-1) / (args.ne - 1)).mean()
+    em = float(np.sqrt(np.mean((xg.mean(-1) - xa_ref.mean(-1)) ** 2)) / spread)
+    pert = lambda x: x - x.mean(-1, keepdims=True)
+    ep = float(np.sqrt(np.mean((pert(xg) - pert(xa_ref)) ** 2)) / spread)
+    sa = lambda x: np.sqrt((pert(x) ** 2).sum(-1) / (args.ne - 1))
+    es = float(np.sqrt(np.mean((sa(xg) - sa(xa_ref)) ** 2)) / spread)
+    dgi = sw.diagnostics()
+    out["error_vs_fp64_oracle"] = {"analysis_mean_rms_over_spread": em, "perturbation_rms_over_spread": ep,
+                                   "analysis_spread_rms_over_spread": es,
+                                   "nobsl_bit_exact": bool((dgi["nobsl"][idx] == nl_ref).all()),
+                                   "infl_max_rel": float(np.max(np.abs(dgi["infl"][idx] - inf_ref) / inf_ref)),
+                                   "sample_points": int(idx.size), "target": 1e-4}
+    # ---- FP64 plain form on a strided subset ----
+    sub = np.arange(0, wl.npts, args.fp64_stride)
+    si, sj, sp = wl.points(sub)
+    s64 = Sweep(args.ne, args.nv, args.nlon, args.nlat, sub.size, wl.params, precision=PREC_F64)
+    s64.set_points(si, sj, sp, tile=0)
+    s64.set_obs(wl.ri, wl.rj, wl.lev, dat, wl.err, dep, wl.cls, hdxf.astype(np.float64))
+    s64.set_background(xb[:, torch.as_tensor(sub, device=dev), :].double().cpu().numpy())
+    s64.set_inflation(np.ones(sub.size))
+    s64.run()
+    torch.cuda.synchronize()
+    s64.set_inflation(np.ones(sub.size))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    s64.run(torch.cuda.current_stream().cuda_stream)
+    e1.record()
+    torch.cuda.synchronize()
+    t64 = e0.elapsed_time(e1) / 1e3
+    v64 = sub.size / t64
+    out["fp64_plain"] = {"value": v64, "unit": UNIT, "sample": f"every {args.fp64_stride}th point ({sub.size} points)",
+                         "mixed_over_fp64": (value / world) / v64}
+    s64.close()
+    return out, sw
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+
+        backend = "gloo" if args.impl == "reference" else "nccl"
+        if args.impl != "reference":
+            import torch
+
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        tdist.init_process_group(backend)
+        dist = tdist
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+    else:
+        line, sw = run_gpu(args, rank, world, dist)
+        sw.close()
+    if rank == 0 and line is not None:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

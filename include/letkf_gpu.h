@@ -122,6 +122,64 @@ int letkf_search_speedy(int nlon, int nlat, const double* lon, const double* lat
                         const double* var_local_row, const double* params, const int64_t* offs,
                         int* nobsl, int* idx, double* rloc, double* rdiag, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Analysis sweep with the ensemble resident on the device.  Replaces the
+ * das_letkf grid loop of the SCALE-style drivers (scale/letkf/letkf_tools.f90:
+ * 38-476: obs_local + letkf_core(..., transm=, rdiag_wloc=.true., minfl=) +
+ * the ensemble update with beta = 1) and the MPI scatter / gather around it
+ * (scale/common/common_mpi_scale.f90): one handle owns the points, the
+ * bucket-sorted observations (scale/letkf/letkf_obs.f90:735-830, sorted on
+ * the device), the background and analysis ensembles and the inflation field.
+ * Calls on one handle are serialised by the caller; distinct handles are
+ * independent.
+ * ---------------------------------------------------------------------- */
+#define LETKF_PREC_F64 0   /* FP64 plain form */
+#define LETKF_PREC_MIXED 1 /* FP32 ensemble, fused mixed-precision sweep */
+
+#define LETKF_OPT_GRID_CAP 1   /* cap on the persistent grid (0 = #SM x occupancy) */
+#define LETKF_OPT_MAX_SWEEPS 2 /* Jacobi sweep limit of the mixed form (default 12) */
+
+typedef struct letkf_sweep_desc {
+  int ne;           /* ensemble size (MEMBER) */
+  int nv;           /* variables updated with each point's weights (1..8) */
+  int nlon, nlat;   /* observation bucket grid (grid-index space, 1-based cells) */
+  int npts;         /* analysed grid points */
+  int precision;    /* LETKF_PREC_F64 or LETKF_PREC_MIXED */
+  double params[16];/* SCALE search parameters in the order of letkf_search_scale */
+  double minfl;     /* INFL_MUL_MIN; <= 0 absent */
+} letkf_sweep_desc;
+
+typedef struct letkf_sweep_s* letkf_sweep_t;
+
+int letkf_sweep_create(letkf_sweep_t* h, const letkf_sweep_desc* desc);
+int letkf_sweep_destroy(letkf_sweep_t h);
+/* grid points (host arrays [npts]): ri, rj grid coordinates, rlev pressure,
+ * rz height (may be NULL); tile > 0 orders processing in tile x tile columns */
+int letkf_sweep_set_points(letkf_sweep_t h, const double* ri, const double* rj, const double* rlev,
+                           const double* rz, int tile);
+/* observations (host, unsorted, QC-passed): grid coordinates, level, value,
+ * error, departure, class (see letkf_search_scale), var_local column and row
+ * (NULL: no variable localisation) and the obs-space perturbations
+ * hdxf[nobs][ne] (float32 when hdxf_f32, else float64) */
+int letkf_sweep_set_obs(letkf_sweep_t h, int nobs, const double* ri, const double* rj, const double* lev,
+                        const double* dat, const double* err, const double* dep, const int* cls,
+                        const int* varloc, const double* var_local_row, int nvarloc, const void* hdxf,
+                        int hdxf_f32);
+/* background members xb[nv][npts][ne] (float64 for LETKF_PREC_F64, float32
+ * for LETKF_PREC_MIXED); host or device pointer */
+int letkf_sweep_set_background(letkf_sweep_t h, const void* xb, int on_device);
+int letkf_sweep_set_inflation(letkf_sweep_t h, const double* infl, int on_device);
+int letkf_sweep_set_option(letkf_sweep_t h, int option, int value);
+/* analyse every point; asynchronous on `stream` (NULL: the handle's stream) */
+int letkf_sweep_run(letkf_sweep_t h, void* stream);
+int letkf_sweep_get_analysis(letkf_sweep_t h, void* xa, int on_device);
+/* per-point updated inflation, local obs count, status and Jacobi sweeps (any may be NULL) */
+int letkf_sweep_get_diagnostics(letkf_sweep_t h, double* infl, int* nobsl, int* status, int* sweeps);
+/* the device-side nobsgrd table [(nlon+1)*nlat] after set_obs */
+int letkf_sweep_sorted_obs(letkf_sweep_t h, int* nobsgrd);
+/* device pointers of the resident buffers (for callers that stage data themselves) */
+int letkf_sweep_device_buffers(letkf_sweep_t h, void** xb, void** xa, double** infl, int** nobsl);
+
 /* exclusive scan of n int32 counts into int64 offsets[n+1] (device) */
 int letkf_exclusive_scan(int n, const int* counts, int64_t* offs, void* stream);
 

@@ -38,11 +38,13 @@ template <int NP>
 struct MixedSmem {
   static constexpr int CH = MixedCfg<NP>::CH;
   static constexpr int NBLK = (NP / 2) * (NP / 2 + 1) / 2;  // upper 2x2 blocks incl. diagonal
+  // Y / YW (staged rows, Gram phase only) share V's space when they fit
+  static constexpr bool ALIAS = 2 * CH * NP <= NP * NP;
   static constexpr int A = 0;                       // NP*NP row-major work matrix
   static constexpr int V = A + NP * NP;             // NP*NP eigenvectors, column-major V[q*NP+i]
-  static constexpr int Y = V + NP * NP;             // CH*NP staged rows
+  static constexpr int Y = ALIAS ? V : V + NP * NP; // CH*NP staged rows
   static constexpr int YW = Y + CH * NP;            // CH*NP weighted rows
-  static constexpr int B = YW + CH * NP;            // NP  departure product
+  static constexpr int B = ALIAS ? V + NP * NP : YW + CH * NP;  // NP departure product
   static constexpr int LAM = B + NP;                // NP  eigenvalues
   static constexpr int FQ = LAM + NP;               // NP  sqrt((k-1)/lambda)
   static constexpr int IQ = FQ + NP;                // NP  1/lambda

@@ -1,0 +1,526 @@
+// sweep.cu -- handle-based analysis sweep with the ensemble resident on the device.
+//
+// Replaces the das_letkf driver loop of the SCALE-style models
+// (scale/letkf/letkf_tools.f90:38-476) for one GPU: observations are sorted
+// into grid cells on the device (scale/letkf/letkf_obs.f90:735-830), every
+// grid point is searched and analysed, and the ensemble is updated in place of
+// the MPI scatter / gather (scale/common/common_mpi_scale.f90).  Two forms:
+//   LETKF_PREC_F64    plain form: search -> packed local rows -> FP64 core ->
+//                     FP64 update, in point chunks (scratch sized per chunk);
+//   LETKF_PREC_MIXED  one fused persistent launch (sweep_mixed.cu).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "letkf_common.cuh"
+
+namespace letkf {
+
+struct SweepScaleParams;
+struct SweepArgs;
+int launch_sweep_mixed(const SweepArgs& a, cudaStream_t stream, int grid_cap);
+int launch_sweep_prep_obs(int, const double*, const double*, const double*, const double*, const double*,
+                          const double*, const int*, const int*, const double*, const double*, float4*, float4*, int*,
+                          cudaStream_t);
+int launch_search_scale(int, int, const int*, int, const double*, const double*, const double*, const double*,
+                        const double*, const int*, const int*, int, const double*, const double*, const double*,
+                        const double*, const double*, const double*, const int64_t*, int*, int*, double*, double*,
+                        cudaStream_t);
+int launch_exclusive_scan(int, const int*, int64_t*, int64_t*, cudaStream_t);
+int launch_core_f64(int, int, const int64_t*, const double*, const double*, const double*, const double*, double*,
+                    double*, double*, double*, int, double, int*, cudaStream_t);
+int launch_update_f64_range(int ne, int npts_total, int p0, int cnt, int nv, const double* xb, const double* trans,
+                            const double* transm, double* xa, cudaStream_t stream);
+
+}  // namespace letkf
+
+// full definitions needed here
+#include "sweep_args.cuh"
+
+namespace letkf {
+
+// ---- device bucket sort of observations (stable) ----
+__global__ void obs_cell_kernel(int nobs, int nlon, int nlat, int ihalo, int jhalo, const double* __restrict__ ri,
+                                const double* __restrict__ rj, int* cell, int* counts) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nobs) return;
+  int i = (int)ceil(ri[n] - 0.5) - ihalo, j = (int)ceil(rj[n] - 0.5) - jhalo;
+  i = min(max(i, 1), nlon);
+  j = min(max(j, 1), nlat);
+  const int c = (j - 1) * nlon + (i - 1);
+  cell[n] = c;
+  atomicAdd(&counts[c], 1);
+}
+
+__global__ void obs_scatter_kernel(int nobs, const int* __restrict__ cell, const int64_t* __restrict__ start,
+                                   int* cursor, int* perm) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nobs) return;
+  const int c = cell[n];
+  const int pos = (int)start[c] + atomicAdd(&cursor[c], 1);
+  perm[pos] = n;
+}
+
+// restore input order inside each cell (insertion sort of a short segment)
+__global__ void obs_stabilize_kernel(int ncell, const int64_t* __restrict__ start, int* perm) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncell) return;
+  const int b = (int)start[c], e = (int)start[c + 1];
+  for (int i = b + 1; i < e; i++) {
+    const int v = perm[i];
+    int k = i - 1;
+    while (k >= b && perm[k] > v) {
+      perm[k + 1] = perm[k];
+      k--;
+    }
+    perm[k + 1] = v;
+  }
+}
+
+// nobsgrd(0:nlon, 1:nlat) from the exclusive cell starts (letkf_obs.f90:765-774)
+__global__ void obs_grd_kernel(int nlon, int nlat, const int64_t* __restrict__ start, int* G) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ld = nlon + 1;
+  if (t >= ld * nlat) return;
+  const int j = t / ld, i = t - j * ld;  // j 0-based row, i = 0..nlon
+  G[t] = (int)start[j * nlon + i];       // cumulative count before cell (i+1, j+1) == through cell (i, j+1)
+}
+
+template <typename T>
+__global__ void permute_kernel(int n, int width, const int* __restrict__ perm, const T* __restrict__ src, T* dst) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)n * width) return;
+  const int64_t r = t / width;
+  const int c = (int)(t - r * width);
+  dst[t] = src[(int64_t)perm[r] * width + c];
+}
+
+template <typename T>
+static void permute(int n, int width, const int* perm, const T* src, T* dst, cudaStream_t s) {
+  if (n <= 0) return;
+  const int64_t tot = (int64_t)n * width;
+  permute_kernel<T><<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, width, perm, src, dst);
+  note_launch();
+}
+
+__global__ void f64_to_f32_kernel(int64_t n, const double* __restrict__ a, float* b) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) b[t] = (float)a[t];
+}
+
+}  // namespace letkf
+
+using namespace letkf;
+
+struct letkf_sweep_s {
+  letkf_sweep_desc d;
+  int nobs = 0;
+  // points
+  double *pri = nullptr, *prj = nullptr, *prlev = nullptr, *prz = nullptr;
+  int* order = nullptr;
+  // sorted observations
+  double *ori = nullptr, *orj = nullptr, *olev = nullptr, *odat = nullptr, *oerr = nullptr, *odep = nullptr;
+  int *ocls = nullptr, *ovarloc = nullptr, *G = nullptr;
+  double* var_local = nullptr;
+  float4 *obsF = nullptr, *obsA = nullptr;
+  int* meta = nullptr;
+  float* ens32 = nullptr;
+  double* ens64 = nullptr;
+  // ensemble
+  void *xb = nullptr, *xa = nullptr;
+  double* infl = nullptr;
+  int *status = nullptr, *nobsl = nullptr, *sweeps = nullptr, *counter = nullptr;
+  cudaStream_t stream = nullptr;
+  int grid_cap = 0;
+  int max_sweeps = 12;
+};
+
+static void dfree(void* p) {
+  if (p) cudaFree(p);
+}
+
+template <typename T>
+static int dalloc(T** p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  return cudaMalloc((void**)p, n * sizeof(T)) == cudaSuccess ? LETKF_OK : LETKF_ERR_CUDA;
+}
+
+static size_t elem(const letkf_sweep_s* h) { return h->d.precision == LETKF_PREC_F64 ? 8 : 4; }
+
+extern "C" {
+
+int letkf_sweep_create(letkf_sweep_t* out, const letkf_sweep_desc* d) {
+  if (!out || !d) return LETKF_ERR_ARG;
+  *out = nullptr;
+  if (d->ne < 2 || d->nv < 1 || d->nv > 8 || d->nlon < 1 || d->nlat < 1 || d->npts < 0) return LETKF_ERR_ARG;
+  if (d->precision != LETKF_PREC_F64 && d->precision != LETKF_PREC_MIXED) return LETKF_ERR_ARG;
+  if (d->ne > LETKF_MAX_NE) return LETKF_ERR_CAPACITY;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return LETKF_ERR_NOGPU;
+  }
+  letkf_sweep_s* h = new letkf_sweep_s();
+  h->d = *d;
+  const size_t np = (size_t)d->npts;
+  int st = LETKF_OK;
+  st |= dalloc(&h->pri, np);
+  st |= dalloc(&h->prj, np);
+  st |= dalloc(&h->prlev, np);
+  st |= dalloc(&h->prz, np);
+  st |= dalloc(&h->order, np);
+  st |= dalloc((char**)&h->xb, np * d->nv * d->ne * elem(h));
+  st |= dalloc((char**)&h->xa, np * d->nv * d->ne * elem(h));
+  st |= dalloc(&h->infl, np);
+  st |= dalloc(&h->status, np);
+  st |= dalloc(&h->nobsl, np);
+  st |= dalloc(&h->sweeps, np);
+  st |= dalloc(&h->counter, 1);
+  st |= dalloc(&h->G, (size_t)(d->nlon + 1) * d->nlat);
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) st = LETKF_ERR_CUDA;
+  if (st != LETKF_OK) {
+    letkf_sweep_destroy(h);
+    return LETKF_ERR_CUDA;
+  }
+  cudaMemset(h->prz, 0, np * sizeof(double));
+  cudaMemset(h->G, 0, sizeof(int) * (d->nlon + 1) * d->nlat);
+  std::vector<double> one(np, 1.0);
+  cudaMemcpy(h->infl, one.data(), np * sizeof(double), cudaMemcpyHostToDevice);
+  *out = h;
+  return cuda_status(cudaGetLastError());
+}
+
+int letkf_sweep_destroy(letkf_sweep_t h) {
+  if (!h) return LETKF_OK;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  void* ptrs[] = {h->pri,  h->prj,   h->prlev, h->prz,   h->order, h->ori,     h->orj,    h->olev,
+                  h->odat, h->oerr,  h->odep,  h->ocls,  h->ovarloc, h->G,     h->var_local, h->obsF,
+                  h->obsA, h->meta,  h->ens32, h->ens64, h->xb,    h->xa,      h->infl,   h->status,
+                  h->nobsl, h->sweeps, h->counter};
+  for (void* p : ptrs) dfree(p);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return LETKF_OK;
+}
+
+int letkf_sweep_set_points(letkf_sweep_t h, const double* ri, const double* rj, const double* rlev, const double* rz,
+                           int tile) {
+  if (!h || !ri || !rj || !rlev) return LETKF_ERR_ARG;
+  const int np = h->d.npts;
+  for (int p = 0; p < np; p++)
+    if (!(rlev[p] > 0.0)) return LETKF_ERR_ARG;
+  // processing order: column tiles of tile x tile cells, input order inside a tile
+  std::vector<int> order(np);
+  std::iota(order.begin(), order.end(), 0);
+  if (tile > 0) {
+    std::vector<int64_t> key(np);
+    const int64_t ntx = (h->d.nlon + tile - 1) / tile + 1;
+    for (int p = 0; p < np; p++) {
+      const int64_t ti = (int64_t)std::floor((ri[p] - 0.5) / tile), tj = (int64_t)std::floor((rj[p] - 0.5) / tile);
+      key[p] = (tj + 1) * (ntx + 1) + (ti + 1);
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key[a] < key[b]; });
+  }
+  cudaStream_t s = h->stream;
+  cudaMemcpyAsync(h->pri, ri, sizeof(double) * np, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(h->prj, rj, sizeof(double) * np, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(h->prlev, rlev, sizeof(double) * np, cudaMemcpyHostToDevice, s);
+  if (rz) cudaMemcpyAsync(h->prz, rz, sizeof(double) * np, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(h->order, order.data(), sizeof(int) * np, cudaMemcpyHostToDevice, s);
+  return cuda_status(cudaStreamSynchronize(s));
+}
+
+int letkf_sweep_set_obs(letkf_sweep_t h, int nobs, const double* ri, const double* rj, const double* lev,
+                        const double* dat, const double* err, const double* dep, const int* cls, const int* varloc,
+                        const double* var_local_row, int nvarloc, const void* hdxf, int hdxf_f32) {
+  if (!h || nobs < 0) return LETKF_ERR_ARG;
+  if (nobs > 0 && (!ri || !rj || !lev || !dat || !err || !dep || !cls || !hdxf)) return LETKF_ERR_ARG;
+  if (var_local_row && (!varloc || nvarloc < 1)) return LETKF_ERR_ARG;
+  if (varloc)
+    for (int i = 0; i < nobs; i++)
+      if (varloc[i] < 0 || (var_local_row && varloc[i] >= nvarloc)) return LETKF_ERR_ARG;
+  for (int i = 0; i < nobs; i++)
+    if (cls[i] < 0 || cls[i] > 6) return LETKF_ERR_ARG;
+  const int ne = h->d.ne, nlon = h->d.nlon, nlat = h->d.nlat;
+  cudaStream_t s = h->stream;
+  void* old[] = {h->ori, h->orj, h->olev, h->odat, h->oerr, h->odep, h->ocls, h->ovarloc, h->var_local,
+                 h->obsF, h->obsA, h->meta, h->ens32, h->ens64};
+  cudaStreamSynchronize(s);
+  for (void* p : old) dfree(p);
+  h->ori = h->orj = h->olev = h->odat = h->oerr = h->odep = nullptr;
+  h->ocls = h->ovarloc = h->meta = nullptr;
+  h->var_local = nullptr;
+  h->obsF = h->obsA = nullptr;
+  h->ens32 = nullptr;
+  h->ens64 = nullptr;
+  h->nobs = nobs;
+  const size_t n = (size_t)nobs;
+  int st = LETKF_OK;
+  st |= dalloc(&h->ori, n);
+  st |= dalloc(&h->orj, n);
+  st |= dalloc(&h->olev, n);
+  st |= dalloc(&h->odat, n);
+  st |= dalloc(&h->oerr, n);
+  st |= dalloc(&h->odep, n);
+  st |= dalloc(&h->ocls, n);
+  st |= dalloc(&h->ovarloc, n);
+  st |= dalloc(&h->obsF, n);
+  st |= dalloc(&h->obsA, n);
+  st |= dalloc(&h->meta, n);
+  if (h->d.precision == LETKF_PREC_MIXED) st |= dalloc(&h->ens32, n * ne);
+  else st |= dalloc(&h->ens64, n * ne);
+  if (var_local_row) st |= dalloc(&h->var_local, (size_t)nvarloc);
+  if (st != LETKF_OK) return LETKF_ERR_CUDA;
+  if (var_local_row)
+    cudaMemcpyAsync(h->var_local, var_local_row, sizeof(double) * nvarloc, cudaMemcpyHostToDevice, s);
+  if (nobs == 0) {
+    cudaMemsetAsync(h->G, 0, sizeof(int) * (nlon + 1) * nlat, s);
+    return cuda_status(cudaStreamSynchronize(s));
+  }
+  // staging of the unsorted records
+  double *t_ri, *t_rj, *t_lev, *t_dat, *t_err, *t_dep;
+  int *t_cls, *t_vl, *cell, *counts, *cursor, *perm;
+  int64_t *start, *scr;
+  void* t_ens;
+  const size_t es = hdxf_f32 ? 4 : 8;
+  const int ncell = nlon * nlat;
+  st |= dalloc(&t_ri, n);
+  st |= dalloc(&t_rj, n);
+  st |= dalloc(&t_lev, n);
+  st |= dalloc(&t_dat, n);
+  st |= dalloc(&t_err, n);
+  st |= dalloc(&t_dep, n);
+  st |= dalloc(&t_cls, n);
+  st |= dalloc(&t_vl, n);
+  st |= dalloc(&cell, n);
+  st |= dalloc(&perm, n);
+  st |= dalloc(&counts, (size_t)ncell);
+  st |= dalloc(&cursor, (size_t)ncell);
+  st |= dalloc(&start, (size_t)ncell + 1);
+  st |= dalloc(&scr, (size_t)ncell / 1024 + 2);
+  st |= dalloc((char**)&t_ens, n * ne * es);
+  if (st != LETKF_OK) return LETKF_ERR_CUDA;
+  cudaMemcpyAsync(t_ri, ri, 8 * n, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(t_rj, rj, 8 * n, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(t_lev, lev, 8 * n, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(t_dat, dat, 8 * n, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(t_err, err, 8 * n, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(t_dep, dep, 8 * n, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(t_cls, cls, 4 * n, cudaMemcpyHostToDevice, s);
+  if (varloc) cudaMemcpyAsync(t_vl, varloc, 4 * n, cudaMemcpyHostToDevice, s);
+  else cudaMemsetAsync(t_vl, 0, 4 * n, s);
+  cudaMemcpyAsync(t_ens, hdxf, n * ne * es, cudaMemcpyHostToDevice, s);
+  cudaMemsetAsync(counts, 0, sizeof(int) * ncell, s);
+  cudaMemsetAsync(cursor, 0, sizeof(int) * ncell, s);
+  const unsigned gb = (unsigned)((n + 255) / 256);
+  obs_cell_kernel<<<gb, 256, 0, s>>>(nobs, nlon, nlat, 0, 0, t_ri, t_rj, cell, counts);
+  note_launch();
+  launch_exclusive_scan(ncell, counts, start, scr, s);
+  obs_scatter_kernel<<<gb, 256, 0, s>>>(nobs, cell, start, cursor, perm);
+  obs_stabilize_kernel<<<(ncell + 255) / 256, 256, 0, s>>>(ncell, start, perm);
+  obs_grd_kernel<<<((nlon + 1) * nlat + 255) / 256, 256, 0, s>>>(nlon, nlat, start, h->G);
+  note_launch();
+  note_launch();
+  note_launch();
+  permute<double>(nobs, 1, perm, t_ri, h->ori, s);
+  permute<double>(nobs, 1, perm, t_rj, h->orj, s);
+  permute<double>(nobs, 1, perm, t_lev, h->olev, s);
+  permute<double>(nobs, 1, perm, t_dat, h->odat, s);
+  permute<double>(nobs, 1, perm, t_err, h->oerr, s);
+  permute<double>(nobs, 1, perm, t_dep, h->odep, s);
+  permute<int>(nobs, 1, perm, t_cls, h->ocls, s);
+  permute<int>(nobs, 1, perm, t_vl, h->ovarloc, s);
+  if (h->d.precision == LETKF_PREC_MIXED) {
+    if (hdxf_f32) {
+      permute<float>(nobs, ne, perm, (const float*)t_ens, h->ens32, s);
+    } else {
+      float* tmp;
+      dalloc(&tmp, n * ne);
+      f64_to_f32_kernel<<<(unsigned)((n * ne + 255) / 256), 256, 0, s>>>((int64_t)(n * ne), (const double*)t_ens,
+                                                                         tmp);
+      note_launch();
+      permute<float>(nobs, ne, perm, tmp, h->ens32, s);
+      cudaStreamSynchronize(s);
+      cudaFree(tmp);
+    }
+  } else {
+    if (hdxf_f32) return LETKF_ERR_ARG;
+    permute<double>(nobs, ne, perm, (const double*)t_ens, h->ens64, s);
+  }
+  launch_sweep_prep_obs(nobs, h->ori, h->orj, h->olev, h->odat, h->oerr, h->odep, h->ocls, h->ovarloc, h->var_local,
+                        h->d.params, h->obsF, h->obsA, h->meta, s);
+  cudaError_t e = cudaStreamSynchronize(s);
+  void* tmpb[] = {t_ri, t_rj, t_lev, t_dat, t_err, t_dep, t_cls, t_vl, cell, perm, counts, cursor, start, scr, t_ens};
+  for (void* p : tmpb) cudaFree(p);
+  return cuda_status(e);
+}
+
+int letkf_sweep_set_background(letkf_sweep_t h, const void* xb, int on_device) {
+  if (!h || !xb) return LETKF_ERR_ARG;
+  const size_t bytes = (size_t)h->d.npts * h->d.nv * h->d.ne * elem(h);
+  cudaMemcpyAsync(h->xb, xb, bytes, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream);
+  return cuda_status(cudaStreamSynchronize(h->stream));
+}
+
+int letkf_sweep_set_inflation(letkf_sweep_t h, const double* infl, int on_device) {
+  if (!h || !infl) return LETKF_ERR_ARG;
+  cudaMemcpyAsync(h->infl, infl, sizeof(double) * h->d.npts,
+                  on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream);
+  return cuda_status(cudaStreamSynchronize(h->stream));
+}
+
+int letkf_sweep_device_buffers(letkf_sweep_t h, void** xb, void** xa, double** infl, int** nobsl) {
+  if (!h) return LETKF_ERR_ARG;
+  if (xb) *xb = h->xb;
+  if (xa) *xa = h->xa;
+  if (infl) *infl = h->infl;
+  if (nobsl) *nobsl = h->nobsl;
+  return LETKF_OK;
+}
+
+int letkf_sweep_set_option(letkf_sweep_t h, int option, int value) {
+  if (!h) return LETKF_ERR_ARG;
+  switch (option) {
+    case LETKF_OPT_GRID_CAP: h->grid_cap = value; return LETKF_OK;
+    case LETKF_OPT_MAX_SWEEPS:
+      if (value < 1 || value > 64) return LETKF_ERR_ARG;
+      h->max_sweeps = value;
+      return LETKF_OK;
+    default: return LETKF_ERR_ARG;
+  }
+}
+
+static int run_f64(letkf_sweep_t h, cudaStream_t s) {
+  // plain form in chunks of points: search (count, scan, fill), gather, core, update
+  const int ne = h->d.ne, nv = h->d.nv, np = h->d.npts, nobs = h->nobs;
+  const int chunk = std::min(np, 16384);
+  int *cnt, *idx = nullptr;
+  int64_t *offs, *scr;
+  double *rloc = nullptr, *rdiag = nullptr, *rows = nullptr, *dep = nullptr, *trans, *transm;
+  int st = LETKF_OK;
+  st |= dalloc(&cnt, (size_t)chunk);
+  st |= dalloc(&offs, (size_t)chunk + 1);
+  st |= dalloc(&scr, (size_t)chunk / 1024 + 2);
+  st |= dalloc(&trans, (size_t)chunk * ne * ne);
+  st |= dalloc(&transm, (size_t)chunk * ne);
+  if (st != LETKF_OK) return LETKF_ERR_CUDA;
+  size_t cap = 0;
+  for (int p0 = 0; p0 < np && st == LETKF_OK; p0 += chunk) {
+    const int c = std::min(chunk, np - p0);
+    st = launch_search_scale(h->d.nlon, h->d.nlat, h->G, nobs, h->ori, h->orj, h->olev, h->odat, h->oerr, h->ocls,
+                             h->ovarloc, c, h->pri + p0, h->prj + p0, h->prlev + p0, h->prz + p0, h->var_local,
+                             h->d.params, nullptr, cnt, nullptr, nullptr, nullptr, s);
+    if (st) break;
+    st = launch_exclusive_scan(c, cnt, offs, scr, s);
+    int64_t total = 0;
+    cudaMemcpyAsync(&total, offs + c, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    cudaMemcpyAsync(h->nobsl + p0, cnt, sizeof(int) * c, cudaMemcpyDeviceToDevice, s);
+    if ((size_t)total > cap) {
+      cudaStreamSynchronize(s);
+      dfree(idx);
+      dfree(rloc);
+      dfree(rdiag);
+      dfree(rows);
+      dfree(dep);
+      cap = (size_t)total + (size_t)total / 4 + 1024;
+      st |= dalloc(&idx, cap);
+      st |= dalloc(&rloc, cap);
+      st |= dalloc(&rdiag, cap);
+      st |= dalloc(&rows, cap * ne);
+      st |= dalloc(&dep, cap);
+      if (st) break;
+    }
+    st = launch_search_scale(h->d.nlon, h->d.nlat, h->G, nobs, h->ori, h->orj, h->olev, h->odat, h->oerr, h->ocls,
+                             h->ovarloc, c, h->pri + p0, h->prj + p0, h->prlev + p0, h->prz + p0, h->var_local,
+                             h->d.params, offs, cnt, idx, rloc, rdiag, s);
+    if (st) break;
+    if (total > 0) {
+      extern int launch_gather_rows(int, int64_t, const int*, const void*, const void*, int, void*, void*,
+                                    cudaStream_t);
+      st = launch_gather_rows(ne, total, idx, h->ens64, h->odep, 8, rows, dep, s);
+      if (st) break;
+    }
+    // SCALE convention: rdiag = err^2 / rloc with rdiag_wloc (letkf_tools.f90:199-206)
+    st = launch_core_f64(ne, c, offs, rows, rdiag, rloc, dep, h->infl + p0, trans, transm, nullptr, 1, h->d.minfl,
+                         h->status + p0, s);
+    if (st) break;
+    st = launch_update_f64_range(ne, np, p0, c, nv, (const double*)h->xb, trans, transm, (double*)h->xa, s);
+  }
+  cudaStreamSynchronize(s);
+  void* fr[] = {cnt, idx, offs, scr, rloc, rdiag, rows, dep, trans, transm};
+  for (void* p : fr) dfree(p);
+  return st;
+}
+
+int letkf_sweep_run(letkf_sweep_t h, void* stream) {
+  if (!h) return LETKF_ERR_ARG;
+  cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+  if (h->d.precision == LETKF_PREC_F64) return run_f64(h, s);
+  SweepArgs a;
+  memset(&a, 0, sizeof(a));
+  a.n = h->d.ne;
+  a.nv = h->d.nv;
+  a.npts = h->d.npts;
+  a.nlon = h->d.nlon;
+  a.nlat = h->d.nlat;
+  a.nobs = h->nobs;
+  a.G = h->G;
+  a.obsF = h->obsF;
+  a.obsA = h->obsA;
+  a.obsMeta = h->meta;
+  a.ori = h->ori;
+  a.orj = h->orj;
+  a.olev = h->olev;
+  a.odat = h->odat;
+  a.ocls = h->ocls;
+  double* f = &a.P.dx;
+  for (int i = 0; i < 15; i++) f[i] = h->d.params[i];
+  a.ens_obs = h->ens32;
+  a.order = h->order;
+  a.pri = h->pri;
+  a.prj = h->prj;
+  a.prlev = h->prlev;
+  a.prz = h->prz;
+  a.xb = (const float*)h->xb;
+  a.xa = (float*)h->xa;
+  a.infl = h->infl;
+  a.nobsl_out = h->nobsl;
+  a.sweeps_out = h->sweeps;
+  a.status = h->status;
+  a.counter = h->counter;
+  a.minfl = h->d.minfl;
+  a.max_sweeps = h->max_sweeps;
+  cudaMemsetAsync(h->counter, 0, sizeof(int), s);
+  return launch_sweep_mixed(a, s, h->grid_cap);
+}
+
+int letkf_sweep_get_analysis(letkf_sweep_t h, void* xa, int on_device) {
+  if (!h || !xa) return LETKF_ERR_ARG;
+  const size_t bytes = (size_t)h->d.npts * h->d.nv * h->d.ne * elem(h);
+  cudaMemcpyAsync(xa, h->xa, bytes, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream);
+  return cuda_status(cudaStreamSynchronize(h->stream));
+}
+
+int letkf_sweep_get_diagnostics(letkf_sweep_t h, double* infl, int* nobsl, int* status, int* sweeps) {
+  if (!h) return LETKF_ERR_ARG;
+  const size_t np = (size_t)h->d.npts;
+  cudaStreamSynchronize(h->stream);
+  if (infl) cudaMemcpy(infl, h->infl, sizeof(double) * np, cudaMemcpyDeviceToHost);
+  if (nobsl) cudaMemcpy(nobsl, h->nobsl, sizeof(int) * np, cudaMemcpyDeviceToHost);
+  if (status) cudaMemcpy(status, h->status, sizeof(int) * np, cudaMemcpyDeviceToHost);
+  if (sweeps) cudaMemcpy(sweeps, h->sweeps, sizeof(int) * np, cudaMemcpyDeviceToHost);
+  return cuda_status(cudaGetLastError());
+}
+
+int letkf_sweep_sorted_obs(letkf_sweep_t h, int* nobsgrd) {
+  if (!h || !nobsgrd) return LETKF_ERR_ARG;
+  cudaStreamSynchronize(h->stream);
+  return cuda_status(
+      cudaMemcpy(nobsgrd, h->G, sizeof(int) * (h->d.nlon + 1) * h->d.nlat, cudaMemcpyDeviceToHost));
+}
+
+}  // extern "C"

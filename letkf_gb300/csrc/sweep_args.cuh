@@ -1,0 +1,35 @@
+// sweep_args.cuh -- argument block of the fused mixed-precision sweep kernel.
+#pragma once
+#include "letkf_common.cuh"
+
+namespace letkf {
+
+struct SweepScaleParams {
+  double dx, dy, dlon_zero, dlat_zero, sigma_obs, sigma_obsv, sigma_obs_rain, sigma_obsv_rain, base_obsv_rain,
+      sigma_obs_radar, sigma_obs_radar_noref, sigma_obsz_radar, radar_ref_thres_dbz, sigma_obs_tc, sigma_obsv_tc;
+};
+
+struct SweepArgs {
+  int n, nv, npts, nlon, nlat, nobs;
+  const int* G;           // nobsgrd [(nlon+1)*nlat]
+  const float4* obsF;     // [nobs] ri, rj, vertical coordinate, 1/sigma_h^2
+  const float4* obsA;     // [nobs] 1/sigma_v^2, 1/err^2, dep, var_local weight
+  const int* obsMeta;     // [nobs] bit0 height vertical, bit1 rejected by var_local
+  const double *ori, *orj, *olev, *odat;  // FP64 records for the exact re-test
+  const int* ocls;
+  SweepScaleParams P;
+  const float* ens_obs;   // [nobs][n]
+  const int* order;       // [npts]
+  const double *pri, *prj, *prlev, *prz;
+  const float* xb;        // [nv][npts][n]
+  float* xa;
+  double* infl;           // [npts] in/out
+  int* nobsl_out;         // [npts] or NULL
+  int* sweeps_out;        // [npts] or NULL
+  int* status;            // [npts]
+  int* counter;
+  double minfl;
+  int max_sweeps;
+};
+
+}  // namespace letkf

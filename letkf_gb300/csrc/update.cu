@@ -11,7 +11,10 @@ namespace letkf {
 
 constexpr int UPD_NT = 128;
 
-__global__ void __launch_bounds__(UPD_NT) update_f64_kernel(int n, int npts, int nv, const double* __restrict__ xb,
+// Points p0 .. p0+cnt-1 of arrays holding npts_total points; trans / transm
+// are indexed from p0.
+__global__ void __launch_bounds__(UPD_NT) update_f64_kernel(int n, int npts_total, int p0, int cnt, int nv,
+                                                             const double* __restrict__ xb,
                                                              const double* __restrict__ trans,
                                                              const double* __restrict__ transm, double* xa) {
   extern __shared__ __align__(16) double su[];
@@ -20,13 +23,14 @@ __global__ void __launch_bounds__(UPD_NT) update_f64_kernel(int n, int npts, int
   double* xp = tm + n;       // nv*n
   double* mean = xp + nv * n;  // nv
   const int tid = threadIdx.x;
-  for (int p = blockIdx.x; p < npts; p += gridDim.x) {
+  for (int pl = blockIdx.x; pl < cnt; pl += gridDim.x) {
+    const int p = p0 + pl;
     __syncthreads();
-    for (int idx = tid; idx < n * n; idx += UPD_NT) W[idx] = trans[(size_t)p * n * n + idx];
-    for (int k = tid; k < n; k += UPD_NT) tm[k] = transm ? transm[(size_t)p * n + k] : 0.0;
+    for (int idx = tid; idx < n * n; idx += UPD_NT) W[idx] = trans[(size_t)pl * n * n + idx];
+    for (int k = tid; k < n; k += UPD_NT) tm[k] = transm ? transm[(size_t)pl * n + k] : 0.0;
     for (int t = tid; t < nv * n; t += UPD_NT) {
       const int v = t / n, m = t - v * n;
-      xp[t] = xb[((size_t)v * npts + p) * n + m];
+      xp[t] = xb[((size_t)v * npts_total + p) * n + m];
     }
     __syncthreads();
     for (int v = tid; v < nv; v += UPD_NT) {
@@ -45,16 +49,17 @@ __global__ void __launch_bounds__(UPD_NT) update_f64_kernel(int n, int npts, int
       } else {
         for (int k = 0; k < n; k++) a = a + xp[v * n + k] * W[(size_t)m * n + k];
       }
-      xa[((size_t)v * npts + p) * n + m] = a;
+      xa[((size_t)v * npts_total + p) * n + m] = a;
     }
   }
 }
 
-int launch_update_f64(int ne, int npts, int nv, const double* xb, const double* trans, const double* transm,
-                      double* xa, cudaStream_t stream) {
-  if (ne < 2 || npts < 0 || nv < 1) return LETKF_ERR_ARG;
+int launch_update_f64_range(int ne, int npts_total, int p0, int cnt, int nv, const double* xb, const double* trans,
+                            const double* transm, double* xa, cudaStream_t stream) {
+  if (ne < 2 || npts_total < 0 || p0 < 0 || cnt < 0 || p0 + cnt > npts_total || nv < 1) return LETKF_ERR_ARG;
   if (ne > LETKF_MAX_NE) return LETKF_ERR_CAPACITY;
-  if (npts == 0) return LETKF_OK;
+  if (cnt == 0) return LETKF_OK;
+  const int npts = cnt;
   const size_t smem = sizeof(double) * ((size_t)ne * ne + ne + (size_t)nv * ne + nv);
   cudaError_t err = cudaFuncSetAttribute(update_f64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return cuda_status(err);
@@ -63,9 +68,14 @@ int launch_update_f64(int ne, int npts, int nv, const double* xb, const double* 
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   int grid = nsm * 8;
   if (grid > npts) grid = npts;
-  update_f64_kernel<<<grid, UPD_NT, smem, stream>>>(ne, npts, nv, xb, trans, transm, xa);
+  update_f64_kernel<<<grid, UPD_NT, smem, stream>>>(ne, npts_total, p0, cnt, nv, xb, trans, transm, xa);
   note_launch();
   return cuda_status(cudaGetLastError());
+}
+
+int launch_update_f64(int ne, int npts, int nv, const double* xb, const double* trans, const double* transm,
+                      double* xa, cudaStream_t stream) {
+  return launch_update_f64_range(ne, npts, 0, npts, nv, xb, trans, transm, xa, stream);
 }
 
 }  // namespace letkf

@@ -170,40 +170,51 @@ def regional_levels(nlev):
     return np.exp(np.linspace(math.log(REGIONAL_P_BOT), math.log(REGIONAL_P_TOP), nlev))
 
 
-def regional_obs(rng, nobs, nlon, nlat, nblob=48, frac_blob=0.75, blob_sigma_cells=(4.0, 14.0), frac_ps=0.02):
-    """Observation positions in grid coordinates (1-based ri, rj) with a
-    clustered density: Gaussian blobs (radar-like) over a uniform background.
-    A share frac_ps are surface-pressure reports (class 1)."""
-    nb = int(frac_blob * nobs)
-    centers = np.stack([rng.uniform(1, nlon, nblob), rng.uniform(1, nlat, nblob)], -1)
-    sig = rng.uniform(*blob_sigma_cells, nblob)
-    w = rng.dirichlet(np.ones(nblob) * 0.7)
-    which = rng.choice(nblob, nb, p=w)
-    ri = centers[which, 0] + sig[which] * rng.standard_normal(nb)
-    rj = centers[which, 1] + sig[which] * rng.standard_normal(nb)
-    ok = (ri >= 0.5) & (ri < nlon + 0.5) & (rj >= 0.5) & (rj < nlat + 0.5)
-    ri, rj = ri[ok], rj[ok]
-    nu = nobs - ri.size
-    ri = np.concatenate([ri, rng.uniform(0.5, nlon + 0.5 - 1e-9, nu)])
-    rj = np.concatenate([rj, rng.uniform(0.5, nlat + 0.5 - 1e-9, nu)])
-    perm = rng.permutation(nobs)
-    ri, rj = ri[perm], rj[perm]
+def regional_obs(rng, nobs, nlon, nlat, void_frac=0.2, nmode=8, wavelength_cells=(40.0, 120.0), frac_ps=0.02):
+    """Observation positions in grid coordinates (1-based ri, rj) drawn from a
+    clustered density: a smooth random field G (nmode random plane waves of
+    wavelength_cells) cut at the quantile void_frac, rho = max(G - t, 0), so
+    that about void_frac of the domain has no observations and the rest is
+    uneven.  A share frac_ps are surface-pressure reports (class 1).  Levels
+    are uniform in ln p between 1000 and 100 hPa."""
+    ang = rng.uniform(0, 2 * math.pi, nmode)
+    wl = rng.uniform(*wavelength_cells, nmode)
+    kx, ky = 2 * math.pi / wl * np.cos(ang), 2 * math.pi / wl * np.sin(ang)
+    ph = rng.uniform(0, 2 * math.pi, nmode)
+
+    def G(x, y):
+        return np.cos(np.outer(x, kx) + np.outer(y, ky) + ph).sum(1)
+
+    gx, gy = np.meshgrid(np.linspace(0.5, nlon + 0.5, 128), np.linspace(0.5, nlat + 0.5, 128))
+    gs = G(gx.ravel(), gy.ravel())
+    t = np.quantile(gs, void_frac)
+    gmax = gs.max() - t
+    ri = np.empty(0)
+    rj = np.empty(0)
+    while ri.size < nobs:
+        m = 2 * (nobs - ri.size) + 1024
+        x = rng.uniform(0.5, nlon + 0.5, m)
+        y = rng.uniform(0.5, nlat + 0.5, m)
+        keep = rng.uniform(0, gmax, m) < (G(x, y) - t)
+        ri = np.concatenate([ri, x[keep]])
+        rj = np.concatenate([rj, y[keep]])
+    ri, rj = ri[:nobs], rj[:nobs]
     lnp = rng.uniform(math.log(REGIONAL_P_TOP), math.log(REGIONAL_P_BOT), nobs)
     cls = (rng.uniform(size=nobs) < frac_ps).astype(np.int32)
     return ri, rj, np.exp(lnp), cls
 
 
-REGIONAL_SIGMA_OBS = 4.0e3   # horizontal localisation (m); see DESIGN: keeps 0-2000 local obs with 1e6 obs
+REGIONAL_SIGMA_OBS = 3.0e3   # horizontal localisation (m): 1e6 obs on 768 km x 768 km give 0-2035 local obs
 REGIONAL_SIGMA_OBSV = 0.4    # vertical localisation (ln p)
 
 
 def regional_case(seed=0, nlon=32, nlat=32, nlev=8, ne=64, nobs=20000, nvar=6, dx=3000.0,
-                  sigma_obs=REGIONAL_SIGMA_OBS, sigma_obsv=REGIONAL_SIGMA_OBSV, nblob=None, dtype=np.float64,
+                  sigma_obs=REGIONAL_SIGMA_OBS, sigma_obsv=REGIONAL_SIGMA_OBSV, dtype=np.float64,
                   with_grid_ensemble=True):
     """Cartesian regional case (SCALE-style search).  Small by default for
     tests; bench.py builds the full-size case on the device."""
     rng = np.random.default_rng(seed)
-    ri, rj, lev, cls = regional_obs(rng, nobs, nlon, nlat, nblob=nblob or max(4, nlon * nlat // 1400))
+    ri, rj, lev, cls = regional_obs(rng, nobs, nlon, nlat)
     var = rng.integers(0, nvar, nobs)
     err = np.where(cls == 1, 100.0, 1.0)
     dat_ps = 1.0e5 * (1 + 0.01 * rng.standard_normal(nobs))

@@ -136,6 +136,15 @@ int oracle_l96_select(int nx, int ny, const double* h /* ny x nx col-major */, i
  * (speedy/common/common_speedy.f90:335-370).  x is [npts][ne] row-major. */
 void oracle_ensmean(int npts, int ne, const double* x, double* mean, double* pert);
 
+/* SCALE-style grid loop over npts points (or the `subset` of nsub of them):
+ * obs_local + letkf_core(transm, rdiag_wloc) + update of nv variables.
+ * hdxf[nobs][ne] and odep[nobs] are in the sorted obs order; xb, xa are
+ * [nv][npts][ne]; infl[npts] in/out.  Returns the number of failed points. */
+int oracle_scale_sweep(const oracle_scale_obs* o, const double* hdxf, const double* odep, int ne, int nv, int npts,
+                       const int* subset, int nsub, const double* pri, const double* prj, const double* prlev,
+                       const double* prz, const double* xb, double* xa, double* infl, int* nobsl_out,
+                       double minfl, int nthreads);
+
 /* relax_beta / RTPP / RTPS (scale/letkf/letkf_tools.f90:1182-1268) */
 void oracle_weight_rtpp(int ne, const double* w, double alpha, double* wrlx);
 void oracle_weight_rtps(int ne, const double* w, const double* pa, const double* xb, double alpha,

@@ -47,6 +47,9 @@ def lib():
         _lib.oracle_l96_select.restype = C.c_int
         _lib.oracle_l96_select.argtypes = [C.c_int, C.c_int, pd, C.c_int, d, d, pi, pd]
         _lib.oracle_ensmean.argtypes = [C.c_int, C.c_int, pd, pd, pd]
+        _lib.oracle_scale_sweep.restype = C.c_int
+        _lib.oracle_scale_sweep.argtypes = [C.c_void_p, pd, pd, C.c_int, C.c_int, C.c_int, pi, C.c_int, pd, pd, pd,
+                                            pd, pd, pd, pd, pi, d, C.c_int]
         _lib.oracle_weight_rtpp.argtypes = [C.c_int, pd, d, pd]
         _lib.oracle_weight_rtps.argtypes = [C.c_int, pd, pd, pd, d, pd, pd]
     return _lib
@@ -223,6 +226,25 @@ class ScaleObs:
                            p["sigma_obsz_radar"], p["radar_ref_thres_dbz"], p["sigma_obs_tc"],
                            p["sigma_obsv_tc"], None if k[10] is None else k[10].ctypes.data,
                            int(max_nobs_per_grid))
+
+    def sweep(self, hdxf, dep, xb, pri, prj, prlev, infl, prz=None, subset=None, minfl=0.0, nthreads=0):
+        """SCALE grid loop (oracle_scale_sweep).  hdxf (nobs, ne) and dep in
+        sorted order; xb (nv, npts, ne).  Returns (xa, infl, nobsl); with a
+        subset only those points' entries are meaningful."""
+        hdxf = _f64(hdxf)
+        xb = _f64(xb)
+        nv, npts, ne = xb.shape
+        xa = np.zeros_like(xb)
+        infl = np.array(infl, dtype=np.float64).copy()
+        nobsl = np.zeros(npts, dtype=np.int32)
+        sub = None if subset is None else np.ascontiguousarray(subset, dtype=np.int32)
+        bad = lib().oracle_scale_sweep(C.byref(self.s), _pd(hdxf), _pd(_f64(dep)), ne, nv, npts, _pi(sub),
+                                       0 if sub is None else sub.size, _pd(_f64(pri)), _pd(_f64(prj)),
+                                       _pd(_f64(prlev)), None if prz is None else _pd(_f64(prz)), _pd(xb), _pd(xa),
+                                       _pd(infl), _pi(nobsl), float(minfl), int(nthreads))
+        if bad:
+            raise RuntimeError(f"oracle sweep: {bad} points failed")
+        return xa, infl, nobsl
 
     def obs_local(self, ri, rj, rlev, rz=0.0):
         n = max(self.s.nobs, 1)

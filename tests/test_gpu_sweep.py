@@ -1,0 +1,114 @@
+"""The device-resident analysis sweep (search + core + update of every point)
+against the oracle's SCALE grid loop.
+
+FP64 plain form: analysis within 1e-10 of the oracle (relative to the
+background spread).  Mixed form: analysis-mean and spread RMS error below
+1e-4 of the background spread.  Both: local obs counts bit-exact."""
+import numpy as np
+import pytest
+
+from letkf_gb300 import synthetic as S
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(seed=3, nlon=24, nlat=20, nlev=6, ne=40, nobs=2500, sigma_obs=10.0e3, f32=False, var_local=None):
+    case = S.regional_case(seed, nlon=nlon, nlat=nlat, nlev=nlev, ne=ne, nobs=nobs, sigma_obs=sigma_obs,
+                           dtype=np.float32 if f32 else np.float64)
+    prm = S.scale_params(case)
+    perm, grd = O.scale_sort_obs(nlon, nlat, case["ri"], case["rj"])
+    nob = perm.size
+    varloc = (case["var"] % 3).astype(np.int32)
+    hdxf = case["hdxf"].astype(np.float32).astype(np.float64) if f32 else case["hdxf"]
+    dep = case["dep"]
+    so = O.ScaleObs(nlon, nlat, grd, case["ri"][perm], case["rj"][perm], case["lev"][perm], case["dat"][perm],
+                    case["err"][perm], case["cls"][perm], np.zeros(nob), np.zeros(nob), varloc[perm], 1, 1,
+                    prm["dx"], prm["dy"], prm["dlon_zero"], prm["dlat_zero"], prm["sigma_obs"], prm["sigma_obsv"],
+                    var_local)
+    return case, prm, perm, grd, so, varloc, hdxf, dep
+
+
+def _spread(xb):
+    return np.sqrt(((xb - xb.mean(-1, keepdims=True)) ** 2).sum(-1) / (xb.shape[-1] - 1)).mean()
+
+
+@pytest.mark.parametrize("ne,var_local", [(40, None), (64, [1.0, 0.5, 0.0]), (20, None)])
+def test_mixed_sweep_against_oracle(cuda, ne, var_local):
+    from letkf_gb300.sweep import PREC_MIXED, Sweep
+
+    case, prm, perm, grd, so, varloc, hdxf, dep = _setup(ne=ne, f32=True, var_local=var_local)
+    xb = case["xb"].astype(np.float64)
+    npts = case["pri"].size
+    infl0 = np.full(npts, 1.05)
+    xa_ref, infl_ref, nl_ref = so.sweep(hdxf[perm], dep[perm], xb, case["pri"], case["prj"], case["prlev"], infl0,
+                                        minfl=1.0)
+    sw = Sweep(ne, case["nvar"], case["nlon"], case["nlat"], npts, prm, precision=PREC_MIXED, minfl=1.0)
+    sw.set_points(case["pri"], case["prj"], case["prlev"])
+    sw.set_obs(case["ri"], case["rj"], case["lev"], case["dat"], case["err"], dep, case["cls"],
+               hdxf.astype(np.float32), varloc=varloc if var_local is not None else None, var_local_row=var_local)
+    np.testing.assert_array_equal(sw.nobsgrd(), grd)
+    sw.set_background(case["xb"])
+    sw.set_inflation(infl0)
+    sw.run()
+    xa = sw.analysis().astype(np.float64)
+    dg = sw.diagnostics()
+    sw.close()
+    np.testing.assert_array_equal(dg["nobsl"], nl_ref)
+    assert (dg["status"] == 0).all()
+    assert nl_ref.max() > 100 and (nl_ref == 0).sum() >= 0
+    spread = _spread(xb)
+    em = np.sqrt(np.mean((xa.mean(-1) - xa_ref.mean(-1)) ** 2)) / spread
+    ep = np.sqrt(np.mean(((xa - xa.mean(-1, keepdims=True)) - (xa_ref - xa_ref.mean(-1, keepdims=True))) ** 2))
+    ep /= spread
+    assert em < 1e-4, f"analysis-mean error {em:.2e} of spread"
+    assert ep < 1e-4, f"analysis-perturbation error {ep:.2e} of spread"
+    np.testing.assert_allclose(dg["infl"], infl_ref, rtol=1e-4)
+
+
+def test_f64_sweep_against_oracle(cuda):
+    from letkf_gb300.sweep import PREC_F64, Sweep
+
+    case, prm, perm, grd, so, varloc, hdxf, dep = _setup(ne=32, nobs=5000)
+    xb = case["xb"]
+    npts = case["pri"].size
+    infl0 = np.linspace(0.9, 1.2, npts)
+    xa_ref, infl_ref, nl_ref = so.sweep(hdxf[perm], dep[perm], xb, case["pri"], case["prj"], case["prlev"], infl0,
+                                        minfl=1.0)
+    sw = Sweep(32, case["nvar"], case["nlon"], case["nlat"], npts, prm, precision=PREC_F64, minfl=1.0)
+    sw.set_points(case["pri"], case["prj"], case["prlev"])
+    sw.set_obs(case["ri"], case["rj"], case["lev"], case["dat"], case["err"], dep, case["cls"], hdxf)
+    sw.set_background(xb)
+    sw.set_inflation(infl0)
+    sw.run()
+    xa = sw.analysis()
+    dg = sw.diagnostics()
+    sw.close()
+    np.testing.assert_array_equal(dg["nobsl"], nl_ref)
+    spread = _spread(xb)
+    err = np.abs(xa - xa_ref).max() / spread
+    assert err < 1e-10, f"FP64 sweep error {err:.2e} of spread"
+    np.testing.assert_allclose(dg["infl"], infl_ref, rtol=1e-12)
+
+
+def test_mixed_sweep_no_obs(cuda):
+    """Every point without local obs: xa = mean + sqrt(infl) xb' and infl unchanged (common_letkf.f90:82-96)."""
+    from letkf_gb300.sweep import PREC_MIXED, Sweep
+
+    case, prm, perm, grd, so, varloc, hdxf, dep = _setup(ne=20, nobs=10, f32=True)
+    npts = case["pri"].size
+    sw = Sweep(20, case["nvar"], case["nlon"], case["nlat"], npts, prm, precision=PREC_MIXED)
+    sw.set_points(case["pri"], case["prj"], case["prlev"])
+    sw.set_obs(case["ri"][:0], case["rj"][:0], case["lev"][:0], case["dat"][:0], case["err"][:0], dep[:0],
+               case["cls"][:0], np.zeros((0, 20), np.float32))
+    sw.set_background(case["xb"])
+    sw.set_inflation(np.full(npts, 1.21))
+    sw.run()
+    xa = sw.analysis().astype(np.float64)
+    dg = sw.diagnostics()
+    sw.close()
+    xb = case["xb"].astype(np.float64)
+    m = xb.mean(-1, keepdims=True)
+    np.testing.assert_allclose(xa, m + 1.1 * (xb - m), rtol=0, atol=2e-6 * np.abs(xb).max())
+    assert (dg["nobsl"] == 0).all()
+    np.testing.assert_array_equal(dg["infl"], 1.21)
