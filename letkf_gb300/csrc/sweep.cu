@@ -33,6 +33,7 @@ int launch_core_f64(int, int, const int64_t*, const double*, const double*, cons
                     double*, double*, double*, int, double, int*, cudaStream_t);
 int launch_update_f64_range(int ne, int npts_total, int p0, int cnt, int nv, const double* xb, const double* trans,
                             const double* transm, double* xa, cudaStream_t stream);
+int launch_gather_rows(int, int64_t, const int*, const void*, const void*, int, void*, void*, cudaStream_t);
 
 }  // namespace letkf
 
@@ -439,9 +440,7 @@ static int run_f64(letkf_sweep_t h, cudaStream_t s) {
                              h->d.params, offs, cnt, idx, rloc, rdiag, s);
     if (st) break;
     if (total > 0) {
-      extern int launch_gather_rows(int, int64_t, const int*, const void*, const void*, int, void*, void*,
-                                    cudaStream_t);
-      st = launch_gather_rows(ne, total, idx, h->ens64, h->odep, 8, rows, dep, s);
+      st = letkf::launch_gather_rows(ne, total, idx, h->ens64, h->odep, 8, rows, dep, s);
       if (st) break;
     }
     // SCALE convention: rdiag = err^2 / rloc with rdiag_wloc (letkf_tools.f90:199-206)
