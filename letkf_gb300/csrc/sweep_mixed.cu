@@ -71,7 +71,7 @@ struct SweepSmem {
   static constexpr int ROWPRE = ROWIB + SW_MAXROWS;  // int [SW_MAXROWS+1]
   static constexpr int WCNT = ROWPRE + SW_MAXROWS + 1;  // int [NT/32 + 1]
   static constexpr int MEAN = ((WCNT + NT / 32 + 2) + 1) & ~1;  // double [8] (even float index)
-  static constexpr int CTRL = MEAN + 16;      // int [8]
+  static constexpr int CTRL = MEAN + 32;      // int [8]   (MEAN holds 16 doubles)
   static constexpr int TOTAL = CTRL + 8;
   static constexpr size_t BYTES = sizeof(float) * (size_t)TOTAL;
 };
@@ -122,11 +122,11 @@ __global__ void __launch_bounds__(MixedCfg<NP>::NT) sweep_mixed_kernel(SweepArgs
     for (int jb = jmin; any && jb <= jmax; jb += SW_MAXROWS) {
       const int nrow = min(SW_MAXROWS, jmax - jb + 1);
       // row table: candidate ranges of obs_choose in row order
-      if (tid < nrow) {
-        const int j = jb + tid;
+      for (int r = tid; r < nrow; r += NT) {
+        const int j = jb + r;
         const int ib = a.G[(size_t)(j - 1) * ld + imin - 1], ie = a.G[(size_t)(j - 1) * ld + imax];
-        rowib[tid] = ib;
-        rowpre[tid + 1] = ie - ib;
+        rowib[r] = ib;
+        rowpre[r + 1] = ie - ib;
       }
       __syncthreads();
       if (tid == 0) {
