@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
     ap.add_argument("--fp64-stride", type=int, default=64, help="FP64 plain form on every n-th point")
     ap.add_argument("--no-extras", action="store_true", help="skip e2e, fp64, cpu baseline (profiling runs)")
+    ap.add_argument("--eig", default="newton-schulz", choices=["newton-schulz", "jacobi"],
+                    help="transform of the mixed form")
     return ap.parse_args()
 
 
@@ -208,7 +210,7 @@ def config_block(args, wl):
     return {"workload": f"regional {args.nlon}x{args.nlat}x{args.nlev} (3 km), {args.nv} vars, k={args.ne}, "
                         f"{args.nobs} clustered obs, sigma_h={wl.sigma_obs:.0f} m, sigma_v={wl.sigma_obsv} ln p",
             "points_per_sweep": wl.npts, "ensemble": args.ne, "variables": args.nv, "observations": args.nobs,
-            "local_obs": "0-2000 per point", "form": "mixed (FP32 ensemble / Gram / Jacobi, FP64 mean)",
+            "local_obs": "0-2000 per point", "form": "mixed (FP32 ensemble, Gram and transform; FP64 mean and mean increment)",
             "l2": "inputs larger than L2 (background ensemble %.1f GB)" % (wl.npts * args.nv * args.ne * 4 / 1e9),
             "parallelism": f"dp{args.gpus} (independent domains per GPU)"}
 
@@ -218,7 +220,7 @@ def run_gpu(args, rank, world, dist):
     import torch
 
     from letkf_gb300 import lib as L
-    from letkf_gb300.sweep import PREC_F64, PREC_MIXED, Sweep
+    from letkf_gb300.sweep import OPT_EIGENSOLVER, PREC_F64, PREC_MIXED, Sweep
     from letkf_gb300.workload import RegionalWorkload
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
@@ -230,6 +232,7 @@ def run_gpu(args, rank, world, dist):
     sw = Sweep(args.ne, args.nv, args.nlon, args.nlat, wl.npts, wl.params, precision=PREC_MIXED)
     sw.set_points(ri, rj, plev, tile=4)
     sw.set_obs(wl.ri, wl.rj, wl.lev, dat, wl.err, dep, wl.cls, hdxf)
+    sw.set_option(OPT_EIGENSOLVER, 0 if args.eig == "newton-schulz" else 1)
     sw.set_background_device(xb.data_ptr())
     infl0 = np.ones(wl.npts)
     sw.set_inflation(infl0)
@@ -285,8 +288,9 @@ def run_gpu(args, rank, world, dist):
     nl = nobsl.astype(np.float64)
     out["local_obs"] = {"min": int(nl.min()), "mean": float(nl.mean()), "p50": float(np.median(nl)),
                         "p99": float(np.percentile(nl, 99)), "max": int(nl.max()), "zero_frac": float((nl == 0).mean())}
-    out["jacobi_sweeps"] = {"mean": float(dg["sweeps"][nobsl > 0].mean()) if (nobsl > 0).any() else 0.0,
-                            "max": int(dg["sweeps"].max())}
+    out["transform"] = {"method": args.eig,
+                        "iterations_mean": float(dg["sweeps"][nobsl > 0].mean()) if (nobsl > 0).any() else 0.0,
+                        "iterations_max": int(dg["sweeps"].max())}
     if args.no_extras:
         return out, sw
     # ---- e2e: host buffers through the C ABI ----

@@ -138,6 +138,9 @@ int letkf_search_speedy(int nlon, int nlat, const double* lon, const double* lat
 
 #define LETKF_OPT_GRID_CAP 1   /* cap on the persistent grid (0 = #SM x occupancy) */
 #define LETKF_OPT_MAX_SWEEPS 2 /* Jacobi sweep limit of the mixed form (default 12) */
+#define LETKF_OPT_EIGENSOLVER 3 /* transform of the mixed form: */
+#define LETKF_EIG_NEWTON_SCHULZ 0 /*   W = sqrt((k-1)) A^(-1/2) by Newton-Schulz (default) */
+#define LETKF_EIG_JACOBI 1        /*   eigen-decomposition by parallel Jacobi */
 
 typedef struct letkf_sweep_desc {
   int ne;           /* ensemble size (MEMBER) */

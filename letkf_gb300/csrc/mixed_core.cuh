@@ -265,6 +265,166 @@ __device__ int jacobi_eig(float* sm, int max_sweeps) {
   return sweep;
 }
 
+// ---------------------------------------------------------------------------
+// Newton-Schulz inverse square root (GEMM-only replacement of the eigensolve
+// for the fused sweep).  A = Gram + c I is SPD with every eigenvalue >= c, so
+// with s >= lambda_max / 2 the coupled iteration
+//   T = Z Y,  Y <- Y (3I - T) / 2,  Z <- (3I - T) Z / 2,   Y0 = A / s, Z0 = I
+// converges to Y = (A/s)^(1/2), Z = (A/s)^(-1/2).  Then
+//   W    = sqrt((k-1)/s) Z          = sqrt((k-1) Pa)     (common_letkf.f90:186-193)
+//   wbar = Z (Z b) / s              = Pa hdxb_rinv^T dep (:146-182)
+// All iterates are polynomials in A, hence symmetric and commuting, so every
+// product reads its left factor by rows of the symmetric storage.
+// ---------------------------------------------------------------------------
+template <int NP>
+struct NSSmem {
+  using S = MixedSmem<NP>;
+  static constexpr int T = S::TOTAL;          // NP*NP product T = Z Y
+  static constexpr int TOTAL = T + NP * NP;
+};
+
+// acc = X Yb for this thread's TR x TC tile (X, Yb symmetric, row-major, ld NP)
+template <int NP>
+__device__ __forceinline__ void sym_gemm_tile(const float* X, const float* Yb, int i0, int j0,
+                                              float (&acc)[MixedCfg<NP>::TR][MixedCfg<NP>::TC]) {
+  using C = MixedCfg<NP>;
+#pragma unroll
+  for (int a = 0; a < C::TR; a++)
+#pragma unroll
+    for (int b = 0; b < C::TC; b++) acc[a][b] = 0.f;
+#pragma unroll 4
+  for (int k = 0; k < NP; k++) {
+    float av[C::TR], bv[C::TC];
+#pragma unroll
+    for (int t = 0; t < C::TR; t += 4) {
+      const float4 x = *reinterpret_cast<const float4*>(X + k * NP + i0 + t);
+      av[t] = x.x;
+      av[t + 1] = x.y;
+      av[t + 2] = x.z;
+      av[t + 3] = x.w;
+    }
+#pragma unroll
+    for (int t = 0; t < C::TC; t += 4) {
+      const float4 y = *reinterpret_cast<const float4*>(Yb + k * NP + j0 + t);
+      bv[t] = y.x;
+      bv[t + 1] = y.y;
+      bv[t + 2] = y.z;
+      bv[t + 3] = y.w;
+    }
+#pragma unroll
+    for (int a = 0; a < C::TR; a++)
+#pragma unroll
+      for (int b = 0; b < C::TC; b++) acc[a][b] = fmaf(av[a], bv[b], acc[a][b]);
+  }
+}
+
+// Newton-Schulz on sm[A] (SPD, all eigenvalues >= cdiag > 0).  Leaves
+// Z = (A/s)^(-1/2) in sm[V] (row-major, symmetric), scratch in sm[NS::T], and
+// returns s (> 0); *iters gets the iterations used.
+template <int NP>
+__device__ float ns_invsqrt(float* sm, float cdiag, int max_iter, int* iters) {
+  using C = MixedCfg<NP>;
+  using S = MixedSmem<NP>;
+  using N = NSSmem<NP>;
+  constexpr int NTI = NP / C::TR;
+  const int tid = threadIdx.x;
+  float* A = sm + S::A;
+  float* Z = sm + S::V;
+  float* T = sm + N::T;
+  float* xv = sm + S::G;   // power-iteration vector
+  float* yv = sm + S::LAM;
+  float* redf = sm + S::RED;
+  double* red = reinterpret_cast<double*>(sm + S::RED);
+  // Gershgorin bound (>= lambda_max) and a power-iteration estimate
+  float g = 0.f;
+  if (tid < NP) {
+    float s = 0.f;
+    for (int j = 0; j < NP; j++) s += fabsf(A[tid * NP + j]);
+    g = s;
+    xv[tid] = A[tid * NP + tid] * (1.f + 0.25f * __sinf(1.7f * tid));
+  }
+  g = warp_max(g);
+  __syncthreads();
+  if ((tid & 31) == 0) redf[tid >> 5] = g;
+  __syncthreads();
+  float gmax = redf[0];
+  for (int w = 1; w < C::NT / 32; w++) gmax = fmaxf(gmax, redf[w]);
+  __syncthreads();
+  float lam = 0.f;
+  for (int it = 0; it < 8; it++) {
+    double part = 0.0;
+    if (tid < NP) {
+      float s = 0.f;
+      for (int j = 0; j < NP; j++) s = fmaf(A[tid * NP + j], xv[j], s);
+      yv[tid] = s;
+      part = (double)s * (double)s;
+    }
+    const double nrm2 = block_sum<double, C::NT>(part, red);
+    double xx = 0.0;
+    if (tid < NP) xx = (double)xv[tid] * (double)xv[tid];
+    const double x2 = block_sum<double, C::NT>(xx, red);
+    lam = (float)sqrt(nrm2 / fmax(x2, 1e-300));
+    const float inv = (float)(1.0 / sqrt(fmax(nrm2, 1e-300)));
+    if (tid < NP) xv[tid] = yv[tid] * inv;
+    __syncthreads();
+  }
+  const float s = fmaxf(1.05f * lam, 0.5f * gmax);
+  const float inv_s = 1.f / s;
+  // Y0 = A/s (in place), Z0 = I
+  for (int idx = tid; idx < NP * NP; idx += C::NT) {
+    A[idx] *= inv_s;
+    Z[idx] = (idx / NP == idx % NP) ? 1.f : 0.f;
+  }
+  __syncthreads();
+  const int i0 = (tid % NTI) * C::TR, j0 = (tid / NTI) * C::TC;
+  float acc[C::TR][C::TC];
+  int it = 0;
+  bool last = false;
+  for (; it < max_iter; it++) {
+    // T = Z Y and ||T - I||_F^2
+    sym_gemm_tile<NP>(Z, A, i0, j0, acc);
+    double e2 = 0.0;
+#pragma unroll
+    for (int a = 0; a < C::TR; a++)
+#pragma unroll
+      for (int b = 0; b < C::TC; b++) {
+        T[(i0 + a) * NP + j0 + b] = acc[a][b];
+        const float d = acc[a][b] - ((i0 + a) == (j0 + b) ? 1.f : 0.f);
+        e2 += (double)d * (double)d;
+      }
+    e2 = block_sum<double, C::NT>(e2, red);  // also publishes T
+    // ||T - I||_F < 1e-4: one more (quadratically convergent) step reaches the FP32 floor
+    if (e2 < 1.0e-8) last = true;
+    // Y' = 1.5 Y - 0.5 Y T ; Z' = 1.5 Z - 0.5 T Z
+    float ynew[C::TR][C::TC];
+    sym_gemm_tile<NP>(A, T, i0, j0, acc);
+#pragma unroll
+    for (int a = 0; a < C::TR; a++)
+#pragma unroll
+      for (int b = 0; b < C::TC; b++) ynew[a][b] = 1.5f * A[(i0 + a) * NP + j0 + b] - 0.5f * acc[a][b];
+    sym_gemm_tile<NP>(T, Z, i0, j0, acc);
+#pragma unroll
+    for (int a = 0; a < C::TR; a++)
+#pragma unroll
+      for (int b = 0; b < C::TC; b++) acc[a][b] = 1.5f * Z[(i0 + a) * NP + j0 + b] - 0.5f * acc[a][b];
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < C::TR; a++)
+#pragma unroll
+      for (int b = 0; b < C::TC; b++) {
+        A[(i0 + a) * NP + j0 + b] = ynew[a][b];
+        Z[(i0 + a) * NP + j0 + b] = acc[a][b];
+      }
+    __syncthreads();
+    if (last) {
+      it++;
+      break;
+    }
+  }
+  if (iters) *iters = it;
+  return s;
+}
+
 // From sm[V], sm[LAM], sm[B]: fq, 1/lambda, wbar into sm[FQ], sm[IQ], sm[WB];
 // returns 0 ok, LETKF_ERR_EIG when all eigenvalues are <= 0.
 template <int NP>

@@ -136,6 +136,7 @@ struct letkf_sweep_s {
   cudaStream_t stream = nullptr;
   int grid_cap = 0;
   int max_sweeps = 12;
+  int use_ns = 1;
 };
 
 static void dfree(void* p) {
@@ -390,6 +391,10 @@ int letkf_sweep_set_option(letkf_sweep_t h, int option, int value) {
       if (value < 1 || value > 64) return LETKF_ERR_ARG;
       h->max_sweeps = value;
       return LETKF_OK;
+    case LETKF_OPT_EIGENSOLVER:
+      if (value != LETKF_EIG_NEWTON_SCHULZ && value != LETKF_EIG_JACOBI) return LETKF_ERR_ARG;
+      h->use_ns = value == LETKF_EIG_NEWTON_SCHULZ;
+      return LETKF_OK;
     default: return LETKF_ERR_ARG;
   }
 }
@@ -493,6 +498,8 @@ int letkf_sweep_run(letkf_sweep_t h, void* stream) {
   a.counter = h->counter;
   a.minfl = h->d.minfl;
   a.max_sweeps = h->max_sweeps;
+  a.max_ns_iter = 24;
+  a.use_ns = h->use_ns;
   cudaMemsetAsync(h->counter, 0, sizeof(int), s);
   return launch_sweep_mixed(a, s, h->grid_cap);
 }

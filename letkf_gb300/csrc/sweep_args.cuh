@@ -29,7 +29,9 @@ struct SweepArgs {
   int* status;            // [npts]
   int* counter;
   double minfl;
-  int max_sweeps;
+  int max_sweeps;   // Jacobi sweeps (fallback eigensolver)
+  int max_ns_iter;  // Newton-Schulz iterations
+  int use_ns;       // 1: Newton-Schulz inverse square root, 0: Jacobi eigensolver
 };
 
 }  // namespace letkf

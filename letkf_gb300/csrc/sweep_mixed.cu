@@ -63,15 +63,19 @@ struct SweepSmem {
   static constexpr int NT = MixedCfg<NP>::NT;
   static constexpr int CH = S::CH;
   static constexpr int PCAP = CH + NT;        // pending list capacity
-  static constexpr int PIDX = S::TOTAL;       // int [PCAP]
+  // search-phase tables, aliased with the Newton-Schulz product T (NSSmem::T)
+  static constexpr int U = S::TOTAL;
+  static constexpr int PIDX = U;              // int [PCAP]
   static constexpr int PW = PIDX + PCAP;      // float [PCAP]
   static constexpr int PD = PW + PCAP;
   static constexpr int PR = PD + PCAP;
   static constexpr int ROWIB = PR + PCAP;     // int [SW_MAXROWS]
   static constexpr int ROWPRE = ROWIB + SW_MAXROWS;  // int [SW_MAXROWS+1]
   static constexpr int WCNT = ROWPRE + SW_MAXROWS + 1;  // int [NT/32 + 1]
-  static constexpr int MEAN = ((WCNT + NT / 32 + 2) + 1) & ~1;  // double [8] (even float index)
-  static constexpr int CTRL = MEAN + 32;      // int [8]   (MEAN holds 16 doubles)
+  static constexpr int TAIL = WCNT + NT / 32 + 2 - U;
+  static constexpr int USIZE = TAIL > NP * NP ? TAIL : NP * NP;
+  static constexpr int MEAN = (U + USIZE + 1) & ~1;  // double [16]
+  static constexpr int CTRL = MEAN + 32;      // int [8]
   static constexpr int TOTAL = CTRL + 8;
   static constexpr size_t BYTES = sizeof(float) * (size_t)TOTAL;
 };
@@ -269,29 +273,53 @@ __global__ void __launch_bounds__(MixedCfg<NP>::NT) sweep_mixed_kernel(SweepArgs
       const float cdiag = (float)((double)(n - 1) / infl);
       for (int i = tid; i < NP; i += NT) sm[S::A + i * NP + i] += cdiag;
       __syncthreads();
-      sweeps = jacobi_eig<NP>(sm, a.max_sweeps);
-      const int st = eig_postprocess<NP>(sm, n);
-      if (st != LETKF_OK) {
-        // reference STOP 2: flag the point and leave the background unchanged
-        for (int i = tid; i < NP; i += NT) {
-          sm[S::FQ + i] = 0.f;
-          sm[S::WB + i] = 0.f;
+      int st = LETKF_OK;
+      if (a.use_ns && cdiag > 0.f && trace < 1.0e6 * (double)cdiag) {
+        // Newton-Schulz: spectrum within [c, c + tr(G)], far from the
+        // mtx_eigen truncation threshold lambda_max * sqrt(eps)
+        int its = 0;
+        const float s = ns_invsqrt<NP>(sm, cdiag, a.max_ns_iter, &its);
+        sweeps = its;
+        const float* Z = sm + S::V;
+        if (tid < NP) {
+          float acc_g = 0.f;
+          for (int j = 0; j < NP; j++) acc_g = fmaf(Z[tid * NP + j], sm[S::B + j], acc_g);
+          sm[S::G + tid] = acc_g;
         }
-        if (tid == 0) a.status[pt] = st;
-      } else if (tid == 0) {
-        a.status[pt] = LETKF_OK;
+        __syncthreads();
+        if (tid < NP) {
+          float acc_w = 0.f;
+          for (int j = 0; j < NP; j++) acc_w = fmaf(Z[tid * NP + j], sm[S::G + j], acc_w);
+          sm[S::WB + tid] = acc_w / s;
+        }
+        const float coef = sqrtf((float)(n - 1) / s);
+        for (int idx = tid; idx < NP * NP; idx += NT) sm[S::A + idx] = coef * Z[idx];
+        if (tid == 0) a.status[pt] = LETKF_OK;
+      } else {
+        sweeps = jacobi_eig<NP>(sm, a.max_sweeps);
+        st = eig_postprocess<NP>(sm, n);
+        if (st != LETKF_OK) {
+          // reference STOP 2: flag the point and leave the background unchanged
+          for (int i = tid; i < NP; i += NT) {
+            sm[S::FQ + i] = 0.f;
+            sm[S::WB + i] = 0.f;
+          }
+          if (tid == 0) a.status[pt] = st;
+        } else if (tid == 0) {
+          a.status[pt] = LETKF_OK;
+        }
+        __syncthreads();
+        // W into registers, then into sm[A] (row k = background member, column m)
+        float wt[C::TR][C::TC];
+        constexpr int NTI = NP / C::TR;
+        const int wi0 = (tid % NTI) * C::TR, wj0 = (tid / NTI) * C::TC;
+        form_w<NP>(sm, [&](int i, int j, float v) { wt[i - wi0][j - wj0] = v; });
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < C::TR; r++)
+#pragma unroll
+          for (int c = 0; c < C::TC; c++) sm[S::A + (wi0 + r) * NP + wj0 + c] = wt[r][c];
       }
-      __syncthreads();
-      // W into registers, then into sm[A] (row k = background member, column m)
-      float wt[C::TR][C::TC];
-      constexpr int NTI = NP / C::TR;
-      const int wi0 = (tid % NTI) * C::TR, wj0 = (tid / NTI) * C::TC;
-      form_w<NP>(sm, [&](int i, int j, float v) { wt[i - wi0][j - wj0] = v; });
-      __syncthreads();
-#pragma unroll
-      for (int r = 0; r < C::TR; r++)
-#pragma unroll
-        for (int c = 0; c < C::TC; c++) sm[S::A + (wi0 + r) * NP + wj0 + c] = wt[r][c];
       if (st == LETKF_OK && tid == 0) a.infl[pt] = infl_update(n, infl, acc.p1, trace, acc.p3);
       if (st != LETKF_OK)
         for (int idx = tid; idx < NP * NP; idx += NT) sm[S::A + idx] = (idx / NP == idx % NP) ? 1.f : 0.f;

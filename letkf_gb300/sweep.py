@@ -19,6 +19,9 @@ PREC_F64 = 0
 PREC_MIXED = 1
 OPT_GRID_CAP = 1
 OPT_MAX_SWEEPS = 2
+OPT_EIGENSOLVER = 3
+EIG_NEWTON_SCHULZ = 0
+EIG_JACOBI = 1
 
 
 class SweepDesc(C.Structure):

@@ -33,9 +33,10 @@ def _spread(xb):
     return np.sqrt(((xb - xb.mean(-1, keepdims=True)) ** 2).sum(-1) / (xb.shape[-1] - 1)).mean()
 
 
-@pytest.mark.parametrize("ne,var_local", [(40, None), (64, [1.0, 0.5, 0.0]), (20, None)])
-def test_mixed_sweep_against_oracle(cuda, ne, var_local):
-    from letkf_gb300.sweep import PREC_MIXED, Sweep
+@pytest.mark.parametrize("ne,var_local,eig", [(40, None, 0), (64, [1.0, 0.5, 0.0], 0), (20, None, 0),
+                                            (100, None, 0), (64, None, 1)])
+def test_mixed_sweep_against_oracle(cuda, ne, var_local, eig):
+    from letkf_gb300.sweep import OPT_EIGENSOLVER, PREC_MIXED, Sweep
 
     case, prm, perm, grd, so, varloc, hdxf, dep = _setup(ne=ne, f32=True, var_local=var_local)
     xb = case["xb"].astype(np.float64)
@@ -48,6 +49,7 @@ def test_mixed_sweep_against_oracle(cuda, ne, var_local):
     sw.set_obs(case["ri"], case["rj"], case["lev"], case["dat"], case["err"], dep, case["cls"],
                hdxf.astype(np.float32), varloc=varloc if var_local is not None else None, var_local_row=var_local)
     np.testing.assert_array_equal(sw.nobsgrd(), grd)
+    sw.set_option(OPT_EIGENSOLVER, eig)
     sw.set_background(case["xb"])
     sw.set_inflation(infl0)
     sw.run()
