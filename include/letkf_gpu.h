@@ -186,6 +186,19 @@ int letkf_sweep_device_buffers(letkf_sweep_t h, void** xb, void** xa, double** i
 /* exclusive scan of n int32 counts into int64 offsets[n+1] (device) */
 int letkf_exclusive_scan(int n, const int* counts, int64_t* offs, void* stream);
 
+/* Allocation-free exclusive scan.  No counterpart in the reference: it exists
+ * for callers that must not allocate device memory (a Fortran driver whose
+ * device memory comes from its own pool, code under a fixed memory budget).
+ * Same result as letkf_exclusive_scan, but its scratch is a 128 KiB device
+ * array inside the library instead of an allocation.
+ *   - n <= LETKF_SCAN_STATIC_MAX_N, else LETKF_ERR_CAPACITY;
+ *   - the first call on a device looks up that array's device address, so
+ *     make it before any stream capture;
+ *   - every call shares the array: calls that overlap on the GPU (other
+ *     streams, other threads) race, so serialise them. */
+#define LETKF_SCAN_STATIC_MAX_N (16 * 1024 * 1024)
+int letkf_exclusive_scan_static(int n, const int* counts, int64_t* offs, void* stream);
+
 /* gather packed local rows: rows_out[r][ne] = ens[idx[r]][ne] (double or
  * float via elem_bytes 8/4), dep_out[r] = dep[idx[r]] */
 int letkf_gather_rows(int ne, int64_t nrows, const int* idx, const void* ens, const void* dep,

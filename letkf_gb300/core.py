@@ -125,6 +125,12 @@ def exclusive_scan(counts, stream=None):
     return offs
 
 
+def exclusive_scan_static(counts, offs, stream=None):
+    """Allocation-free scan into the caller's offs (int64 [n+1]); returns the
+    status code instead of raising, for callers that check it themselves."""
+    return int(lib().letkf_exclusive_scan_static(counts.numel(), _dptr(counts), _dptr(offs), _stream(stream)))
+
+
 def gather_rows(idx, ens, dep, stream=None):
     """rows[r] = ens[idx[r]], dep_out[r] = dep[idx[r]] (same dtype as ens)."""
     import torch

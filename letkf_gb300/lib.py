@@ -51,6 +51,7 @@ _SIGS = {
     "letkf_search_speedy": (_i, [_i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp,
                                  _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "letkf_exclusive_scan": (_i, [_i, _vp, _vp, _vp]),
+    "letkf_exclusive_scan_static": (_i, [_i, _vp, _vp, _vp]),
     "letkf_gather_rows": (_i, [_i, _i64, _vp, _vp, _vp, _i, _vp, _vp, _vp]),
 }
 
