@@ -22,15 +22,15 @@ template <int NP>
 struct MixedCfg;
 template <>
 struct MixedCfg<32> {
-  static constexpr int NT = 64, TR = 4, TC = 4, CH = 32;
+  static constexpr int NT = 64, TR = 4, TC = 4, CH = 32, MINB = 6;
 };
 template <>
 struct MixedCfg<64> {
-  static constexpr int NT = 128, TR = 8, TC = 4, CH = 32;
+  static constexpr int NT = 128, TR = 8, TC = 4, CH = 32, MINB = 4;
 };
 template <>
 struct MixedCfg<128> {
-  static constexpr int NT = 256, TR = 8, TC = 8, CH = 16;
+  static constexpr int NT = 256, TR = 8, TC = 8, CH = 16, MINB = 1;
 };
 
 // Shared-memory layout (floats) of one point's mixed core.
@@ -67,15 +67,15 @@ struct GramAcc {
   static constexpr int TR = MixedCfg<NP>::TR, TC = MixedCfg<NP>::TC;
   float a[TR][TC];
   float bacc;
-  double p1, p3;  // thread 0 only
+  float p1, p3;  // per-thread partial inflation sums; block totals after gram_finish
   __device__ void zero() {
 #pragma unroll
     for (int r = 0; r < TR; r++)
 #pragma unroll
       for (int c = 0; c < TC; c++) a[r][c] = 0.f;
     bacc = 0.f;
-    p1 = 0.0;
-    p3 = 0.0;
+    p1 = 0.f;
+    p3 = 0.f;
   }
 };
 
@@ -117,19 +117,18 @@ __device__ __forceinline__ void gram_chunk(const float* sm, int nr, GramAcc<NP>&
     for (int r = 0; r < nr; r++) s = fmaf(yw[r * NP + tid], sm[S::DR + r], s);
     acc.bacc = s;
   }
-  if (tid == 0) {
-    for (int r = 0; r < nr; r++) {
-      const double dd = sm[S::DR + r];
-      acc.p1 += dd * dd * (double)sm[S::WR + r];
-      acc.p3 += (double)sm[S::RL + r];
-    }
+  if (tid < nr) {  // one staged row per thread (CH <= NT)
+    const float dd = sm[S::DR + tid];
+    acc.p1 = fmaf(dd * dd, sm[S::WR + tid], acc.p1);
+    acc.p3 += sm[S::RL + tid];
   }
 }
 
 // Write the Gram tiles into sm[A] (symmetrised from the lower triangle), the
-// departure product into sm[B], and return trace(Gram) in FP64 (all threads).
+// departure product into sm[B], reduce the inflation sums into acc.p1 / acc.p3
+// of every thread, and return trace(Gram) in FP64 (all threads).
 template <int NP>
-__device__ __forceinline__ double gram_finish(float* sm, const GramAcc<NP>& acc) {
+__device__ __forceinline__ double gram_finish(float* sm, GramAcc<NP>& acc) {
   using C = MixedCfg<NP>;
   using S = MixedSmem<NP>;
   constexpr int NTI = NP / C::TR;
@@ -148,10 +147,13 @@ __device__ __forceinline__ double gram_finish(float* sm, const GramAcc<NP>& acc)
     const int i = idx / NP, j = idx - i * NP;
     if (i < j) A[idx] = A[j * NP + i];
   }
-  double tr = 0.0;
-  for (int i = tid; i < NP; i += C::NT) tr += (double)A[i * NP + i];
-  double* red = reinterpret_cast<double*>(sm + S::RED);
-  return block_sum<double, C::NT>(tr, red);
+  float tr = 0.f;
+  for (int i = tid; i < NP; i += C::NT) tr += A[i * NP + i];
+  float* red = sm + S::RED;
+  const float trace = block_sum<float, C::NT>(tr, red);
+  acc.p1 = block_sum<float, C::NT>(acc.p1, red);
+  acc.p3 = block_sum<float, C::NT>(acc.p3, red);
+  return (double)trace;
 }
 
 // Parallel cyclic Jacobi on sm[A] (symmetric, NP x NP), eigenvectors into
@@ -334,12 +336,12 @@ __device__ float ns_invsqrt(float* sm, float cdiag, int max_iter, int* iters) {
   float* xv = sm + S::G;   // power-iteration vector
   float* yv = sm + S::LAM;
   float* redf = sm + S::RED;
-  double* red = reinterpret_cast<double*>(sm + S::RED);
-  // Gershgorin bound (>= lambda_max) and a power-iteration estimate
+  // Gershgorin bound (>= lambda_max) and a power-iteration estimate.  A is
+  // symmetric: row i is read as column i (consecutive lanes, no bank conflicts).
   float g = 0.f;
   if (tid < NP) {
     float s = 0.f;
-    for (int j = 0; j < NP; j++) s += fabsf(A[tid * NP + j]);
+    for (int j = 0; j < NP; j++) s += fabsf(A[j * NP + tid]);
     g = s;
     xv[tid] = A[tid * NP + tid] * (1.f + 0.25f * __sinf(1.7f * tid));
   }
@@ -352,19 +354,18 @@ __device__ float ns_invsqrt(float* sm, float cdiag, int max_iter, int* iters) {
   __syncthreads();
   float lam = 0.f;
   for (int it = 0; it < 8; it++) {
-    double part = 0.0;
+    float part = 0.f, xx = 0.f;
     if (tid < NP) {
       float s = 0.f;
-      for (int j = 0; j < NP; j++) s = fmaf(A[tid * NP + j], xv[j], s);
+      for (int j = 0; j < NP; j++) s = fmaf(A[j * NP + tid], xv[j], s);
       yv[tid] = s;
-      part = (double)s * (double)s;
+      part = s * s;
+      xx = xv[tid] * xv[tid];
     }
-    const double nrm2 = block_sum<double, C::NT>(part, red);
-    double xx = 0.0;
-    if (tid < NP) xx = (double)xv[tid] * (double)xv[tid];
-    const double x2 = block_sum<double, C::NT>(xx, red);
-    lam = (float)sqrt(nrm2 / fmax(x2, 1e-300));
-    const float inv = (float)(1.0 / sqrt(fmax(nrm2, 1e-300)));
+    const float nrm2 = block_sum<float, C::NT>(part, redf);
+    const float x2 = block_sum<float, C::NT>(xx, redf);
+    lam = sqrtf(nrm2 / fmaxf(x2, 1e-30f));
+    const float inv = rsqrtf(fmaxf(nrm2, 1e-30f));
     if (tid < NP) xv[tid] = yv[tid] * inv;
     __syncthreads();
   }
@@ -383,18 +384,18 @@ __device__ float ns_invsqrt(float* sm, float cdiag, int max_iter, int* iters) {
   for (; it < max_iter; it++) {
     // T = Z Y and ||T - I||_F^2
     sym_gemm_tile<NP>(Z, A, i0, j0, acc);
-    double e2 = 0.0;
+    float e2 = 0.f;
 #pragma unroll
     for (int a = 0; a < C::TR; a++)
 #pragma unroll
       for (int b = 0; b < C::TC; b++) {
         T[(i0 + a) * NP + j0 + b] = acc[a][b];
         const float d = acc[a][b] - ((i0 + a) == (j0 + b) ? 1.f : 0.f);
-        e2 += (double)d * (double)d;
+        e2 = fmaf(d, d, e2);
       }
-    e2 = block_sum<double, C::NT>(e2, red);  // also publishes T
+    e2 = block_sum<float, C::NT>(e2, redf);  // also publishes T
     // ||T - I||_F < 1e-4: one more (quadratically convergent) step reaches the FP32 floor
-    if (e2 < 1.0e-8) last = true;
+    if (e2 < 1.0e-8f) last = true;
     // Y' = 1.5 Y - 0.5 Y T ; Z' = 1.5 Z - 0.5 T Z
     float ynew[C::TR][C::TC];
     sym_gemm_tile<NP>(A, T, i0, j0, acc);

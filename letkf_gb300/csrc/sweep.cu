@@ -119,7 +119,7 @@ struct letkf_sweep_s {
   letkf_sweep_desc d;
   int nobs = 0;
   // points
-  double *pri = nullptr, *prj = nullptr, *prlev = nullptr, *prz = nullptr;
+  double *pri = nullptr, *prj = nullptr, *prlev = nullptr, *prz = nullptr, *plogr = nullptr;
   int* order = nullptr;
   // sorted observations
   double *ori = nullptr, *orj = nullptr, *olev = nullptr, *odat = nullptr, *oerr = nullptr, *odep = nullptr;
@@ -173,6 +173,7 @@ int letkf_sweep_create(letkf_sweep_t* out, const letkf_sweep_desc* d) {
   st |= dalloc(&h->prj, np);
   st |= dalloc(&h->prlev, np);
   st |= dalloc(&h->prz, np);
+  st |= dalloc(&h->plogr, np);
   st |= dalloc(&h->order, np);
   st |= dalloc((char**)&h->xb, np * d->nv * d->ne * elem(h));
   st |= dalloc((char**)&h->xa, np * d->nv * d->ne * elem(h));
@@ -198,7 +199,7 @@ int letkf_sweep_create(letkf_sweep_t* out, const letkf_sweep_desc* d) {
 int letkf_sweep_destroy(letkf_sweep_t h) {
   if (!h) return LETKF_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
-  void* ptrs[] = {h->pri,  h->prj,   h->prlev, h->prz,   h->order, h->ori,     h->orj,    h->olev,
+  void* ptrs[] = {h->pri,  h->prj,   h->prlev, h->prz,   h->plogr,   h->order, h->ori,     h->orj,    h->olev,
                   h->odat, h->oerr,  h->odep,  h->ocls,  h->ovarloc, h->G,     h->var_local, h->obsF,
                   h->obsA, h->meta,  h->ens32, h->ens64, h->xb,    h->xa,      h->infl,   h->status,
                   h->nobsl, h->sweeps, h->counter};
@@ -226,7 +227,10 @@ int letkf_sweep_set_points(letkf_sweep_t h, const double* ri, const double* rj, 
     }
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key[a] < key[b]; });
   }
+  std::vector<double> lg(np);
+  for (int p = 0; p < np; p++) lg[p] = std::log(rlev[p]);
   cudaStream_t s = h->stream;
+  cudaMemcpyAsync(h->plogr, lg.data(), sizeof(double) * np, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(h->pri, ri, sizeof(double) * np, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(h->prj, rj, sizeof(double) * np, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(h->prlev, rlev, sizeof(double) * np, cudaMemcpyHostToDevice, s);
@@ -489,6 +493,7 @@ int letkf_sweep_run(letkf_sweep_t h, void* stream) {
   a.prj = h->prj;
   a.prlev = h->prlev;
   a.prz = h->prz;
+  a.plogr = h->plogr;
   a.xb = (const float*)h->xb;
   a.xa = (float*)h->xa;
   a.infl = h->infl;

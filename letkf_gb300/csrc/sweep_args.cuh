@@ -21,6 +21,7 @@ struct SweepArgs {
   const float* ens_obs;   // [nobs][n]
   const int* order;       // [npts]
   const double *pri, *prj, *prlev, *prz;
+  const double* plogr;    // [npts] log(rlev)
   const float* xb;        // [nv][npts][n]
   float* xa;
   double* infl;           // [npts] in/out

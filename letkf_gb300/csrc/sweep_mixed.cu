@@ -81,7 +81,7 @@ struct SweepSmem {
 };
 
 template <int NP>
-__global__ void __launch_bounds__(MixedCfg<NP>::NT) sweep_mixed_kernel(SweepArgs a) {
+__global__ void __launch_bounds__(MixedCfg<NP>::NT, MixedCfg<NP>::MINB) sweep_mixed_kernel(SweepArgs a) {
   using C = MixedCfg<NP>;
   using S = MixedSmem<NP>;
   using W = SweepSmem<NP>;
@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(MixedCfg<NP>::NT) sweep_mixed_kernel(SweepArgs
     if (q >= a.npts) break;
     const int pt = a.order[q];
     const double ri = a.pri[pt], rj = a.prj[pt], rlev = a.prlev[pt], rz = a.prz ? a.prz[pt] : 0.0;
-    const double logr = log(rlev);
+    const double logr = a.plogr[pt];
     const float rif = (float)ri, rjf = (float)rj, logrf = (float)logr, rzf = (float)rz;
     int imin = (int)floor(ri - a.P.dlon_zero), imax = (int)ceil(ri + a.P.dlon_zero);
     int jmin = (int)floor(rj - a.P.dlat_zero), jmax = (int)ceil(rj + a.P.dlat_zero);
@@ -283,13 +283,13 @@ __global__ void __launch_bounds__(MixedCfg<NP>::NT) sweep_mixed_kernel(SweepArgs
         const float* Z = sm + S::V;
         if (tid < NP) {
           float acc_g = 0.f;
-          for (int j = 0; j < NP; j++) acc_g = fmaf(Z[tid * NP + j], sm[S::B + j], acc_g);
+          for (int j = 0; j < NP; j++) acc_g = fmaf(Z[j * NP + tid], sm[S::B + j], acc_g);
           sm[S::G + tid] = acc_g;
         }
         __syncthreads();
         if (tid < NP) {
           float acc_w = 0.f;
-          for (int j = 0; j < NP; j++) acc_w = fmaf(Z[tid * NP + j], sm[S::G + j], acc_w);
+          for (int j = 0; j < NP; j++) acc_w = fmaf(Z[j * NP + tid], sm[S::G + j], acc_w);
           sm[S::WB + tid] = acc_w / s;
         }
         const float coef = sqrtf((float)(n - 1) / s);
@@ -341,21 +341,19 @@ __global__ void __launch_bounds__(MixedCfg<NP>::NT) sweep_mixed_kernel(SweepArgs
       xs[v * NP + m] = a.xb[((size_t)v * a.npts + pt) * n + m];
     }
     __syncthreads();
-    if (tid < nv) {
-      double s = 0.0;
-      for (int m = 0; m < n; m++) s += (double)xs[tid * NP + m];
-      meanv[tid] = s / (double)n;
-    }
-    __syncthreads();
-    for (int t = tid; t < nv * n; t += NT) {
-      const int v = t / n, m = t - v * n;
-      xs[v * NP + m] = (float)((double)xs[v * NP + m] - meanv[v]);
-    }
-    __syncthreads();
-    if (tid < nv) {
+    // mean and mean increment in FP64, one warp per variable
+    for (int v = wid; v < nv; v += NT / 32) {
+      double sx = 0.0;
+      for (int m = lane; m < n; m += 32) sx += (double)xs[v * NP + m];
+      const double mean = warp_sum(sx) / (double)n;
       double dlt = 0.0;
-      for (int k = 0; k < n; k++) dlt += (double)xs[tid * NP + k] * (double)sm[S::WB + k];
-      meanv[8 + tid] = meanv[tid] + dlt;  // analysis mean, FP64
+      for (int m = lane; m < n; m += 32) {
+        const float xp = (float)((double)xs[v * NP + m] - mean);
+        xs[v * NP + m] = xp;
+        dlt += (double)xp * (double)sm[S::WB + m];
+      }
+      dlt = warp_sum(dlt);
+      if (lane == 0) meanv[8 + v] = mean + dlt;  // analysis mean, FP64
     }
     __syncthreads();
     for (int t = tid; t < nv * n; t += NT) {
