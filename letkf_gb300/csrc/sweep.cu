@@ -21,6 +21,7 @@ namespace letkf {
 struct SweepScaleParams;
 struct SweepArgs;
 int launch_sweep_mixed(const SweepArgs& a, cudaStream_t stream, int grid_cap);
+int launch_sweep_tc(const SweepArgs& a, cudaStream_t stream, int grid_cap);
 int launch_sweep_prep_obs(int, const double*, const double*, const double*, const double*, const double*,
                           const double*, const int*, const int*, const double*, const double*, float4*, float4*, int*,
                           cudaStream_t);
@@ -133,10 +134,12 @@ struct letkf_sweep_s {
   void *xb = nullptr, *xa = nullptr;
   double* infl = nullptr;
   int *status = nullptr, *nobsl = nullptr, *sweeps = nullptr, *counter = nullptr;
+  int *defer_list = nullptr, *defer_count = nullptr, *err_flag = nullptr;
   cudaStream_t stream = nullptr;
   int grid_cap = 0;
   int max_sweeps = 12;
   int use_ns = 1;
+  int use_tc = 1;
 };
 
 static void dfree(void* p) {
@@ -182,6 +185,9 @@ int letkf_sweep_create(letkf_sweep_t* out, const letkf_sweep_desc* d) {
   st |= dalloc(&h->nobsl, np);
   st |= dalloc(&h->sweeps, np);
   st |= dalloc(&h->counter, 1);
+  st |= dalloc(&h->defer_list, np);
+  st |= dalloc(&h->defer_count, 1);
+  st |= dalloc(&h->err_flag, 1);
   st |= dalloc(&h->G, (size_t)(d->nlon + 1) * d->nlat);
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) st = LETKF_ERR_CUDA;
   if (st != LETKF_OK) {
@@ -190,6 +196,7 @@ int letkf_sweep_create(letkf_sweep_t* out, const letkf_sweep_desc* d) {
   }
   cudaMemset(h->prz, 0, np * sizeof(double));
   cudaMemset(h->G, 0, sizeof(int) * (d->nlon + 1) * d->nlat);
+  cudaMemset(h->err_flag, 0, sizeof(int));
   std::vector<double> one(np, 1.0);
   cudaMemcpy(h->infl, one.data(), np * sizeof(double), cudaMemcpyHostToDevice);
   *out = h;
@@ -202,7 +209,7 @@ int letkf_sweep_destroy(letkf_sweep_t h) {
   void* ptrs[] = {h->pri,  h->prj,   h->prlev, h->prz,   h->plogr,   h->order, h->ori,     h->orj,    h->olev,
                   h->odat, h->oerr,  h->odep,  h->ocls,  h->ovarloc, h->G,     h->var_local, h->obsF,
                   h->obsA, h->meta,  h->ens32, h->ens64, h->xb,    h->xa,      h->infl,   h->status,
-                  h->nobsl, h->sweeps, h->counter};
+                  h->nobsl, h->sweeps, h->counter, h->defer_list, h->defer_count, h->err_flag};
   for (void* p : ptrs) dfree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -395,6 +402,10 @@ int letkf_sweep_set_option(letkf_sweep_t h, int option, int value) {
       if (value < 1 || value > 64) return LETKF_ERR_ARG;
       h->max_sweeps = value;
       return LETKF_OK;
+    case LETKF_OPT_TENSOR_CORES:
+      if (value != 0 && value != 1) return LETKF_ERR_ARG;
+      h->use_tc = value;
+      return LETKF_OK;
     case LETKF_OPT_EIGENSOLVER:
       if (value != LETKF_EIG_NEWTON_SCHULZ && value != LETKF_EIG_JACOBI) return LETKF_ERR_ARG;
       h->use_ns = value == LETKF_EIG_NEWTON_SCHULZ;
@@ -505,15 +516,37 @@ int letkf_sweep_run(letkf_sweep_t h, void* stream) {
   a.max_sweeps = h->max_sweeps;
   a.max_ns_iter = 24;
   a.use_ns = h->use_ns;
+  a.err_flag = h->err_flag;
   cudaMemsetAsync(h->counter, 0, sizeof(int), s);
+  if (h->use_tc && h->use_ns && h->d.ne <= 64) {
+    // tensor-core sweep, then the Jacobi pass over the points it deferred
+    a.defer_list = h->defer_list;
+    a.defer_count = h->defer_count;
+    cudaMemsetAsync(h->defer_count, 0, sizeof(int), s);
+    int st = launch_sweep_tc(a, s, h->grid_cap);
+    if (st != LETKF_OK) return st;
+    SweepArgs b = a;
+    b.order = h->defer_list;
+    b.npts_dev = h->defer_count;
+    b.use_ns = 0;
+    cudaMemsetAsync(h->counter, 0, sizeof(int), s);
+    return launch_sweep_mixed(b, s, h->grid_cap);
+  }
   return launch_sweep_mixed(a, s, h->grid_cap);
+}
+
+static int check_err(letkf_sweep_t h) {
+  int f = 0;
+  if (cudaMemcpy(&f, h->err_flag, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return LETKF_ERR_CUDA;
+  return f ? LETKF_ERR_TIMEOUT : LETKF_OK;
 }
 
 int letkf_sweep_get_analysis(letkf_sweep_t h, void* xa, int on_device) {
   if (!h || !xa) return LETKF_ERR_ARG;
   const size_t bytes = (size_t)h->d.npts * h->d.nv * h->d.ne * elem(h);
   cudaMemcpyAsync(xa, h->xa, bytes, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream);
-  return cuda_status(cudaStreamSynchronize(h->stream));
+  const int st = cuda_status(cudaStreamSynchronize(h->stream));
+  return st != LETKF_OK ? st : check_err(h);
 }
 
 int letkf_sweep_get_diagnostics(letkf_sweep_t h, double* infl, int* nobsl, int* status, int* sweeps) {
@@ -524,7 +557,8 @@ int letkf_sweep_get_diagnostics(letkf_sweep_t h, double* infl, int* nobsl, int* 
   if (nobsl) cudaMemcpy(nobsl, h->nobsl, sizeof(int) * np, cudaMemcpyDeviceToHost);
   if (status) cudaMemcpy(status, h->status, sizeof(int) * np, cudaMemcpyDeviceToHost);
   if (sweeps) cudaMemcpy(sweeps, h->sweeps, sizeof(int) * np, cudaMemcpyDeviceToHost);
-  return cuda_status(cudaGetLastError());
+  const int st = cuda_status(cudaGetLastError());
+  return st != LETKF_OK ? st : check_err(h);
 }
 
 int letkf_sweep_sorted_obs(letkf_sweep_t h, int* nobsgrd) {

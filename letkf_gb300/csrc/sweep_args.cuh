@@ -33,6 +33,10 @@ struct SweepArgs {
   int max_sweeps;   // Jacobi sweeps (fallback eigensolver)
   int max_ns_iter;  // Newton-Schulz iterations
   int use_ns;       // 1: Newton-Schulz inverse square root, 0: Jacobi eigensolver
+  const int* npts_dev;  // if set, the number of entries of `order` to process (device scalar)
+  int* defer_list;      // tensor-core sweep: points handed to the Jacobi pass
+  int* defer_count;
+  int* err_flag;        // set when a bounded wait gave up
 };
 
 }  // namespace letkf

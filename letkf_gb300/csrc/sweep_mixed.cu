@@ -103,12 +103,13 @@ __global__ void __launch_bounds__(MixedCfg<NP>::NT, MixedCfg<NP>::MINB) sweep_mi
   const float band_lo = dzf2 * (1.f - SW_BAND), band_hi = dzf2 * (1.f + SW_BAND);
   const float dx2 = (float)(a.P.dx * a.P.dx), dy2 = (float)(a.P.dy * a.P.dy);
 
+  const int npts_work = a.npts_dev ? *a.npts_dev : a.npts;
   for (;;) {
     __syncthreads();
     if (tid == 0) ctrl[0] = atomicAdd(a.counter, 1);
     __syncthreads();
     const int q = ctrl[0];
-    if (q >= a.npts) break;
+    if (q >= npts_work) break;
     const int pt = a.order[q];
     const double ri = a.pri[pt], rj = a.prj[pt], rlev = a.prlev[pt], rz = a.prz ? a.prz[pt] : 0.0;
     const double logr = a.plogr[pt];

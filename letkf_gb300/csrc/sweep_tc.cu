@@ -1,0 +1,553 @@
+// sweep_tc.cu -- fused analysis sweep with the contractions on the tcgen05 tensor cores.
+//
+// Same work as sweep_mixed.cu (search, Gram, transform, update per grid point,
+// one persistent launch), for ensembles up to 64 members, with the two
+// contraction stages issued as tcgen05.mma (kind::f16, bf16 operands, FP32
+// accumulation in tensor memory) from shared-memory descriptors:
+//
+//  * Gram  G = Ywᵀ Y (common/common_letkf.f90:101-118): every chunk of 32
+//    accepted observations is staged as A = [Yw_hiᵀ ; Yw_loᵀ] (128 x 32) and
+//    B = Y_hi, Y_lo (64 x 32, K-major), where x_hi = bf16(x) and
+//    x_lo = bf16(x - x_hi).  Two M=128 MMAs accumulate D0 = A Y_hiᵀ and
+//    D1 = A Y_loᵀ in TMEM; G is the sum of their four 64 x 64 blocks, i.e. the
+//    product of the two-term splits (about 16 significant bits per factor).
+//    Staging of chunk c+1 overlaps the MMAs of chunk c (two buffers, one
+//    mbarrier each).
+//  * Newton-Schulz  A^(-1/2): the iterates Y, Z commute, so one iteration is
+//    T = Z Y and [Y;Z] <- 1.5 [Y;Z] - 0.5 [Y;Z] T: two M=128 MMAs with the
+//    stacked operand S = [Y;Z] (128 x 64) and B = Y or T (64 x 64), each as
+//    the three split products hi.hi + hi.lo + lo.hi.
+//
+// Points where the transform needs mtx_eigen's truncation semantics (c <= 0 or
+// tr(G) >= 1e6 c) are appended to a deferred list for the Jacobi pass.
+#include <cuda_bf16.h>
+
+#include "mixed_core.cuh"
+#include "sweep_search.cuh"
+#include "tc_sm100.cuh"
+
+namespace letkf {
+
+constexpr int TC_NT = 128;
+constexpr int TC_CH = 32;
+constexpr int TC_NP = 64;
+constexpr uint32_t TC_TMEM_COLS = 128;
+constexpr uint32_t TC_WAIT = 1u << 22;
+
+// byte offsets in dynamic shared memory
+struct TcLayout {
+  // operand region, 48 KB, reused by phase
+  static constexpr int STG = 0;           // two Gram stages of 16 KB
+  static constexpr int STG_A = 0;         //   A = [Yw_hi^T; Yw_lo^T]: 128 x 32 bf16 (8 KB)
+  static constexpr int STG_BH = 8192;     //   Y_hi^T: 64 x 32 bf16 (4 KB)
+  static constexpr int STG_BL = 12288;    //   Y_lo^T
+  static constexpr int STG_SIZE = 16384;
+  static constexpr int S_HI = 0;          // Newton-Schulz S = [Y; Z]: 128 x 64 bf16 (16 KB)
+  static constexpr int S_LO = 16384;
+  static constexpr int B_HI = 32768;      // B = Y or T: 64 x 64 bf16 (8 KB)
+  static constexpr int B_LO = 40960;
+  static constexpr int GTMP = 32768;      // Gram in FP32, 64 x 64 row-major (over B)
+  static constexpr int WMAT = 32768;      // transform W in FP32, 64 x 64 row-major (over B)
+  static constexpr int XS = 0;            // update staging, nv x 64 FP32 (over S)
+  static constexpr int OPER_END = 49152;
+  // small data
+  static constexpr int VB = OPER_END;            // float[64] departure product
+  static constexpr int VBP = VB + 256;           // float[128] partial departure products
+  static constexpr int VWB = VBP + 512;          // float[64] wbar
+  static constexpr int VG = VWB + 256;           // float[64]
+  static constexpr int VX = VG + 256;            // float[64] power iteration
+  static constexpr int VY = VX + 256;            // float[64]
+  static constexpr int RED = VY + 256;           // float[64]
+  static constexpr int PIDX = RED + 256;         // int[CH+NT]
+  static constexpr int PW = PIDX + 4 * (TC_CH + TC_NT);
+  static constexpr int PD = PW + 4 * (TC_CH + TC_NT);
+  static constexpr int PR = PD + 4 * (TC_CH + TC_NT);
+  static constexpr int ROWIB = PR + 4 * (TC_CH + TC_NT);
+  static constexpr int ROWPRE = ROWIB + 4 * SW_MAXROWS;
+  static constexpr int WCNT = ROWPRE + 4 * (SW_MAXROWS + 1);
+  static constexpr int MEAN = ((WCNT + 4 * (TC_NT / 32 + 2)) + 7) & ~7;  // double[16]
+  static constexpr int MBAR = MEAN + 128;        // uint64[3]
+  static constexpr int TMEMH = MBAR + 24;        // uint32
+  static constexpr int CTRL = TMEMH + 8;         // int[4]
+  static constexpr int TOTAL = CTRL + 16;
+};
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+// 8 values -> hi and lo bf16 packs (16 bytes each)
+__device__ __forceinline__ void split8(const float* v, uint4& hi, uint4& lo) {
+  float h[8], l[8];
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    h[j] = __bfloat162float(__float2bfloat16_rn(v[j]));
+    l[j] = v[j] - h[j];
+  }
+  hi = make_uint4(pack_bf16x2(h[0], h[1]), pack_bf16x2(h[2], h[3]), pack_bf16x2(h[4], h[5]), pack_bf16x2(h[6], h[7]));
+  lo = make_uint4(pack_bf16x2(l[0], l[1]), pack_bf16x2(l[2], l[3]), pack_bf16x2(l[4], l[5]), pack_bf16x2(l[6], l[7]));
+}
+
+__device__ __forceinline__ void unpack8(uint4 p, float* v) {
+  const uint32_t w[4] = {p.x, p.y, p.z, p.w};
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const __nv_bfloat162 b = *reinterpret_cast<const __nv_bfloat162*>(&w[j]);
+    v[2 * j] = __low2float(b);
+    v[2 * j + 1] = __high2float(b);
+  }
+}
+
+// 12 MMAs: D = S_hi B_hi + S_hi B_lo + S_lo B_hi over K = 64 (4 steps of 16)
+__device__ __forceinline__ void ns_mma(uint32_t d, uint32_t s_hi, uint32_t s_lo, uint32_t b_hi, uint32_t b_lo,
+                                       uint32_t idesc) {
+#pragma unroll
+  for (int pass = 0; pass < 3; pass++) {
+    const uint32_t sa = pass == 2 ? s_lo : s_hi;
+    const uint32_t sb = pass == 1 ? b_lo : b_hi;
+#pragma unroll
+    for (int s = 0; s < 4; s++)
+      tc::mma_bf16(d, tc::smem_desc(sa + s * 256, 128, 1024), tc::smem_desc(sb + s * 256, 128, 1024), idesc,
+                   (pass == 0 && s == 0) ? 0u : 1u);
+  }
+}
+
+__global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
+  using L = TcLayout;
+  extern __shared__ __align__(1024) unsigned char sm[];
+  float* vb = reinterpret_cast<float*>(sm + L::VB);
+  float* vbp = reinterpret_cast<float*>(sm + L::VBP);
+  float* vwb = reinterpret_cast<float*>(sm + L::VWB);
+  float* vg = reinterpret_cast<float*>(sm + L::VG);
+  float* vx = reinterpret_cast<float*>(sm + L::VX);
+  float* vy = reinterpret_cast<float*>(sm + L::VY);
+  float* red = reinterpret_cast<float*>(sm + L::RED);
+  double* meanv = reinterpret_cast<double*>(sm + L::MEAN);
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + L::MBAR);
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(sm + L::TMEMH);
+  int* ctrl = reinterpret_cast<int*>(sm + L::CTRL);
+  SearchSmem ss;
+  ss.pidx = reinterpret_cast<int*>(sm + L::PIDX);
+  ss.pw = reinterpret_cast<float*>(sm + L::PW);
+  ss.pd = reinterpret_cast<float*>(sm + L::PD);
+  ss.pr = reinterpret_cast<float*>(sm + L::PR);
+  ss.rowib = reinterpret_cast<int*>(sm + L::ROWIB);
+  ss.rowpre = reinterpret_cast<int*>(sm + L::ROWPRE);
+  ss.wcnt = reinterpret_cast<int*>(sm + L::WCNT);
+  float* Gt = reinterpret_cast<float*>(sm + L::GTMP);
+  float* Wm = reinterpret_cast<float*>(sm + L::WMAT);
+  float* xs = reinterpret_cast<float*>(sm + L::XS);
+
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int n = a.n, nv = a.nv;
+  const uint32_t sbase = tc::smem_u32(sm);
+  const uint32_t idesc = tc::idesc_bf16(128, 64);
+
+  if (tid == 0) {
+    tc::mbar_init(&mbar[0], 1);
+    tc::mbar_init(&mbar[1], 1);
+    tc::mbar_init(&mbar[2], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (wid == 0) tc::tmem_alloc(tmem_holder, TC_TMEM_COLS);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tbase = *tmem_holder;
+  const uint32_t D0 = tbase, D1 = tbase + 64;
+  const uint32_t lane_off = (uint32_t)(wid * 32) << 16;
+  const int r = tid;  // the tile row this thread owns in TMEM / S
+  uint32_t par[3] = {0u, 0u, 0u};
+  bool outst[2] = {false, false};
+  int tmo = 0;  // this thread saw a bounded wait give up
+  const int npts_work = a.npts_dev ? *a.npts_dev : a.npts;
+
+  auto wait_bar = [&](int i) {
+    if (!tc::mbar_wait(&mbar[i], par[i], TC_WAIT)) tmo = 1;
+    par[i] ^= 1u;
+  };
+
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) ctrl[0] = atomicAdd(a.counter, 1);
+    __syncthreads();
+    const int q = ctrl[0];
+    if (q >= npts_work) break;
+    const int pt = a.order[q];
+    const double ri = a.pri[pt], rj = a.prj[pt], rz = a.prz ? a.prz[pt] : 0.0;
+    const double logr = a.plogr[pt];
+
+    // ---- search + Gram on the tensor cores ----
+    const int m = tid & 63, hh = tid >> 6;
+    float bpart = 0.f, p1 = 0.f, p3 = 0.f;
+    int chunk = 0;
+    bool first = true;
+    auto flush = [&](int nr) {
+      const int buf = chunk & 1;
+      if (outst[buf]) {
+        wait_bar(buf);
+        outst[buf] = false;
+      }
+      tc::fence_after_sync();
+      unsigned char* stg = sm + L::STG + buf * L::STG_SIZE;
+      float yv[16], wv[16];
+#pragma unroll
+      for (int kk = 0; kk < 16; kk++) {
+        const int k = hh * 16 + kk;
+        float y = 0.f, w = 0.f, dd = 0.f;
+        if (k < nr) {
+          w = ss.pw[k];
+          dd = ss.pd[k];
+          if (m < n) y = a.ens_obs[(size_t)ss.pidx[k] * n + m];
+        }
+        yv[kk] = y;
+        wv[kk] = y * w;
+        bpart = fmaf(wv[kk], dd, bpart);
+      }
+#pragma unroll
+      for (int g = 0; g < 2; g++) {
+        uint4 h, l;
+        const uint32_t off = tc::kmajor_off_bf16(m, hh * 16 + g * 8, TC_CH);
+        split8(wv + 8 * g, h, l);
+        *reinterpret_cast<uint4*>(stg + L::STG_A + off) = h;
+        *reinterpret_cast<uint4*>(stg + L::STG_A + tc::kmajor_off_bf16(64 + m, hh * 16 + g * 8, TC_CH)) = l;
+        split8(yv + 8 * g, h, l);
+        *reinterpret_cast<uint4*>(stg + L::STG_BH + off) = h;
+        *reinterpret_cast<uint4*>(stg + L::STG_BL + off) = l;
+      }
+      if (tid < nr) {
+        const float dd = ss.pd[tid];
+        p1 = fmaf(dd * dd, ss.pw[tid], p1);
+        p3 += ss.pr[tid];
+      }
+      tc::fence_smem_async();
+      tc::fence_before_sync();
+      __syncthreads();
+      if (tid == 0) {
+        tc::fence_after_sync();
+        const uint32_t sa = sbase + L::STG + buf * L::STG_SIZE;
+#pragma unroll
+        for (int s = 0; s < 2; s++)
+          tc::mma_bf16(D0, tc::smem_desc(sa + L::STG_A + s * 256, 128, 512),
+                       tc::smem_desc(sa + L::STG_BH + s * 256, 128, 512), idesc, (first && s == 0) ? 0u : 1u);
+#pragma unroll
+        for (int s = 0; s < 2; s++)
+          tc::mma_bf16(D1, tc::smem_desc(sa + L::STG_A + s * 256, 128, 512),
+                       tc::smem_desc(sa + L::STG_BL + s * 256, 128, 512), idesc, (first && s == 0) ? 0u : 1u);
+        tc::mma_commit(&mbar[buf]);
+      }
+      outst[buf] = true;
+      first = false;
+      chunk++;
+    };
+    const int Lp = sweep_search<TC_NT, TC_CH>(a, ri, rj, logr, rz, ss, flush);
+    for (int b = 0; b < 2; b++)
+      if (outst[b]) {
+        wait_bar(b);
+        outst[b] = false;
+      }
+    tc::fence_after_sync();
+    if (__syncthreads_or(tmo)) {
+      tmo = 1;
+      break;
+    }
+
+    double infl = a.infl[pt];
+    bool deferred = false;
+    if (Lp > 0) {
+      if (a.minfl > 0.0 && infl < a.minfl) infl = a.minfl;
+      const float cdiag = (float)((double)(n - 1) / infl);
+      // G = D0[r] + D0[r+64] + D1[r] + D1[r+64]: warps 2-3 first, then warps 0-1 add
+      if (wid >= 2) {
+#pragma unroll
+        for (int c0 = 0; c0 < 64; c0 += 16) {
+          float v0[16], v1[16];
+          tc::tmem_ld16(D0 + lane_off + c0, v0);
+          tc::tmem_ld16(D1 + lane_off + c0, v1);
+          float* dst = Gt + (r - 64) * 64 + c0;
+#pragma unroll
+          for (int j = 0; j < 16; j += 4)
+            *reinterpret_cast<float4*>(dst + j) =
+                make_float4(v0[j] + v1[j], v0[j + 1] + v1[j + 1], v0[j + 2] + v1[j + 2], v0[j + 3] + v1[j + 3]);
+        }
+      }
+      vbp[tid] = bpart;
+      __syncthreads();
+      if (wid < 2) {
+#pragma unroll
+        for (int c0 = 0; c0 < 64; c0 += 16) {
+          float v0[16], v1[16];
+          tc::tmem_ld16(D0 + lane_off + c0, v0);
+          tc::tmem_ld16(D1 + lane_off + c0, v1);
+          float* dst = Gt + r * 64 + c0;
+#pragma unroll
+          for (int j = 0; j < 16; j++) dst[j] += v0[j] + v1[j];
+        }
+        vb[r] = vbp[r] + vbp[r + 64];
+      }
+      tc::fence_before_sync();
+      __syncthreads();
+      // symmetrise (pairs owned by one thread) and take the trace
+      for (int idx = tid; idx < 64 * 64; idx += TC_NT) {
+        const int i = idx >> 6, j = idx & 63;
+        if (i < j) {
+          const float v = 0.5f * (Gt[i * 64 + j] + Gt[j * 64 + i]);
+          Gt[i * 64 + j] = v;
+          Gt[j * 64 + i] = v;
+        }
+      }
+      __syncthreads();
+      const float trace = block_sum<float, TC_NT>(tid < 64 ? Gt[tid * 64 + tid] : 0.f, red);
+      p1 = block_sum<float, TC_NT>(p1, red);
+      p3 = block_sum<float, TC_NT>(p3, red);
+      if (!(cdiag > 0.f) || !((double)trace < 1.0e6 * (double)cdiag)) {
+        deferred = true;  // needs the eigensolver with mtx_eigen's truncation
+      } else {
+        if (tid < 64) Gt[tid * 64 + tid] += cdiag;
+        __syncthreads();
+        // scaling s: power iteration guarded by the Gershgorin bound (s >= lambda_max / 2)
+        float gsum = 0.f;
+        if (tid < 64) {
+          for (int j = 0; j < 64; j++) gsum += fabsf(Gt[j * 64 + tid]);
+          vx[tid] = Gt[tid * 64 + tid] * (1.f + 0.25f * __sinf(1.7f * tid));
+        }
+        gsum = warp_max(gsum);
+        __syncthreads();
+        if (lane == 0) red[wid] = gsum;
+        __syncthreads();
+        const float gmax = fmaxf(fmaxf(red[0], red[1]), fmaxf(red[2], red[3]));
+        __syncthreads();
+        float lam = 0.f;
+        for (int it = 0; it < 8; it++) {
+          float part = 0.f, xx = 0.f;
+          if (tid < 64) {
+            float acc = 0.f;
+            for (int j = 0; j < 64; j++) acc = fmaf(Gt[j * 64 + tid], vx[j], acc);
+            vy[tid] = acc;
+            part = acc * acc;
+            xx = vx[tid] * vx[tid];
+          }
+          const float nrm2 = block_sum<float, TC_NT>(part, red);
+          const float x2 = block_sum<float, TC_NT>(xx, red);
+          lam = sqrtf(nrm2 / fmaxf(x2, 1e-30f));
+          const float inv = rsqrtf(fmaxf(nrm2, 1e-30f));
+          if (tid < 64) vx[tid] = vy[tid] * inv;
+          __syncthreads();
+        }
+        const float s = fmaxf(1.05f * lam, 0.5f * gmax);
+        const float inv_s = 1.f / s;
+        // S = [A/s ; I] split into bf16 hi / lo (row r per thread)
+#pragma unroll
+        for (int c0 = 0; c0 < 64; c0 += 8) {
+          float v[8];
+          if (r < 64) {
+            const float4 x0 = *reinterpret_cast<const float4*>(Gt + r * 64 + c0);
+            const float4 x1 = *reinterpret_cast<const float4*>(Gt + r * 64 + c0 + 4);
+            v[0] = x0.x * inv_s; v[1] = x0.y * inv_s; v[2] = x0.z * inv_s; v[3] = x0.w * inv_s;
+            v[4] = x1.x * inv_s; v[5] = x1.y * inv_s; v[6] = x1.z * inv_s; v[7] = x1.w * inv_s;
+          } else {
+#pragma unroll
+            for (int j = 0; j < 8; j++) v[j] = (r - 64 == c0 + j) ? 1.f : 0.f;
+          }
+          uint4 h, l;
+          split8(v, h, l);
+          const uint32_t off = tc::kmajor_off_bf16(r, c0, 64);
+          *reinterpret_cast<uint4*>(sm + L::S_HI + off) = h;
+          *reinterpret_cast<uint4*>(sm + L::S_LO + off) = l;
+        }
+        __syncthreads();
+        // B = Y: rows 0..63 of S have the same K-major offsets in an 8 KB operand
+        for (int i = tid; i < 8192 / 16; i += TC_NT) {
+          reinterpret_cast<uint4*>(sm + L::B_HI)[i] = reinterpret_cast<const uint4*>(sm + L::S_HI)[i];
+          reinterpret_cast<uint4*>(sm + L::B_LO)[i] = reinterpret_cast<const uint4*>(sm + L::S_LO)[i];
+        }
+        tc::fence_smem_async();
+        tc::fence_before_sync();
+        __syncthreads();
+        const float coef = sqrtf((float)(n - 1) / s);
+        int it = 0;
+        for (bool last = false; !last; it++) {
+          if (it == a.max_ns_iter - 1) last = true;
+          // T = Z Y  (rows 64..127 of S Y)
+          if (tid == 0) {
+            tc::fence_after_sync();
+            ns_mma(D0, sbase + L::S_HI, sbase + L::S_LO, sbase + L::B_HI, sbase + L::B_LO, idesc);
+            tc::mma_commit(&mbar[2]);
+          }
+          wait_bar(2);
+          tc::fence_after_sync();
+          float e2 = 0.f;
+          if (wid >= 2) {
+#pragma unroll
+            for (int c0 = 0; c0 < 64; c0 += 16) {
+              float v[16];
+              tc::tmem_ld16(D0 + lane_off + c0, v);
+#pragma unroll
+              for (int j = 0; j < 16; j++) {
+                const float dlt = v[j] - ((r - 64 == c0 + j) ? 1.f : 0.f);
+                e2 = fmaf(dlt, dlt, e2);
+              }
+#pragma unroll
+              for (int g = 0; g < 2; g++) {
+                uint4 h, l;
+                split8(v + 8 * g, h, l);
+                const uint32_t off = tc::kmajor_off_bf16(r - 64, c0 + 8 * g, 64);
+                *reinterpret_cast<uint4*>(sm + L::B_HI + off) = h;
+                *reinterpret_cast<uint4*>(sm + L::B_LO + off) = l;
+              }
+            }
+          }
+          tc::fence_before_sync();
+          e2 = block_sum<float, TC_NT>(e2, red);
+          if (e2 < 1.0e-8f) last = true;
+          tc::fence_smem_async();
+          tc::fence_before_sync();
+          __syncthreads();
+          // [Y;Z] T
+          if (tid == 0) {
+            tc::fence_after_sync();
+            ns_mma(D0, sbase + L::S_HI, sbase + L::S_LO, sbase + L::B_HI, sbase + L::B_LO, idesc);
+            tc::mma_commit(&mbar[2]);
+          }
+          wait_bar(2);
+          tc::fence_after_sync();
+          if (__syncthreads_or(tmo)) {
+            tmo = 1;
+            break;
+          }
+          // S <- 1.5 S - 0.5 S T  (final step: W = coef * Z into WMAT)
+#pragma unroll
+          for (int c0 = 0; c0 < 64; c0 += 16) {
+            float v[16];
+            tc::tmem_ld16(D0 + lane_off + c0, v);
+#pragma unroll
+            for (int g = 0; g < 2; g++) {
+              const uint32_t off = tc::kmajor_off_bf16(r, c0 + 8 * g, 64);
+              float sh[8], sl[8], sn[8];
+              unpack8(*reinterpret_cast<const uint4*>(sm + L::S_HI + off), sh);
+              unpack8(*reinterpret_cast<const uint4*>(sm + L::S_LO + off), sl);
+#pragma unroll
+              for (int j = 0; j < 8; j++) sn[j] = 1.5f * (sh[j] + sl[j]) - 0.5f * v[8 * g + j];
+              if (!last) {
+                uint4 h, l;
+                split8(sn, h, l);
+                // S rows are rewritten only after every thread has read its own row
+                // (each thread touches only row r), so no barrier is needed here
+                *reinterpret_cast<uint4*>(sm + L::S_HI + off) = h;
+                *reinterpret_cast<uint4*>(sm + L::S_LO + off) = l;
+              } else if (r >= 64) {
+                float* dst = Wm + (r - 64) * 64 + c0 + 8 * g;
+#pragma unroll
+                for (int j = 0; j < 8; j++) dst[j] = coef * sn[j];
+              }
+            }
+          }
+          tc::fence_before_sync();
+          __syncthreads();
+          if (!last) {
+            for (int i = tid; i < 8192 / 16; i += TC_NT) {
+              reinterpret_cast<uint4*>(sm + L::B_HI)[i] = reinterpret_cast<const uint4*>(sm + L::S_HI)[i];
+              reinterpret_cast<uint4*>(sm + L::B_LO)[i] = reinterpret_cast<const uint4*>(sm + L::S_LO)[i];
+            }
+            tc::fence_smem_async();
+            tc::fence_before_sync();
+            __syncthreads();
+          }
+        }
+        if (tmo) break;
+        // wbar = Z (Z b) / s with Z = W / coef (W symmetric: column reads)
+        if (tid < 64) {
+          float acc = 0.f;
+          for (int j = 0; j < 64; j++) acc = fmaf(Wm[j * 64 + tid], vb[j], acc);
+          vg[tid] = acc / coef;
+        }
+        __syncthreads();
+        if (tid < 64) {
+          float acc = 0.f;
+          for (int j = 0; j < 64; j++) acc = fmaf(Wm[j * 64 + tid], vg[j], acc);
+          vwb[tid] = acc / (coef * s);
+        }
+        if (tid == 0) {
+          a.infl[pt] = infl_update(n, infl, (double)p1, (double)trace, (double)p3);
+          a.status[pt] = LETKF_OK;
+          if (a.sweeps_out) a.sweeps_out[pt] = it;
+        }
+      }
+    } else {
+      const float sq = (float)sqrt(infl);
+      for (int idx = tid; idx < 64 * 64; idx += TC_NT) Wm[idx] = ((idx >> 6) == (idx & 63)) ? sq : 0.f;
+      if (tid < 64) vwb[tid] = 0.f;
+      if (tid == 0) {
+        a.status[pt] = LETKF_OK;
+        if (a.sweeps_out) a.sweeps_out[pt] = 0;
+      }
+    }
+    if (tid == 0 && a.nobsl_out) a.nobsl_out[pt] = Lp;
+    if (deferred) {
+      if (tid == 0) a.defer_list[atomicAdd(a.defer_count, 1)] = pt;
+      continue;
+    }
+    __syncthreads();
+    // ---- update: xa = mean + xp (W + wbar 1^T); FP64 mean and mean increment ----
+    for (int t = tid; t < nv * n; t += TC_NT) {
+      const int v = t / n, mm = t - v * n;
+      xs[v * 64 + mm] = a.xb[((size_t)v * a.npts + pt) * n + mm];
+    }
+    __syncthreads();
+    for (int v = wid; v < nv; v += TC_NT / 32) {
+      double sx = 0.0;
+      for (int mm = lane; mm < n; mm += 32) sx += (double)xs[v * 64 + mm];
+      const double mean = warp_sum(sx) / (double)n;
+      double dlt = 0.0;
+      for (int mm = lane; mm < n; mm += 32) {
+        const float xp = (float)((double)xs[v * 64 + mm] - mean);
+        xs[v * 64 + mm] = xp;
+        dlt += (double)xp * (double)vwb[mm];
+      }
+      dlt = warp_sum(dlt);
+      if (lane == 0) meanv[8 + v] = mean + dlt;
+    }
+    __syncthreads();
+    for (int t = tid; t < nv * n; t += TC_NT) {
+      const int v = t / n, mm = t - v * n;
+      float acc = 0.f;
+      const float* xp = xs + v * 64;
+      for (int k = 0; k < n; k++) acc = fmaf(xp[k], Wm[k * 64 + mm], acc);
+      a.xa[((size_t)v * a.npts + pt) * n + mm] = (float)(meanv[8 + v] + (double)acc);
+    }
+  }
+  // drain (bounded), report, release tensor memory
+  for (int b = 0; b < 2; b++)
+    if (outst[b]) wait_bar(b);
+  if (__syncthreads_or(tmo) && tid == 0 && a.err_flag) atomicExch(a.err_flag, 1);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (wid == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tbase, TC_TMEM_COLS);
+  }
+}
+
+int launch_sweep_tc(const SweepArgs& a, cudaStream_t stream, int grid_cap) {
+  if (a.n < 2 || a.n > TC_NP || a.nv < 1 || a.nv > 8) return LETKF_ERR_ARG;
+  if (a.npts == 0) return LETKF_OK;
+  constexpr size_t bytes = TcLayout::TOTAL;
+  cudaError_t err = cudaFuncSetAttribute(sweep_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (err != cudaSuccess) return cuda_status(err);
+  int dev = 0, nsm = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_tc_kernel, TC_NT, bytes);
+  if (per_sm < 1) per_sm = 1;
+  // tensor memory: 512 columns per SM
+  if (per_sm > (int)(512 / TC_TMEM_COLS)) per_sm = 512 / TC_TMEM_COLS;
+  int grid = nsm * per_sm;
+  if (grid_cap > 0 && grid > grid_cap) grid = grid_cap;
+  if (grid > a.npts) grid = a.npts;
+  sweep_tc_kernel<<<grid, TC_NT, bytes, stream>>>(a);
+  note_launch();
+  return cuda_status(cudaGetLastError());
+}
+
+}  // namespace letkf

@@ -22,6 +22,7 @@ OPT_MAX_SWEEPS = 2
 OPT_EIGENSOLVER = 3
 EIG_NEWTON_SCHULZ = 0
 EIG_JACOBI = 1
+OPT_TENSOR_CORES = 4
 
 
 class SweepDesc(C.Structure):

@@ -33,10 +33,11 @@ def _spread(xb):
     return np.sqrt(((xb - xb.mean(-1, keepdims=True)) ** 2).sum(-1) / (xb.shape[-1] - 1)).mean()
 
 
-@pytest.mark.parametrize("ne,var_local,eig", [(40, None, 0), (64, [1.0, 0.5, 0.0], 0), (20, None, 0),
-                                            (100, None, 0), (64, None, 1)])
-def test_mixed_sweep_against_oracle(cuda, ne, var_local, eig):
-    from letkf_gb300.sweep import OPT_EIGENSOLVER, PREC_MIXED, Sweep
+@pytest.mark.parametrize("ne,var_local,eig,tc", [(40, None, 0, 1), (64, [1.0, 0.5, 0.0], 0, 1), (20, None, 0, 1),
+                                               (64, None, 0, 0), (100, None, 0, 1), (64, None, 1, 1)])
+def test_mixed_sweep_against_oracle(cuda, ne, var_local, eig, tc):
+    """tc=1, eig=0 and ne <= 64 runs the tcgen05 sweep; otherwise the SIMT sweep."""
+    from letkf_gb300.sweep import OPT_EIGENSOLVER, OPT_TENSOR_CORES, PREC_MIXED, Sweep
 
     case, prm, perm, grd, so, varloc, hdxf, dep = _setup(ne=ne, f32=True, var_local=var_local)
     xb = case["xb"].astype(np.float64)
@@ -50,6 +51,7 @@ def test_mixed_sweep_against_oracle(cuda, ne, var_local, eig):
                hdxf.astype(np.float32), varloc=varloc if var_local is not None else None, var_local_row=var_local)
     np.testing.assert_array_equal(sw.nobsgrd(), grd)
     sw.set_option(OPT_EIGENSOLVER, eig)
+    sw.set_option(OPT_TENSOR_CORES, tc)
     sw.set_background(case["xb"])
     sw.set_inflation(infl0)
     sw.run()
@@ -114,3 +116,37 @@ def test_mixed_sweep_no_obs(cuda):
     np.testing.assert_allclose(xa, m + 1.1 * (xb - m), rtol=0, atol=2e-6 * np.abs(xb).max())
     assert (dg["nobsl"] == 0).all()
     np.testing.assert_array_equal(dg["infl"], 1.21)
+
+
+def test_tc_sweep_defers_points_to_the_jacobi_pass(cuda):
+    """Points with a non-positive inflation term c = (k-1)/rho cannot use
+    Newton-Schulz; the tensor-core sweep hands them to the Jacobi pass, whose
+    results must equal those of the all-Jacobi sweep exactly."""
+    from letkf_gb300.sweep import EIG_JACOBI, OPT_EIGENSOLVER, OPT_TENSOR_CORES, PREC_MIXED, Sweep
+
+    case, prm, perm, grd, so, varloc, hdxf, dep = _setup(ne=64, f32=True)
+    npts = case["pri"].size
+    infl0 = np.full(npts, 1.05)
+    infl0[::7] = -0.5
+    out = []
+    for tc, eig in ((1, 0), (0, EIG_JACOBI)):
+        sw = Sweep(64, case["nvar"], case["nlon"], case["nlat"], npts, prm, precision=PREC_MIXED)
+        sw.set_points(case["pri"], case["prj"], case["prlev"])
+        sw.set_obs(case["ri"], case["rj"], case["lev"], case["dat"], case["err"], dep, case["cls"],
+                   hdxf.astype(np.float32))
+        sw.set_option(OPT_TENSOR_CORES, tc)
+        sw.set_option(OPT_EIGENSOLVER, eig)
+        sw.set_background(case["xb"])
+        sw.set_inflation(infl0)
+        sw.run()
+        out.append((sw.analysis(), sw.diagnostics()))
+        sw.close()
+    (xa_tc, dg_tc), (xa_j, dg_j) = out
+    neg = np.zeros(npts, bool)
+    neg[::7] = True
+    np.testing.assert_array_equal(dg_tc["status"][neg], dg_j["status"][neg])
+    np.testing.assert_array_equal(xa_tc[:, neg], xa_j[:, neg])
+    np.testing.assert_array_equal(dg_tc["infl"][neg], dg_j["infl"][neg])
+    spread = _spread(case["xb"].astype(np.float64))
+    ok = ~neg
+    assert np.abs(xa_tc[:, ok].astype(np.float64) - xa_j[:, ok]).max() < 1e-3 * spread
