@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip e2e, fp64, cpu baseline (profiling runs)")
     ap.add_argument("--eig", default="newton-schulz", choices=["newton-schulz", "jacobi"],
                     help="transform of the mixed form")
+    ap.add_argument("--tc", type=int, default=1, choices=[0, 1],
+                    help="1: Gram and Newton-Schulz on the tcgen05 tensor cores (ne <= 64)")
     return ap.parse_args()
 
 
@@ -220,7 +222,7 @@ def run_gpu(args, rank, world, dist):
     import torch
 
     from letkf_gb300 import lib as L
-    from letkf_gb300.sweep import OPT_EIGENSOLVER, PREC_F64, PREC_MIXED, Sweep
+    from letkf_gb300.sweep import OPT_EIGENSOLVER, OPT_TENSOR_CORES, PREC_F64, PREC_MIXED, Sweep
     from letkf_gb300.workload import RegionalWorkload
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
@@ -233,6 +235,7 @@ def run_gpu(args, rank, world, dist):
     sw.set_points(ri, rj, plev, tile=4)
     sw.set_obs(wl.ri, wl.rj, wl.lev, dat, wl.err, dep, wl.cls, hdxf)
     sw.set_option(OPT_EIGENSOLVER, 0 if args.eig == "newton-schulz" else 1)
+    sw.set_option(OPT_TENSOR_CORES, args.tc)
     sw.set_background_device(xb.data_ptr())
     infl0 = np.ones(wl.npts)
     sw.set_inflation(infl0)
@@ -288,7 +291,7 @@ def run_gpu(args, rank, world, dist):
     nl = nobsl.astype(np.float64)
     out["local_obs"] = {"min": int(nl.min()), "mean": float(nl.mean()), "p50": float(np.median(nl)),
                         "p99": float(np.percentile(nl, 99)), "max": int(nl.max()), "zero_frac": float((nl == 0).mean())}
-    out["transform"] = {"method": args.eig,
+    out["transform"] = {"method": args.eig, "tensor_cores": bool(args.tc and args.ne <= 64 and args.eig == "newton-schulz"),
                         "iterations_mean": float(dg["sweeps"][nobsl > 0].mean()) if (nobsl > 0).any() else 0.0,
                         "iterations_max": int(dg["sweeps"].max())}
     if args.no_extras:
