@@ -62,6 +62,7 @@ def parse():
                     help="transform of the mixed form")
     ap.add_argument("--tc", type=int, default=1, choices=[0, 1],
                     help="1: Gram and Newton-Schulz on the tcgen05 tensor cores (ne <= 64)")
+    ap.add_argument("--tc-ns", type=int, default=None, help="tensor-core Newton-Schulz iterations before the FP32 ones")
     return ap.parse_args()
 
 
@@ -222,7 +223,7 @@ def run_gpu(args, rank, world, dist):
     import torch
 
     from letkf_gb300 import lib as L
-    from letkf_gb300.sweep import OPT_EIGENSOLVER, OPT_TENSOR_CORES, PREC_F64, PREC_MIXED, Sweep
+    from letkf_gb300.sweep import OPT_EIGENSOLVER, OPT_TC_NS_ITERS, OPT_TENSOR_CORES, PREC_F64, PREC_MIXED, Sweep
     from letkf_gb300.workload import RegionalWorkload
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
@@ -236,6 +237,8 @@ def run_gpu(args, rank, world, dist):
     sw.set_obs(wl.ri, wl.rj, wl.lev, dat, wl.err, dep, wl.cls, hdxf)
     sw.set_option(OPT_EIGENSOLVER, 0 if args.eig == "newton-schulz" else 1)
     sw.set_option(OPT_TENSOR_CORES, args.tc)
+    if args.tc_ns is not None:
+        sw.set_option(OPT_TC_NS_ITERS, args.tc_ns)
     sw.set_background_device(xb.data_ptr())
     infl0 = np.ones(wl.npts)
     sw.set_inflation(infl0)

@@ -142,6 +142,7 @@ int letkf_search_speedy(int nlon, int nlat, const double* lon, const double* lat
 #define LETKF_EIG_NEWTON_SCHULZ 0 /*   W = sqrt((k-1)) A^(-1/2) by Newton-Schulz (default) */
 #define LETKF_EIG_JACOBI 1        /*   eigen-decomposition by parallel Jacobi */
 #define LETKF_OPT_TENSOR_CORES 4  /* 1 (default): Gram and Newton-Schulz on tcgen05 for ne <= 64 */
+#define LETKF_OPT_TC_NS_ITERS 5   /* tensor-core Newton-Schulz iterations before the FP32 ones (default 14) */
 
 typedef struct letkf_sweep_desc {
   int ne;           /* ensemble size (MEMBER) */

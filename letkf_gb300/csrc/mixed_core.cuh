@@ -320,6 +320,126 @@ __device__ __forceinline__ void sym_gemm_tile(const float* X, const float* Yb, i
   }
 }
 
+// Coupled Newton-Schulz iterations in FP32 on row-major symmetric Y, Z with
+// scratch T (NP x NP each), until ||ZY - I||_F < 1e-4 plus one more step (the
+// quadratic convergence then reaches the FP32 floor) or max_iter.  Returns the
+// iterations done; Y, Z hold the last iterate.
+template <int NP>
+__device__ int ns_iterate(float* Y, float* Z, float* T, float* redf, int max_iter) {
+  using C = MixedCfg<NP>;
+  constexpr int NTI = NP / C::TR;
+  const int tid = threadIdx.x;
+  const int i0 = (tid % NTI) * C::TR, j0 = (tid / NTI) * C::TC;
+  float acc[C::TR][C::TC];
+  int it = 0;
+  bool last = false;
+  for (; it < max_iter; it++) {
+    // T = Z Y and ||T - I||_F^2
+    sym_gemm_tile<NP>(Z, Y, i0, j0, acc);
+    float e2 = 0.f;
+#pragma unroll
+    for (int a = 0; a < C::TR; a++)
+#pragma unroll
+      for (int b = 0; b < C::TC; b++) {
+        T[(i0 + a) * NP + j0 + b] = acc[a][b];
+        const float d = acc[a][b] - ((i0 + a) == (j0 + b) ? 1.f : 0.f);
+        e2 = fmaf(d, d, e2);
+      }
+    e2 = block_sum<float, C::NT>(e2, redf);  // also publishes T
+    if (e2 < 1.0e-8f) last = true;
+    // Y' = 1.5 Y - 0.5 Y T ; Z' = 1.5 Z - 0.5 T Z
+    float ynew[C::TR][C::TC];
+    sym_gemm_tile<NP>(Y, T, i0, j0, acc);
+#pragma unroll
+    for (int a = 0; a < C::TR; a++)
+#pragma unroll
+      for (int b = 0; b < C::TC; b++) ynew[a][b] = 1.5f * Y[(i0 + a) * NP + j0 + b] - 0.5f * acc[a][b];
+    sym_gemm_tile<NP>(T, Z, i0, j0, acc);
+#pragma unroll
+    for (int a = 0; a < C::TR; a++)
+#pragma unroll
+      for (int b = 0; b < C::TC; b++) acc[a][b] = 1.5f * Z[(i0 + a) * NP + j0 + b] - 0.5f * acc[a][b];
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < C::TR; a++)
+#pragma unroll
+      for (int b = 0; b < C::TC; b++) {
+        Y[(i0 + a) * NP + j0 + b] = ynew[a][b];
+        Z[(i0 + a) * NP + j0 + b] = acc[a][b];
+      }
+    __syncthreads();
+    if (last) {
+      it++;
+      break;
+    }
+  }
+  return it;
+}
+
+// Uncoupled Newton-Schulz refinement of Z ~ As^(-1/2) for symmetric As:
+//   P = As Z, Q = Z P (= Z As Z, symmetric), Z <- 1.5 Z - 0.5 Q Z, then Z is
+// symmetrised.  Stops after the step following ||Q - I||_F < 1e-4 or after
+// max_iter; returns the iterations done.  P is scratch (NP x NP).
+template <int NP>
+__device__ int ns_polish(const float* As, float* Z, float* P, float* redf, int max_iter) {
+  using C = MixedCfg<NP>;
+  constexpr int NTI = NP / C::TR;
+  const int tid = threadIdx.x;
+  const int i0 = (tid % NTI) * C::TR, j0 = (tid / NTI) * C::TC;
+  float acc[C::TR][C::TC];
+  int it = 0;
+  bool last = false;
+  for (; it < max_iter; it++) {
+    sym_gemm_tile<NP>(As, Z, i0, j0, acc);  // As Z
+#pragma unroll
+    for (int a = 0; a < C::TR; a++)
+#pragma unroll
+      for (int b = 0; b < C::TC; b++) P[(i0 + a) * NP + j0 + b] = acc[a][b];
+    __syncthreads();
+    sym_gemm_tile<NP>(Z, P, i0, j0, acc);   // Z^T (As Z)
+    float e2 = 0.f;
+#pragma unroll
+    for (int a = 0; a < C::TR; a++)
+#pragma unroll
+      for (int b = 0; b < C::TC; b++) {
+        const float d = acc[a][b] - ((i0 + a) == (j0 + b) ? 1.f : 0.f);
+        e2 = fmaf(d, d, e2);
+      }
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < C::TR; a++)
+#pragma unroll
+      for (int b = 0; b < C::TC; b++) P[(i0 + a) * NP + j0 + b] = acc[a][b];
+    e2 = block_sum<float, C::NT>(e2, redf);  // also publishes Q
+    if (e2 < 1.0e-8f) last = true;
+    sym_gemm_tile<NP>(P, Z, i0, j0, acc);   // Q Z
+#pragma unroll
+    for (int a = 0; a < C::TR; a++)
+#pragma unroll
+      for (int b = 0; b < C::TC; b++) acc[a][b] = 1.5f * Z[(i0 + a) * NP + j0 + b] - 0.5f * acc[a][b];
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < C::TR; a++)
+#pragma unroll
+      for (int b = 0; b < C::TC; b++) Z[(i0 + a) * NP + j0 + b] = acc[a][b];
+    __syncthreads();
+    for (int idx = tid; idx < NP * NP; idx += C::NT) {
+      const int i = idx / NP, j = idx - i * NP;
+      if (i < j) {
+        const float v = 0.5f * (Z[i * NP + j] + Z[j * NP + i]);
+        Z[i * NP + j] = v;
+        Z[j * NP + i] = v;
+      }
+    }
+    __syncthreads();
+    if (last) {
+      it++;
+      break;
+    }
+  }
+  return it;
+}
+
 // Newton-Schulz on sm[A] (SPD, all eigenvalues >= cdiag > 0).  Leaves
 // Z = (A/s)^(-1/2) in sm[V] (row-major, symmetric), scratch in sm[NS::T], and
 // returns s (> 0); *iters gets the iterations used.
@@ -377,51 +497,7 @@ __device__ float ns_invsqrt(float* sm, float cdiag, int max_iter, int* iters) {
     Z[idx] = (idx / NP == idx % NP) ? 1.f : 0.f;
   }
   __syncthreads();
-  const int i0 = (tid % NTI) * C::TR, j0 = (tid / NTI) * C::TC;
-  float acc[C::TR][C::TC];
-  int it = 0;
-  bool last = false;
-  for (; it < max_iter; it++) {
-    // T = Z Y and ||T - I||_F^2
-    sym_gemm_tile<NP>(Z, A, i0, j0, acc);
-    float e2 = 0.f;
-#pragma unroll
-    for (int a = 0; a < C::TR; a++)
-#pragma unroll
-      for (int b = 0; b < C::TC; b++) {
-        T[(i0 + a) * NP + j0 + b] = acc[a][b];
-        const float d = acc[a][b] - ((i0 + a) == (j0 + b) ? 1.f : 0.f);
-        e2 = fmaf(d, d, e2);
-      }
-    e2 = block_sum<float, C::NT>(e2, redf);  // also publishes T
-    // ||T - I||_F < 1e-4: one more (quadratically convergent) step reaches the FP32 floor
-    if (e2 < 1.0e-8f) last = true;
-    // Y' = 1.5 Y - 0.5 Y T ; Z' = 1.5 Z - 0.5 T Z
-    float ynew[C::TR][C::TC];
-    sym_gemm_tile<NP>(A, T, i0, j0, acc);
-#pragma unroll
-    for (int a = 0; a < C::TR; a++)
-#pragma unroll
-      for (int b = 0; b < C::TC; b++) ynew[a][b] = 1.5f * A[(i0 + a) * NP + j0 + b] - 0.5f * acc[a][b];
-    sym_gemm_tile<NP>(T, Z, i0, j0, acc);
-#pragma unroll
-    for (int a = 0; a < C::TR; a++)
-#pragma unroll
-      for (int b = 0; b < C::TC; b++) acc[a][b] = 1.5f * Z[(i0 + a) * NP + j0 + b] - 0.5f * acc[a][b];
-    __syncthreads();
-#pragma unroll
-    for (int a = 0; a < C::TR; a++)
-#pragma unroll
-      for (int b = 0; b < C::TC; b++) {
-        A[(i0 + a) * NP + j0 + b] = ynew[a][b];
-        Z[(i0 + a) * NP + j0 + b] = acc[a][b];
-      }
-    __syncthreads();
-    if (last) {
-      it++;
-      break;
-    }
-  }
+  const int it = ns_iterate<NP>(A, Z, T, redf, max_iter);
   if (iters) *iters = it;
   return s;
 }

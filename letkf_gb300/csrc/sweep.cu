@@ -140,6 +140,7 @@ struct letkf_sweep_s {
   int max_sweeps = 12;
   int use_ns = 1;
   int use_tc = 1;
+  int tc_ns_max = 14;
 };
 
 static void dfree(void* p) {
@@ -406,6 +407,10 @@ int letkf_sweep_set_option(letkf_sweep_t h, int option, int value) {
       if (value != 0 && value != 1) return LETKF_ERR_ARG;
       h->use_tc = value;
       return LETKF_OK;
+    case LETKF_OPT_TC_NS_ITERS:
+      if (value < 0 || value > 64) return LETKF_ERR_ARG;
+      h->tc_ns_max = value;
+      return LETKF_OK;
     case LETKF_OPT_EIGENSOLVER:
       if (value != LETKF_EIG_NEWTON_SCHULZ && value != LETKF_EIG_JACOBI) return LETKF_ERR_ARG;
       h->use_ns = value == LETKF_EIG_NEWTON_SCHULZ;
@@ -517,6 +522,7 @@ int letkf_sweep_run(letkf_sweep_t h, void* stream) {
   a.max_ns_iter = 24;
   a.use_ns = h->use_ns;
   a.err_flag = h->err_flag;
+  a.tc_ns_max = h->tc_ns_max;
   cudaMemsetAsync(h->counter, 0, sizeof(int), s);
   if (h->use_tc && h->use_ns && h->d.ne <= 64) {
     // tensor-core sweep, then the Jacobi pass over the points it deferred

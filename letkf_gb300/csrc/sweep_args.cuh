@@ -37,6 +37,7 @@ struct SweepArgs {
   int* defer_list;      // tensor-core sweep: points handed to the Jacobi pass
   int* defer_count;
   int* err_flag;        // set when a bounded wait gave up
+  int tc_ns_max;        // tensor-core Newton-Schulz iterations before the FP32 polish
 };
 
 }  // namespace letkf

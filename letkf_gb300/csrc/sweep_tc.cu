@@ -29,17 +29,18 @@
 namespace letkf {
 
 constexpr int TC_NT = 128;
-constexpr int TC_CH = 32;
+constexpr int TC_CH = 16;  // observations per Gram stage
 constexpr int TC_NP = 64;
 constexpr uint32_t TC_TMEM_COLS = 128;
 constexpr uint32_t TC_WAIT = 1u << 22;
+constexpr int TC_POLISH_MAX = 8;  // FP32 iterations at most
 
 // byte offsets in dynamic shared memory
 struct TcLayout {
   // operand region, 48 KB, reused by phase
   static constexpr int STG = 0;           // two Gram stages of 16 KB
-  static constexpr int STG_A = 0;         //   A = [Yw_hi^T; Yw_lo^T]: 128 x 32 bf16 (8 KB)
-  static constexpr int STG_BH = 8192;     //   Y_hi^T: 64 x 32 bf16 (4 KB)
+  static constexpr int STG_A = 0;         //   A = [Yw_hi^T; Yw_lo^T]: 128 x 16 tf32 (8 KB)
+  static constexpr int STG_BH = 8192;     //   Y_hi^T: 64 x 16 tf32 (4 KB)
   static constexpr int STG_BL = 12288;    //   Y_lo^T
   static constexpr int STG_SIZE = 16384;
   static constexpr int S_HI = 0;          // Newton-Schulz S = [Y; Z]: 128 x 64 bf16 (16 KB)
@@ -49,6 +50,9 @@ struct TcLayout {
   static constexpr int GTMP = 32768;      // Gram in FP32, 64 x 64 row-major (over B)
   static constexpr int WMAT = 32768;      // transform W in FP32, 64 x 64 row-major (over B)
   static constexpr int XS = 0;            // update staging, nv x 64 FP32 (over S)
+  static constexpr int YF = 0;            // FP32 polish: Y (64 x 64), Z, T row-major
+  static constexpr int ZF = 16384;
+  static constexpr int TF = 32768;
   static constexpr int OPER_END = 49152;
   // small data
   static constexpr int VB = OPER_END;            // float[64] departure product
@@ -87,6 +91,15 @@ __device__ __forceinline__ void split8(const float* v, uint4& hi, uint4& lo) {
   }
   hi = make_uint4(pack_bf16x2(h[0], h[1]), pack_bf16x2(h[2], h[3]), pack_bf16x2(h[4], h[5]), pack_bf16x2(h[6], h[7]));
   lo = make_uint4(pack_bf16x2(l[0], l[1]), pack_bf16x2(l[2], l[3]), pack_bf16x2(l[4], l[5]), pack_bf16x2(l[6], l[7]));
+}
+
+// 4 values -> tf32 hi (low 13 mantissa bits cleared) and the FP32 remainder
+__device__ __forceinline__ void split4_tf32(const float* v, float4& hi, float4& lo) {
+  float h[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) h[j] = __uint_as_float(__float_as_uint(v[j]) & 0xFFFFE000u);
+  hi = make_float4(h[0], h[1], h[2], h[3]);
+  lo = make_float4(v[0] - h[0], v[1] - h[1], v[2] - h[2], v[3] - h[3]);
 }
 
 __device__ __forceinline__ void unpack8(uint4 p, float* v) {
@@ -142,7 +155,8 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int n = a.n, nv = a.nv;
   const uint32_t sbase = tc::smem_u32(sm);
-  const uint32_t idesc = tc::idesc_bf16(128, 64);
+  const uint32_t idesc = tc::idesc_bf16(128, 64);    // Newton-Schulz products
+  const uint32_t idesc_g = tc::idesc_tf32(128, 64);  // Gram
 
   if (tid == 0) {
     tc::mbar_init(&mbar[0], 1);
@@ -191,10 +205,10 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
       }
       tc::fence_after_sync();
       unsigned char* stg = sm + L::STG + buf * L::STG_SIZE;
-      float yv[16], wv[16];
+      float yv[8], wv[8];
 #pragma unroll
-      for (int kk = 0; kk < 16; kk++) {
-        const int k = hh * 16 + kk;
+      for (int kk = 0; kk < 8; kk++) {
+        const int k = hh * 8 + kk;
         float y = 0.f, w = 0.f, dd = 0.f;
         if (k < nr) {
           w = ss.pw[k];
@@ -207,14 +221,14 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
       }
 #pragma unroll
       for (int g = 0; g < 2; g++) {
-        uint4 h, l;
-        const uint32_t off = tc::kmajor_off_bf16(m, hh * 16 + g * 8, TC_CH);
-        split8(wv + 8 * g, h, l);
-        *reinterpret_cast<uint4*>(stg + L::STG_A + off) = h;
-        *reinterpret_cast<uint4*>(stg + L::STG_A + tc::kmajor_off_bf16(64 + m, hh * 16 + g * 8, TC_CH)) = l;
-        split8(yv + 8 * g, h, l);
-        *reinterpret_cast<uint4*>(stg + L::STG_BH + off) = h;
-        *reinterpret_cast<uint4*>(stg + L::STG_BL + off) = l;
+        float4 h, l;
+        const uint32_t off = tc::kmajor_off(m, hh * 8 + g * 4, TC_CH);
+        split4_tf32(wv + 4 * g, h, l);
+        *reinterpret_cast<float4*>(stg + L::STG_A + off) = h;
+        *reinterpret_cast<float4*>(stg + L::STG_A + tc::kmajor_off(64 + m, hh * 8 + g * 4, TC_CH)) = l;
+        split4_tf32(yv + 4 * g, h, l);
+        *reinterpret_cast<float4*>(stg + L::STG_BH + off) = h;
+        *reinterpret_cast<float4*>(stg + L::STG_BL + off) = l;
       }
       if (tid < nr) {
         const float dd = ss.pd[tid];
@@ -229,12 +243,12 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
         const uint32_t sa = sbase + L::STG + buf * L::STG_SIZE;
 #pragma unroll
         for (int s = 0; s < 2; s++)
-          tc::mma_bf16(D0, tc::smem_desc(sa + L::STG_A + s * 256, 128, 512),
-                       tc::smem_desc(sa + L::STG_BH + s * 256, 128, 512), idesc, (first && s == 0) ? 0u : 1u);
+          tc::mma_tf32(D0, tc::smem_desc(sa + L::STG_A + s * 256, 128, 512),
+                       tc::smem_desc(sa + L::STG_BH + s * 256, 128, 512), idesc_g, (first && s == 0) ? 0u : 1u);
 #pragma unroll
         for (int s = 0; s < 2; s++)
-          tc::mma_bf16(D1, tc::smem_desc(sa + L::STG_A + s * 256, 128, 512),
-                       tc::smem_desc(sa + L::STG_BL + s * 256, 128, 512), idesc, (first && s == 0) ? 0u : 1u);
+          tc::mma_tf32(D1, tc::smem_desc(sa + L::STG_A + s * 256, 128, 512),
+                       tc::smem_desc(sa + L::STG_BL + s * 256, 128, 512), idesc_g, (first && s == 0) ? 0u : 1u);
         tc::mma_commit(&mbar[buf]);
       }
       outst[buf] = true;
@@ -306,6 +320,18 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
       } else {
         if (tid < 64) Gt[tid * 64 + tid] += cdiag;
         __syncthreads();
+        // keep the exact FP32 A in the Gram's second accumulator (lanes 0..63 of
+        // columns 64..127); the Newton-Schulz products only use columns 0..63
+        if (wid < 2) {
+#pragma unroll
+          for (int c0 = 0; c0 < 64; c0 += 16) {
+            float v[16];
+#pragma unroll
+            for (int j = 0; j < 16; j++) v[j] = Gt[r * 64 + c0 + j];
+            tc::tmem_st16(D1 + lane_off + c0, v);
+          }
+        }
+        tc::fence_before_sync();
         // scaling s: power iteration guarded by the Gershgorin bound (s >= lambda_max / 2)
         float gsum = 0.f;
         if (tid < 64) {
@@ -366,9 +392,12 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
         tc::fence_before_sync();
         __syncthreads();
         const float coef = sqrtf((float)(n - 1) / s);
+        // tensor-core phase: the iterations that move the small eigenvalues of
+        // ZY towards 1; stop once ||ZY - I||_F^2 < 1e-3 (or after TC_NS_MAX)
         int it = 0;
-        for (bool last = false; !last; it++) {
-          if (it == a.max_ns_iter - 1) last = true;
+        const int tc_max = a.tc_ns_max;
+        for (bool done = tc_max <= 0; !done; it++) {
+          if (it == tc_max - 1) done = true;
           // T = Z Y  (rows 64..127 of S Y)
           if (tid == 0) {
             tc::fence_after_sync();
@@ -400,7 +429,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
           }
           tc::fence_before_sync();
           e2 = block_sum<float, TC_NT>(e2, red);
-          if (e2 < 1.0e-8f) last = true;
+          if (e2 < 1.0e-3f) done = true;
           tc::fence_smem_async();
           tc::fence_before_sync();
           __syncthreads();
@@ -416,7 +445,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
             tmo = 1;
             break;
           }
-          // S <- 1.5 S - 0.5 S T  (final step: W = coef * Z into WMAT)
+          // S <- 1.5 S - 0.5 S T (each thread rewrites only its own row)
 #pragma unroll
           for (int c0 = 0; c0 < 64; c0 += 16) {
             float v[16];
@@ -429,23 +458,15 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
               unpack8(*reinterpret_cast<const uint4*>(sm + L::S_LO + off), sl);
 #pragma unroll
               for (int j = 0; j < 8; j++) sn[j] = 1.5f * (sh[j] + sl[j]) - 0.5f * v[8 * g + j];
-              if (!last) {
-                uint4 h, l;
-                split8(sn, h, l);
-                // S rows are rewritten only after every thread has read its own row
-                // (each thread touches only row r), so no barrier is needed here
-                *reinterpret_cast<uint4*>(sm + L::S_HI + off) = h;
-                *reinterpret_cast<uint4*>(sm + L::S_LO + off) = l;
-              } else if (r >= 64) {
-                float* dst = Wm + (r - 64) * 64 + c0 + 8 * g;
-#pragma unroll
-                for (int j = 0; j < 8; j++) dst[j] = coef * sn[j];
-              }
+              uint4 h, l;
+              split8(sn, h, l);
+              *reinterpret_cast<uint4*>(sm + L::S_HI + off) = h;
+              *reinterpret_cast<uint4*>(sm + L::S_LO + off) = l;
             }
           }
           tc::fence_before_sync();
           __syncthreads();
-          if (!last) {
+          if (!done) {
             for (int i = tid; i < 8192 / 16; i += TC_NT) {
               reinterpret_cast<uint4*>(sm + L::B_HI)[i] = reinterpret_cast<const uint4*>(sm + L::S_HI)[i];
               reinterpret_cast<uint4*>(sm + L::B_LO)[i] = reinterpret_cast<const uint4*>(sm + L::S_LO)[i];
@@ -455,6 +476,50 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
             __syncthreads();
           }
         }
+        if (tmo) break;
+        // FP32 polish.  The coupled iteration never looks at A again, so the
+        // 16-bit rounding of the tensor-core phase shifts the matrix it is
+        // converging for.  Finish with the uncoupled iteration
+        //   Q = Z (A/s) Z,  Z <- (3 Z - Q Z) / 2,
+        // which references the exact A (kept in TMEM) at every step and so
+        // converges to (A/s)^(-1/2) from the tensor-core estimate.
+        float* Zf = reinterpret_cast<float*>(sm + L::ZF);
+        float* Af = reinterpret_cast<float*>(sm + L::YF);  // A / s
+        float* Pf = reinterpret_cast<float*>(sm + L::TF);  // A Z, then Q
+        {
+          float row[64];
+          if (r >= 64) {
+#pragma unroll
+            for (int c0 = 0; c0 < 64; c0 += 8) {
+              const uint32_t off = tc::kmajor_off_bf16(r, c0, 64);
+              float sh[8], sl[8];
+              unpack8(*reinterpret_cast<const uint4*>(sm + L::S_HI + off), sh);
+              unpack8(*reinterpret_cast<const uint4*>(sm + L::S_LO + off), sl);
+#pragma unroll
+              for (int j = 0; j < 8; j++) row[c0 + j] = sh[j] + sl[j];
+            }
+          }
+          __syncthreads();
+          if (r >= 64) {
+            float* dst = Zf + (r - 64) * 64;
+#pragma unroll
+            for (int j = 0; j < 64; j += 4)
+              *reinterpret_cast<float4*>(dst + j) = make_float4(row[j], row[j + 1], row[j + 2], row[j + 3]);
+          } else {
+#pragma unroll
+            for (int c0 = 0; c0 < 64; c0 += 16) {
+              float v[16];
+              tc::tmem_ld16(D1 + lane_off + c0, v);
+#pragma unroll
+              for (int j = 0; j < 16; j++) Af[r * 64 + c0 + j] = v[j] * inv_s;
+            }
+          }
+        }
+        tc::fence_before_sync();
+        __syncthreads();
+        it += ns_polish<TC_NP>(Af, Zf, Pf, red, tc_max > 0 ? TC_POLISH_MAX : a.max_ns_iter);
+        for (int idx = tid; idx < 64 * 64; idx += TC_NT) Wm[idx] = coef * Zf[idx];
+        __syncthreads();
         if (tmo) break;
         // wbar = Z (Z b) / s with Z = W / coef (W symmetric: column reads)
         if (tid < 64) {

@@ -23,6 +23,7 @@ OPT_EIGENSOLVER = 3
 EIG_NEWTON_SCHULZ = 0
 EIG_JACOBI = 1
 OPT_TENSOR_CORES = 4
+OPT_TC_NS_ITERS = 5
 
 
 class SweepDesc(C.Structure):
