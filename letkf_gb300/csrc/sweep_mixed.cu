@@ -322,6 +322,8 @@ __global__ void __launch_bounds__(MixedCfg<NP>::NT, MixedCfg<NP>::MINB) sweep_mi
           for (int c = 0; c < C::TC; c++) sm[S::A + (wi0 + r) * NP + wj0 + c] = wt[r][c];
       }
       if (st == LETKF_OK && tid == 0) a.infl[pt] = infl_update(n, infl, acc.p1, trace, acc.p3);
+      // st is uniform over the CTA; the W tiles above are written by other threads
+      __syncthreads();
       if (st != LETKF_OK)
         for (int idx = tid; idx < NP * NP; idx += NT) sm[S::A + idx] = (idx / NP == idx % NP) ? 1.f : 0.f;
     } else {

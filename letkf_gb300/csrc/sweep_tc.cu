@@ -603,8 +603,19 @@ int launch_sweep_tc(const SweepArgs& a, cudaStream_t stream, int grid_cap) {
   int dev = 0, nsm = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_tc_kernel, TC_NT, bytes);
-  if (per_sm < 1) per_sm = 1;
+  {
+    // residency from the registers and shared memory the kernel uses (the
+    // occupancy query reports one CTA per SM for this tensor-memory kernel)
+    cudaFuncAttributes fa;
+    int smem_sm = 0, regs_sm = 0;
+    if (cudaFuncGetAttributes(&fa, sweep_tc_kernel) != cudaSuccess) return LETKF_ERR_CUDA;
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+    const int by_smem = smem_sm / (int)(bytes + fa.sharedSizeBytes + 1024);
+    const int by_regs = regs_sm / (TC_NT * (fa.numRegs > 0 ? fa.numRegs : 128));
+    per_sm = by_smem < by_regs ? by_smem : by_regs;
+    if (per_sm < 1) per_sm = 1;
+  }
   // tensor memory: 512 columns per SM
   if (per_sm > (int)(512 / TC_TMEM_COLS)) per_sm = 512 / TC_TMEM_COLS;
   int grid = nsm * per_sm;
