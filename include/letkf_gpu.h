@@ -122,6 +122,33 @@ int letkf_search_speedy(int nlon, int nlat, const double* lon, const double* lat
                         const double* var_local_row, const double* params, const int64_t* offs,
                         int* nobsl, int* idx, double* rloc, double* rdiag, void* stream);
 
+/* Observation-space perturbations and departures on DEVICE buffers
+ * (speedy/letkf/letkf_obs.f90:157-174; lorenz96/letkf/letkf.f90:196-212):
+ * mean = sum_m hx[n][m] / ne (member order, FP64), hdxf[n][m] = hx[n][m] - mean,
+ * dep[n] = y[n] - mean; with gross_error > 0, |dep| > gross_error * err[n]
+ * sets qc_out[n] = 0.  Observations with qc_in[n] != 1 are skipped (hdxf = hx,
+ * dep = 0, qc_out = 0).  qc_in, qc_out and err (when gross_error <= 0) may be
+ * NULL.  hx and hdxf are [nobs][ne]; ne <= 512. */
+int letkf_obs_departure(int ne, int nobs, const double* hx, const double* y, const double* err,
+                        double gross_error, const int* qc_in, double* hdxf, double* dep, int* qc_out,
+                        void* stream);
+
+/* Lorenz-96 selection (lorenz96/letkf/letkf.f90:220-254).  obs_cell[ny] is
+ * the 1-based grid index of each observation (first maximum of its row of H,
+ * see letkf_l96_obs_cell); pix[npts] are 1-based grid indices.  An
+ * observation is kept when its cyclic distance d < xlocal * 2 sqrt(10/3) and
+ * rloc = exp(-0.5 (d/xlocal)^2) * exp(-0.5 (tdif/tlocal)^2) >= 1e-4
+ * (tdif = 0 when tlocal < 0); lists are in observation-index order and
+ * rdiag = obserr^2.  rdiag may be NULL. */
+int letkf_search_l96(int nx, int ny, const int* obs_cell, int npts, const int* pix, double xlocal,
+                     double tdif, double tlocal, double obserr, const int64_t* offs, int* nobsl,
+                     int* idx, double* rloc, double* rdiag, void* stream);
+
+/* Grid index of each observation of the Lorenz-96 driver: the first maximum
+ * of row i of h (ny x nx, column-major, on the device), 1-based
+ * (lorenz96/letkf/letkf.f90:226-228). */
+int letkf_l96_obs_cell(int nx, int ny, const double* h, int* cell, void* stream);
+
 /* ------------------------------------------------------------------------
  * Analysis sweep with the ensemble resident on the device.  Replaces the
  * das_letkf grid loop of the SCALE-style drivers (scale/letkf/letkf_tools.f90:

@@ -205,5 +205,54 @@ def search_speedy(grid, obs, pts, params, var_local_row, stream=None):
     return offs, idx[:total], rloc[:total], rdiag[:total]
 
 
+def l96_obs_cell(h, stream=None):
+    """Grid index (1-based) of each Lorenz-96 observation: the first maximum of
+    its row of h (ny, nx) (lorenz96/letkf/letkf.f90:226-228).  h: device tensor."""
+    import torch
+
+    ny, nx = h.shape
+    hf = h.to(torch.float64).t().contiguous()  # column-major (ny x nx)
+    cell = torch.empty(ny, dtype=torch.int32, device=h.device)
+    check(lib().letkf_l96_obs_cell(nx, ny, _dptr(hf), _dptr(cell), _stream(stream)), "l96_obs_cell")
+    return cell
+
+
+def obs_departure(hx, y, err=None, gross_error=0.0, qc=None, stream=None):
+    """Observation-space perturbations and departures (speedy/letkf/
+    letkf_obs.f90:157-174): hx float64 [nobs, ne] -> (hdxf, dep, qc_out)."""
+    import torch
+
+    nobs, ne = hx.shape
+    hx = hx.contiguous()
+    y = y.contiguous()
+    hdxf = torch.empty_like(hx)
+    dep = torch.empty(nobs, dtype=torch.float64, device=hx.device)
+    qc_out = torch.empty(nobs, dtype=torch.int32, device=hx.device)
+    check(lib().letkf_obs_departure(ne, nobs, _dptr(hx), _dptr(y), _dptr(err), float(gross_error), _dptr(qc),
+                                    _dptr(hdxf), _dptr(dep), _dptr(qc_out), _stream(stream)), "obs_departure")
+    return hdxf, dep, qc_out
+
+
+def search_l96(nx, obs_cell, pix, xlocal=3.0, obserr=1.0, tdif=0.0, tlocal=-1.0, stream=None):
+    """Lorenz-96 selection (lorenz96/letkf/letkf.f90:220-254) on device tensors.
+    obs_cell int32 [ny] (1-based grid index per observation), pix int32 [npts]
+    (1-based).  Returns (offs int64 [npts+1], idx int32, rloc, rdiag float64)."""
+    import torch
+
+    dev = obs_cell.device
+    npts, ny = pix.numel(), obs_cell.numel()
+    nobsl = torch.empty(npts, dtype=torch.int32, device=dev)
+    args = (nx, ny, _dptr(obs_cell), npts, _dptr(pix), float(xlocal), float(tdif), float(tlocal), float(obserr))
+    check(lib().letkf_search_l96(*args, None, _dptr(nobsl), None, None, None, _stream(stream)), "search_l96")
+    offs = exclusive_scan(nobsl, stream)
+    total = int(offs[-1].item())
+    idx = torch.empty(max(total, 1), dtype=torch.int32, device=dev)
+    rloc = torch.empty(max(total, 1), dtype=torch.float64, device=dev)
+    rdiag = torch.empty(max(total, 1), dtype=torch.float64, device=dev)
+    check(lib().letkf_search_l96(*args, _dptr(offs), None, _dptr(idx), _dptr(rloc), _dptr(rdiag), _stream(stream)),
+          "search_l96")
+    return offs, idx[:total], rloc[:total], rdiag[:total]
+
+
 __all__ = ["letkf_core", "core_batch_f64", "core_batch_mixed", "update_f64", "exclusive_scan", "gather_rows",
-           "search_scale", "search_speedy", "LETKF_OK"]
+           "search_scale", "search_speedy", "search_l96", "l96_obs_cell", "obs_departure", "LETKF_OK"]

@@ -1,0 +1,199 @@
+// search_l96.cu -- Lorenz-96 observation selection (lorenz96/letkf/letkf.f90:220-254).
+//
+// The reference loops over all observations i = 1..ny for every grid point
+// ix, takes the observation's grid index j as the first maximum of row i of H,
+// keeps it when the cyclic distance min(|j - ix|, nx - |j - ix|) < xmaxloc
+// (xmaxloc = xlocal * 2 * sqrt(10/3), :75) and drops it again when
+// rloc = exp(-0.5 (dist/xlocal)^2) * exp(-0.5 (tdif/tlocal)^2) < 1e-4.
+//
+// Here the observations are bucketed by grid cell once per call, each point
+// visits only the cells within the cut-off, and its list is then sorted by
+// observation index, which is the reference's emission order.  Cost per point
+// is O(L log L) instead of O(ny), so domains of 1e5 variables stay cheap.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "letkf_gpu.h"
+
+namespace letkf {
+
+int cuda_status(cudaError_t e);
+void note_launch();
+int launch_exclusive_scan(int n, const int* counts, int64_t* offs, int64_t* scratch, cudaStream_t stream);
+
+// first maximum of row i of h (ny x nx, column-major), 1-based
+__global__ void l96_cell_kernel(int nx, int ny, const double* __restrict__ h, int* __restrict__ cell) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ny) return;
+  double mx = h[i];
+  for (int j = 1; j < nx; j++) mx = fmax(mx, h[(size_t)j * ny + i]);
+  int jj = nx + 1;
+  for (int j = 0; j < nx; j++)
+    if (h[(size_t)j * ny + i] == mx) {
+      jj = j + 1;
+      break;
+    }
+  cell[i] = jj;
+}
+
+__global__ void l96_bucket_count(int nx, int ny, const int* __restrict__ cell, int* __restrict__ cnt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ny) return;
+  const int c = cell[i];
+  if (c >= 1 && c <= nx) atomicAdd(&cnt[c - 1], 1);
+}
+
+__global__ void l96_bucket_fill(int nx, int ny, const int* __restrict__ cell, const int64_t* __restrict__ boff,
+                                int* __restrict__ cursor, int* __restrict__ bobs) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ny) return;
+  const int c = cell[i];
+  if (c >= 1 && c <= nx) bobs[boff[c - 1] + atomicAdd(&cursor[c - 1], 1)] = i;
+}
+
+struct L96Ctx {
+  int nx, ny;
+  const int64_t* boff;  // [nx + 1] bucket offsets
+  const int* bobs;      // observation indices by bucket
+  double xlocal, xmaxloc, tfac;
+};
+
+// rloc of an observation at cyclic distance dist, or -1 when not selected
+__device__ __forceinline__ double l96_rloc(const L96Ctx& c, int dist) {
+  const double d = (double)dist;
+  if (!(d < c.xmaxloc)) return -1.0;
+  const double q = d / c.xlocal;
+  const double r = exp(-0.5 * (q * q)) * c.tfac;
+  return r < 0.0001 ? -1.0 : r;
+}
+
+template <typename F>
+__device__ __forceinline__ void l96_visit(const L96Ctx& c, int ix, F&& f) {
+  const int nx = c.nx;
+  int reach = (int)ceil(c.xmaxloc);  // dist < xmaxloc  =>  dist <= reach
+  if (2 * reach + 1 >= nx) {
+    for (int j = 1; j <= nx; j++) {
+      const int a = abs(j - ix), dist = min(a, nx - a);
+      f(j, dist);
+    }
+  } else {
+    for (int off = -reach; off <= reach; off++) {
+      int j = ix + off;
+      if (j < 1) j += nx;
+      if (j > nx) j -= nx;
+      const int a = abs(j - ix), dist = min(a, nx - a);
+      f(j, dist);
+    }
+  }
+}
+
+__global__ void l96_search_kernel(L96Ctx c, int npts, const int* __restrict__ pix, const int64_t* __restrict__ offs,
+                                  int* __restrict__ nobsl, int* __restrict__ idx, double* __restrict__ rloc,
+                                  double* __restrict__ rdiag, double rdiag_value) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npts) return;
+  const int ix = pix[p];
+  if (!idx) {
+    int n = 0;
+    l96_visit(c, ix, [&](int j, int dist) {
+      if (l96_rloc(c, dist) >= 0.0) n += (int)(c.boff[j] - c.boff[j - 1]);
+    });
+    nobsl[p] = n;
+    return;
+  }
+  const int64_t base = offs[p];
+  int n = 0;
+  l96_visit(c, ix, [&](int j, int dist) {
+    const double r = l96_rloc(c, dist);
+    if (r < 0.0) return;
+    for (int64_t q = c.boff[j - 1]; q < c.boff[j]; q++) {
+      // insertion into the list kept sorted by observation index
+      const int ob = c.bobs[q];
+      int t = n;
+      while (t > 0 && idx[base + t - 1] > ob) {
+        idx[base + t] = idx[base + t - 1];
+        rloc[base + t] = rloc[base + t - 1];
+        t--;
+      }
+      idx[base + t] = ob;
+      rloc[base + t] = r;
+      n++;
+    }
+  });
+  if (rdiag)
+    for (int t = 0; t < n; t++) rdiag[base + t] = rdiag_value;
+}
+
+}  // namespace letkf
+
+using namespace letkf;
+
+extern "C" {
+
+int letkf_l96_obs_cell(int nx, int ny, const double* h, int* cell, void* stream) {
+  if (nx < 1 || ny < 0 || (ny > 0 && (!h || !cell))) return LETKF_ERR_ARG;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n < 1) {
+    cudaGetLastError();
+    return LETKF_ERR_NOGPU;
+  }
+  if (ny == 0) return LETKF_OK;
+  l96_cell_kernel<<<(ny + 127) / 128, 128, 0, (cudaStream_t)stream>>>(nx, ny, h, cell);
+  note_launch();
+  return cuda_status(cudaGetLastError());
+}
+
+int letkf_search_l96(int nx, int ny, const int* obs_cell, int npts, const int* pix, double xlocal, double tdif,
+                     double tlocal, double obserr, const int64_t* offs, int* nobsl, int* idx, double* rloc,
+                     double* rdiag, void* stream) {
+  if (nx < 1 || ny < 0 || npts < 0 || !(xlocal > 0.0) || (ny > 0 && !obs_cell) || (npts > 0 && !pix))
+    return LETKF_ERR_ARG;
+  if (!idx && !nobsl) return LETKF_ERR_ARG;
+  if (idx && (!offs || !rloc)) return LETKF_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return LETKF_ERR_NOGPU;
+  }
+  if (npts == 0) return LETKF_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  // buckets: counts [nx], offsets [nx+1], cursor [nx], observations [ny], scan scratch
+  const int nb = (nx + 1023) / 1024 + 1;
+  const size_t bytes = sizeof(int64_t) * ((size_t)nx + 1 + nb) + sizeof(int) * (2 * (size_t)nx + (size_t)ny + 1);
+  unsigned char* buf = nullptr;
+  if (cudaMallocAsync((void**)&buf, bytes, s) != cudaSuccess) return LETKF_ERR_CUDA;
+  int64_t* boff = reinterpret_cast<int64_t*>(buf);
+  int64_t* scr = boff + nx + 1;
+  int* cnt = reinterpret_cast<int*>(scr + nb);
+  int* cur = cnt + nx;
+  int* bobs = cur + nx;
+  int st = cuda_status(cudaMemsetAsync(cnt, 0, sizeof(int) * 2 * (size_t)nx, s));
+  if (st == LETKF_OK && ny > 0) {
+    l96_bucket_count<<<(ny + 255) / 256, 256, 0, s>>>(nx, ny, obs_cell, cnt);
+    note_launch();
+  }
+  if (st == LETKF_OK) st = launch_exclusive_scan(nx, cnt, boff, scr, s);
+  if (st == LETKF_OK && ny > 0) {
+    l96_bucket_fill<<<(ny + 255) / 256, 256, 0, s>>>(nx, ny, obs_cell, boff, cur, bobs);
+    note_launch();
+  }
+  if (st == LETKF_OK) {
+    L96Ctx c;
+    c.nx = nx;
+    c.ny = ny;
+    c.boff = boff;
+    c.bobs = bobs;
+    c.xlocal = xlocal;
+    c.xmaxloc = xlocal * 2.0 * sqrt(10.0 / 3.0);
+    const double tq = tlocal < 0.0 ? 0.0 : tdif / tlocal;
+    c.tfac = tlocal < 0.0 ? 1.0 : exp(-0.5 * (tq * tq));
+    l96_search_kernel<<<(npts + 127) / 128, 128, 0, s>>>(c, npts, pix, offs, nobsl, idx, rloc, rdiag,
+                                                         obserr * obserr);
+    note_launch();
+    st = cuda_status(cudaGetLastError());
+  }
+  cudaFreeAsync(buf, s);
+  return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,182 @@
+"""Host-side drivers that replace the reference's das_letkf grid loops with
+the device path of this library (search -> gather -> batched core -> update).
+
+* ``l96_letkf``   -- lorenz96/letkf/letkf.f90:180-265 (one time slot)
+* ``speedy_letkf`` -- speedy/letkf/letkf_tools.f90:44-203 (das_letkf)
+* ``speedy_sort_obs`` -- speedy/letkf/letkf_obs.f90:243-313 (bucket sort)
+
+The regional SCALE-style driver is the resident ``sweep.Sweep`` handle.  All
+compute runs in libletkf_gpu.so; torch only holds device memory and does
+layout transposes.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import core as K
+
+
+# ----------------------------------------------------------------------- SPEEDY
+def speedy_sort_obs(lon, lat, olon, olat):
+    """Stable bucket sort of observations by (latitude band, longitude cell)
+    (speedy/letkf/letkf_obs.f90:243-313).  Band j (1-based, 1..nlat-1) holds
+    lat(j) <= y < lat(j+1); cell i holds lon(i) <= x < lon(i+1), the last cell
+    up to 360.  Returns (perm, nobsgrd[nlat, nlon]) with nobsgrd[j-1, i-1] the
+    cumulative count through cell (i, j); observations outside every band are
+    dropped, and row nlat of nobsgrd is never written by the reference (0).
+    Longitudes must lie in [0, 360): the reference counts an observation at
+    360 in its band but places it in no cell, leaving an unfilled slot that
+    the next band's first cell range covers; here it is dropped."""
+    lon = np.asarray(lon, dtype=np.float64)
+    lat = np.asarray(lat, dtype=np.float64)
+    olon = np.asarray(olon, dtype=np.float64)
+    olat = np.asarray(olat, dtype=np.float64)
+    nlon, nlat = lon.size, lat.size
+    j = np.searchsorted(lat, olat, side="right")            # lat[j-1] <= y < lat[j]
+    i = np.searchsorted(lon, olon, side="right")            # lon[i-1] <= x < lon[i] (i < nlon)
+    ok = (j >= 1) & (j <= nlat - 1) & (i >= 1) & ((i < nlon) | (olon < 360.0))
+    key = (j - 1).astype(np.int64) * nlon + (i - 1)
+    sel = np.nonzero(ok)[0]
+    perm = sel[np.argsort(key[sel], kind="stable")].astype(np.int32)
+    counts = np.bincount(key[sel], minlength=nlon * nlat).astype(np.int64)
+    grd = np.cumsum(counts).reshape(nlat, nlon).astype(np.int32)
+    grd[nlat - 1, :] = 0
+    return perm, grd
+
+
+def var_local_n2n(var_local):
+    """speedy/letkf/letkf_tools.f90:50-57: variable n reuses the transform of
+    the first variable i <= n with an identical localisation row (0-based)."""
+    vl = np.asarray(var_local, dtype=np.float64)
+    tiny = np.finfo(np.float64).tiny
+    n2n = np.zeros(vl.shape[0], dtype=np.int64)
+    for n in range(1, vl.shape[0]):
+        for i in range(n + 1):
+            n2n[n] = i
+            if np.max(np.abs(vl[i] - vl[n])) < tiny:
+                break
+    return n2n
+
+
+def speedy_letkf(grid, obs, hdxf, dep, gues3d, logpfm, dlon_zero, params, var_local, infl3d, gues2d=None,
+                 infl2d=None, iv3d_q=3, q_top_lev=5, stream=None):
+    """das_letkf of speedy/letkf/letkf_tools.f90:44-203 on the device.
+
+    grid: dict lon, lat (float64 device), nobsgrd (int32 [nlat, nlon] device).
+    obs: dict elm, lon, lat, lev, dat, err (float64 device, bucket-sorted).
+    hdxf: float64 [nobs, ne]; dep: float64 [nobs] (sorted like obs).
+    gues3d: float64 [nv3d, nlev, ne, nij] full members; gues2d [nv2d, ne, nij].
+    logpfm: float64 [nlev, nij]; dlon_zero: float64 [nij].
+    params: (dist_zero, dist_zerov, dlat_zero, sigma_obs, sigma_obsv).
+    var_local: [nv3d + nv2d, 7] localisation rows (u, v, t, q, rh, ps, rain).
+    infl3d: float64 [nv3d, nlev, nij] (in/out, the reference's work3d);
+    infl2d: float64 [nv2d, nij].
+    Returns (anal3d, anal2d) shaped like the inputs.  Per (point, variable
+    group) the status of the core is checked; a failed eigensolve raises."""
+    import torch
+
+    nv3d, nlev, ne, nij = gues3d.shape
+    nv2d = 0 if gues2d is None else gues2d.shape[0]
+    dev = gues3d.device
+    n2n = var_local_n2n(var_local)
+    npts = nlev * nij
+    ilev = torch.arange(1, nlev + 1, dtype=torch.int32, device=dev).repeat_interleave(nij)
+    ijx = torch.arange(nij, device=dev).repeat(nlev)          # point p = (ilev - 1) * nij + ij
+    nlon = grid["lon"].numel()
+    jj, ii = torch.div(ijx, nlon, rounding_mode="floor"), ijx % nlon
+    pts3 = {"lon": grid["lon"][ii].contiguous(), "lat": grid["lat"][jj].contiguous(),
+            "dlon_zero": dlon_zero[ijx].contiguous(), "ilev": ilev.contiguous(),
+            "logpfm": logpfm.reshape(-1).contiguous()}
+    # members with the member index fastest: [nv][npts][ne]
+    xb3 = gues3d.permute(0, 1, 3, 2).reshape(nv3d, npts, ne).contiguous()
+    xa3 = torch.empty_like(xb3)
+    trans_of = {}
+
+    def analyse(group, pts, infl):
+        offs, idx, rloc, rdiag = K.search_speedy(grid, obs, pts, params, var_local[group], stream)
+        rows, dl = K.gather_rows(idx, hdxf, dep, stream)
+        out = K.core_batch_f64(ne, offs, rows, rdiag, rloc, dl, infl, stream=stream)
+        if bool((out["status"] != K.LETKF_OK).any()):
+            raise K.LetkfError(int(out["status"].max()), "speedy_letkf: eigensolver")
+        return out["trans"]
+
+    for n in range(nv3d):
+        g = int(n2n[n])
+        if g < n:
+            infl3d[n] = infl3d[g]
+        else:
+            pinf = infl3d[n].reshape(-1).contiguous()
+            trans_of[n] = analyse(n, pts3, pinf)
+            infl3d[n] = pinf.reshape(nlev, nij)
+        tr = trans_of[g]
+        if n == iv3d_q and nlev >= q_top_lev:
+            # no analysis of upper-level q (letkf_tools.f90:173-178): identity transform
+            eye = torch.eye(ne, dtype=torch.float64, device=dev)
+            lo = (q_top_lev - 1) * nij
+            tr = tr.clone()
+            tr[lo:] = eye
+        xa3[n] = K.update_f64(xb3[n:n + 1], tr, None, stream)[0]
+    anal3d = xa3.reshape(nv3d, nlev, nij, ne).permute(0, 1, 3, 2).contiguous()
+    anal2d = None
+    if nv2d:
+        pts2 = {k: v[:nij].contiguous() for k, v in pts3.items()}
+        xb2 = gues2d.permute(0, 2, 1).contiguous()
+        xa2 = torch.empty_like(xb2)
+        for n in range(nv2d):
+            g = int(n2n[nv3d + n])
+            if g < nv3d + n:
+                if g < nv3d:
+                    tr = trans_of[g][:nij]
+                    infl2d[n] = infl3d[g][0]
+                else:
+                    tr = trans_of[g]
+                    infl2d[n] = infl2d[g - nv3d]
+            else:
+                pinf = infl2d[n].contiguous()
+                tr = trans_of[nv3d + n] = analyse(nv3d + n, pts2, pinf)
+                infl2d[n] = pinf
+            xa2[n] = K.update_f64(xb2[n:n + 1], tr.contiguous(), None, stream)[0]
+        anal2d = xa2.permute(0, 2, 1).contiguous()
+    return anal3d, anal2d
+
+
+# -------------------------------------------------------------------- Lorenz-96
+def l96_letkf(xf, hxf, y, obs_cell, obserr=1.0, xlocal=3.0, parm_infl=None, msw_infl=1.05, precision="f64",
+              stream=None):
+    """One LETKF analysis of the Lorenz-96 driver (lorenz96/letkf/letkf.f90:
+    180-265, one time slot, fixed localisation).
+
+    xf: float64 [nx, ne] background members; hxf: float64 [ny, ne] = H xf;
+    y: float64 [ny]; obs_cell: int32 [ny] 1-based grid index of each
+    observation (core.l96_obs_cell of H).  parm_infl: float64 [nx] (in/out;
+    default msw_infl everywhere); with msw_infl > 0 it is reset to msw_infl
+    after every core (the reference's fixed inflation).  precision "f64" (the
+    plain form) or "mixed".  Returns (xa [nx, ne], parm_infl)."""
+    import torch
+
+    nx, ne = xf.shape
+    dev = xf.device
+    if parm_infl is None:
+        parm_infl = torch.full((nx,), float(msw_infl), dtype=torch.float64, device=dev)
+    hdxf, dep, _ = K.obs_departure(hxf, y, stream=stream)
+    pix = torch.arange(1, nx + 1, dtype=torch.int32, device=dev)
+    offs, idx, rloc, rdiag = K.search_l96(nx, obs_cell, pix, xlocal, obserr, stream=stream)
+    rows, dl = K.gather_rows(idx, hdxf, dep, stream)
+    if precision == "f64":
+        out = K.core_batch_f64(ne, offs, rows, rdiag, rloc, dl, parm_infl, stream=stream)
+        trans = out["trans"]
+    elif precision == "mixed":
+        f = lambda t: t.to(torch.float32).contiguous()
+        out = K.core_batch_mixed(ne, offs, f(rows), f(rdiag), f(rloc), f(dl), parm_infl, stream=stream)
+        trans = out["trans"].to(torch.float64)
+    else:
+        raise ValueError(f"precision {precision!r}")
+    if bool((out["status"] != K.LETKF_OK).any()):
+        raise K.LetkfError(int(out["status"].max()), "l96_letkf: eigensolver")
+    if msw_infl > 0.0:
+        parm_infl.fill_(float(msw_infl))
+    xa = K.update_f64(xf.reshape(1, nx, ne).contiguous(), trans.contiguous(), None, stream)[0]
+    return xa, parm_infl
+
+
+__all__ = ["speedy_sort_obs", "var_local_n2n", "speedy_letkf", "l96_letkf"]

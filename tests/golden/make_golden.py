@@ -146,7 +146,7 @@ def l96_fixture():
         rloc_all.append(rl)
         offs.append(offs[-1] + idx.size)
         trans_all.append(r["trans"])
-    return {"xf": xf, "h": h, "hdxf": hdxf, "dep": dep, "obserr": np.float64(c["obserr"]), "xa": xa,
+    return {"xf": xf, "h": h, "y": c["y"], "hdxf": hdxf, "dep": dep, "obserr": np.float64(c["obserr"]), "xa": xa,
             "trans": np.array(trans_all), "offs": np.array(offs, dtype=np.int64),
             "idx": np.concatenate(idx_all).astype(np.int32), "rloc": np.concatenate(rloc_all)}
 

@@ -1,0 +1,204 @@
+"""Model drivers on the device path: Lorenz-96 (lorenz96/letkf/letkf.f90:180-265)
+and SPEEDY (speedy/letkf/letkf_tools.f90:44-203), against the golden L96
+analysis and the oracle.  FP64 plain form: 1e-10 relative; local lists bit-exact."""
+import os
+
+import numpy as np
+import pytest
+
+from letkf_gb300 import synthetic as S
+from letkf_gb300.drivers import speedy_sort_obs, var_local_n2n
+from oracle import oracle as O
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _close(a, b, rtol):
+    scale = max(np.abs(b).max(), 1e-300)
+    err = np.abs(np.asarray(a) - b).max() / scale
+    assert err <= rtol, f"relative error {err:.3e} > {rtol:.1e}"
+
+
+# ------------------------------------------------------------------- host (CPU)
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_speedy_sort_matches_oracle(seed):
+    c = S.speedy_case(seed, nstations=150)
+    # observations exactly on grid lines, next to 360, and outside the last band
+    olon = np.concatenate([c["olon"], c["lon"][:6], [359.999999, 0.0, 360.0 - 1e-12]])
+    olat = np.concatenate([c["olat"], c["lat"][:6], [c["lat"][-1], c["lat"][0], 89.9]])
+    p1, g1 = speedy_sort_obs(c["lon"], c["lat"], olon, olat)
+    p2, g2 = O.speedy_sort_obs(c["lon"], c["lat"], olon, olat)
+    np.testing.assert_array_equal(p1, p2)
+    np.testing.assert_array_equal(g1, g2)
+
+
+def test_speedy_sort_empty():
+    lon, lat = S.speedy_grid()
+    p, g = speedy_sort_obs(lon, lat, np.zeros(0), np.zeros(0))
+    assert p.size == 0 and not g.any()
+
+
+def test_var_local_n2n():
+    vl = np.ones((6, 7))
+    assert var_local_n2n(vl).tolist() == [0, 0, 0, 0, 0, 0]
+    vl[2, 3] = 0.5
+    vl[4] = vl[2]
+    vl[5, 0] = 0.0
+    assert var_local_n2n(vl).tolist() == [0, 0, 2, 0, 2, 5]
+
+
+# ------------------------------------------------------------------- Lorenz-96
+def _t(a, dt, dev):
+    import torch
+
+    return torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,rtol", [("f64", 1e-10), ("mixed", 2e-5)])
+def test_l96_analysis_matches_golden(cuda, precision, rtol):
+    import torch
+
+    from letkf_gb300.core import l96_obs_cell
+    from letkf_gb300.drivers import l96_letkf
+
+    g = np.load(os.path.join(GOLD, "l96_analysis.npz"))
+    xf = _t(g["xf"], torch.float64, cuda)
+    h = _t(g["h"], torch.float64, cuda)
+    hxf = h @ xf
+    y = _t(g["y"], torch.float64, cuda)
+    cell = l96_obs_cell(h)
+    assert cell.cpu().numpy().tolist() == list(range(1, 41))
+    xa, infl = l96_letkf(xf, hxf, y, cell, obserr=float(g["obserr"]), precision=precision)
+    _close(xa.cpu().numpy(), g["xa"], rtol)
+    assert np.all(infl.cpu().numpy() == 1.05)
+
+
+@pytest.mark.gpu
+def test_l96_search_matches_oracle_with_shared_cells(cuda):
+    """Observations scattered over the cells (several per cell, empty cells,
+    a dense H with ties) on a 300-variable ring; lists in observation order."""
+    import torch
+
+    from letkf_gb300.core import l96_obs_cell, search_l96
+
+    rng = np.random.default_rng(5)
+    nx, ny = 300, 420
+    cells = rng.integers(1, nx + 1, ny)
+    h = np.zeros((ny, nx))
+    h[np.arange(ny), cells - 1] = 1.0
+    ties = rng.choice(ny, 30, replace=False)
+    h[ties, (cells[ties] + 7) % nx] = 1.0      # a tie: the first maximum wins
+    cell = l96_obs_cell(_t(h, torch.float64, cuda))
+    ref_cell = np.array([np.nonzero(h[i] == h[i].max())[0][0] + 1 for i in range(ny)])
+    np.testing.assert_array_equal(cell.cpu().numpy(), ref_cell)
+    for xlocal in (3.0, 0.7, 40.0):
+        pix = torch.arange(1, nx + 1, dtype=torch.int32, device=cuda)
+        offs, idx, rloc, rdiag = search_l96(nx, cell, pix, xlocal, obserr=0.5)
+        offs, idx, rloc = offs.cpu().numpy(), idx.cpu().numpy(), rloc.cpu().numpy()
+        assert np.all(rdiag.cpu().numpy() == 0.25)
+        for ix in range(1, nx + 1):
+            ri, rl = O.l96_select(h, ix, xlocal)
+            s = slice(offs[ix - 1], offs[ix])
+            np.testing.assert_array_equal(idx[s], ri, err_msg=f"ix {ix} xlocal {xlocal}")
+            np.testing.assert_allclose(rloc[s], rl, rtol=1e-14)
+
+
+@pytest.mark.gpu
+def test_l96_search_small_ring_and_no_obs(cuda):
+    """A ring shorter than the cut-off window visits every cell once; no
+    observations gives empty lists."""
+    import torch
+
+    from letkf_gb300.core import search_l96
+
+    nx = 12
+    h = np.eye(nx)
+    cell = torch.arange(1, nx + 1, dtype=torch.int32, device=cuda)
+    pix = torch.arange(1, nx + 1, dtype=torch.int32, device=cuda)
+    offs, idx, rloc, _ = search_l96(nx, cell, pix, 3.0)
+    offs, idx = offs.cpu().numpy(), idx.cpu().numpy()
+    for ix in range(1, nx + 1):
+        ri, _ = O.l96_select(h, ix, 3.0)
+        np.testing.assert_array_equal(idx[offs[ix - 1]:offs[ix]], ri)
+    offs, idx, _, _ = search_l96(nx, torch.zeros(0, dtype=torch.int32, device=cuda), pix, 3.0)
+    assert offs.cpu().numpy().tolist() == [0] * (nx + 1)
+
+
+@pytest.mark.gpu
+def test_obs_departure_matches_sequential_mean(cuda):
+    import torch
+
+    from letkf_gb300.core import obs_departure
+
+    rng = np.random.default_rng(3)
+    for ne in (20, 64, 130):
+        nobs = 1000 + ne
+        hx = rng.standard_normal((nobs, ne)) * 3 + 10
+        y = rng.standard_normal(nobs) * 2 + 10
+        err = rng.uniform(0.1, 1.0, nobs)
+        qc_in = (rng.uniform(size=nobs) > 0.1).astype(np.int32)
+        hdxf, dep, qc = obs_departure(_t(hx, torch.float64, cuda), _t(y, torch.float64, cuda),
+                                      _t(err, torch.float64, cuda), 3.0, _t(qc_in, torch.int32, cuda))
+        hdxf, dep, qc = hdxf.cpu().numpy(), dep.cpu().numpy(), qc.cpu().numpy()
+        for n in range(nobs):
+            if qc_in[n] != 1:
+                assert qc[n] == 0 and dep[n] == 0.0
+                np.testing.assert_array_equal(hdxf[n], hx[n])
+                continue
+            s = hx[n, 0]
+            for m in range(1, ne):
+                s = s + hx[n, m]
+            s = s / ne
+            assert dep[n] == y[n] - s
+            np.testing.assert_array_equal(hdxf[n], hx[n] - s)
+            assert qc[n] == (0 if abs(y[n] - s) > 3.0 * err[n] else 1)
+
+
+# ---------------------------------------------------------------------- SPEEDY
+@pytest.mark.gpu
+def test_speedy_das_letkf_matches_oracle(cuda):
+    """Full 96x48x7 SPEEDY-grid analysis of u, v, t, q (k = 40) on the device;
+    a subset of points checked against the oracle's obs_local + letkf_core +
+    update, including the no-analysis of upper-level q."""
+    import torch
+
+    from letkf_gb300.drivers import speedy_letkf
+
+    c = S.speedy_case(4, nstations=300)
+    perm, grd = speedy_sort_obs(c["lon"], c["lat"], c["olon"], c["olat"])
+    srt = {k: c[k][perm] for k in ("elm", "olon", "olat", "olev", "odat", "oerr")}
+    hdxf, dep = c["hdxf"][perm], c["dep"][perm]
+    f = lambda a: _t(a, torch.float64, cuda)
+    grid = {"lon": f(c["lon"]), "lat": f(c["lat"]), "nobsgrd": _t(grd, torch.int32, cuda)}
+    obs = {"elm": f(srt["elm"]), "lon": f(srt["olon"]), "lat": f(srt["olat"]), "lev": f(srt["olev"]),
+           "dat": f(srt["odat"]), "err": f(srt["oerr"])}
+    params = (c["dist_zero"], c["dist_zerov"], c["dlat_zero"], c["sigma_obs"], c["sigma_obsv"])
+    nv3d, nlev, ne, nij = c["gues3d"].shape
+    var_local = np.ones((nv3d, 7))
+    infl = torch.full((nv3d, nlev, nij), 1.1, dtype=torch.float64, device=cuda)
+    anal3d, _ = speedy_letkf(grid, obs, f(hdxf), f(dep), f(c["gues3d"]), f(c["logpfm"]), f(c["dlon_zero"]), params,
+                             var_local, infl)
+    anal3d = anal3d.cpu().numpy()
+    infl = infl.cpu().numpy()
+    so = O.SpeedyObs(c["lon"], c["lat"], grd, srt["elm"], srt["olon"], srt["olat"], srt["olev"], srt["odat"],
+                     srt["oerr"], c["dist_zero"], c["dist_zerov"], c["dlat_zero"], c["sigma_obs"], c["sigma_obsv"],
+                     var_local[0])
+    checked = 0
+    for p in range(0, nlev * nij, 53):
+        ilev, ij = divmod(p, nij)
+        ri, rl, rd = so.obs_local(c["glon"][ij], c["glat"][ij], c["dlon_zero"][ij], ilev + 1, c["logpfm"][ilev, ij])
+        r = O.letkf_core(hdxf[ri] if ri.size else np.zeros((1, ne)), rd if ri.size else np.ones(1),
+                         rl if ri.size else np.ones(1), dep[ri] if ri.size else np.zeros(1), 1.1, nobsl=ri.size)
+        assert abs(infl[0, ilev, ij] - r["parm_infl"]) <= 1e-10 * abs(r["parm_infl"])
+        for n in range(nv3d):
+            xb = c["gues3d"][n, ilev, :, ij]
+            m = xb[0]
+            for k in range(1, ne):
+                m = m + xb[k]
+            m = m / ne
+            xp = xb - m
+            ref = m + xp @ (np.eye(ne) if (n == 3 and ilev + 1 >= 5) else r["trans"])
+            _close(anal3d[n, ilev, :, ij], ref, 1e-10)
+        checked += 1
+    assert checked > 40
