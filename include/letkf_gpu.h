@@ -211,6 +211,84 @@ int letkf_sweep_get_diagnostics(letkf_sweep_t h, double* infl, int* nobsl, int* 
 int letkf_sweep_sorted_obs(letkf_sweep_t h, int* nobsgrd);
 /* device pointers of the resident buffers (for callers that stage data themselves) */
 int letkf_sweep_device_buffers(letkf_sweep_t h, void** xb, void** xa, double** infl, int** nobsl);
+/* upper bound of the device bytes a handle with this descriptor and nobs
+ * observations holds, including the staging of set_obs and run */
+int letkf_sweep_footprint(const letkf_sweep_desc* desc, int nobs, size_t* bytes);
+
+/* ------------------------------------------------------------------------
+ * Serving: analysis jobs for domains of different sizes and ensemble sizes,
+ * submitted as they arrive and run with continuous batching on one device.
+ * No counterpart in the reference (its drivers analyse one domain per run).
+ *   - nslots jobs are on the device at once, each on its own stream with
+ *     1/nslots of the SMs for the sweep kernels, so a job that arrives while
+ *     others run starts as soon as a slot and memory are free and overlaps
+ *     with them;
+ *   - admission is by device footprint (letkf_sweep_footprint and the L96
+ *     equivalent) against hbm_budget, in arrival order;
+ *   - jobs with the same domain key >= 0 reuse that domain's device state
+ *     (points, observations and ensemble buffers stay resident between jobs);
+ *     idle resident domains are released oldest first when memory is needed;
+ *   - host buffers of a job must stay valid until the job is finished.
+ * ---------------------------------------------------------------------- */
+#define LETKF_PENDING 7            /* a job that has not finished */
+#define LETKF_JOB_SCALE_SWEEP 0    /* regional sweep (letkf_sweep_* semantics) */
+#define LETKF_JOB_L96 1            /* Lorenz-96 ring (letkf_search_l96 + core + update) */
+
+typedef struct letkf_server_desc {
+  int device;         /* CUDA device ordinal */
+  int nslots;         /* jobs on the device at once, 1..16 */
+  size_t hbm_budget;  /* device bytes for jobs and resident domains; 0: 80% of free memory */
+} letkf_server_desc;
+
+typedef struct letkf_job_desc {
+  int kind;           /* LETKF_JOB_SCALE_SWEEP or LETKF_JOB_L96 */
+  int64_t domain;     /* resident-domain key (>= 0), or -1: release the device state after the job */
+  int precision;      /* LETKF_PREC_F64 or LETKF_PREC_MIXED */
+  int ne, nv;
+  /* grid points: SCALE sweep (nlon x nlat bucket grid, npts points) or the
+   * L96 ring (npts = nx, nv = 1; pri/prj/prlev unused) */
+  int nlon, nlat, npts;
+  const double *pri, *prj, *prlev;
+  double params[16];  /* SCALE search parameters (letkf_search_scale order) */
+  double minfl;
+  /* observations: SCALE records (unsorted), or for L96 obs_cell[nobs] */
+  int nobs;
+  const double *ori, *orj, *olev, *odat, *oerr;
+  const int* ocls;
+  const int* obs_cell;
+  double xlocal, obserr, msw_infl; /* L96 localisation, obs error, fixed inflation (> 0) */
+  const double* dep;  /* [nobs] departures */
+  const void* hdxf;   /* [nobs][ne]: float32 (SCALE, MIXED) else float64 */
+  /* ensemble [nv][npts][ne]: float32 (SCALE, MIXED) else float64; in / out */
+  const void* xb;
+  void* xa;
+  double* infl;       /* [npts] adaptive inflation in / out, may be NULL (1.0) */
+} letkf_job_desc;
+
+typedef struct letkf_job_result {
+  int status;         /* LETKF_OK, LETKF_PENDING or an error */
+  double t_submit, t_start, t_done;  /* seconds since the server started */
+  size_t device_bytes;               /* footprint charged to the job */
+} letkf_job_result;
+
+typedef struct letkf_server_stats {
+  int64_t submitted, completed, failed;
+  double p50_latency_s, p99_latency_s;  /* submit -> done, completed jobs */
+  double points_per_s;                  /* grid points of completed jobs / (last done - first submit) */
+  size_t peak_bytes;                    /* largest charged footprint in use at once */
+  int resident_domains;
+} letkf_server_stats;
+
+typedef struct letkf_server_s* letkf_server_t;
+
+int letkf_server_create(letkf_server_t* server, const letkf_server_desc* desc);
+/* copies the descriptor (not the arrays) and queues the job; *job_id >= 0 */
+int letkf_server_submit(letkf_server_t server, const letkf_job_desc* job, int64_t* job_id);
+/* waits up to timeout_s (< 0: no limit) for the job; LETKF_PENDING on timeout */
+int letkf_server_wait(letkf_server_t server, int64_t job_id, double timeout_s, letkf_job_result* result);
+int letkf_server_stats_get(letkf_server_t server, letkf_server_stats* stats);
+/* finishes every queued job, then releases the device state */
+int letkf_server_destroy(letkf_server_t server);
 
 /* exclusive scan of n int32 counts into int64 offsets[n+1] (device) */
 int letkf_exclusive_scan(int n, const int* counts, int64_t* offs, void* stream);

@@ -53,6 +53,7 @@ const char* letkf_status_string(int s) {
     case LETKF_ERR_CAPACITY: return "size beyond this build's limits";
     case LETKF_ERR_NOGPU: return "no CUDA device";
     case LETKF_ERR_TIMEOUT: return "bounded device wait timed out";
+    case LETKF_PENDING: return "job not finished";
     default: return "unknown status";
   }
 }

@@ -136,6 +136,7 @@ struct letkf_sweep_s {
   int *status = nullptr, *nobsl = nullptr, *sweeps = nullptr, *counter = nullptr;
   int *defer_list = nullptr, *defer_count = nullptr, *err_flag = nullptr;
   cudaStream_t stream = nullptr;
+  cudaEvent_t ran = nullptr;  // recorded after a run issued on another stream
   int grid_cap = 0;
   int max_sweeps = 12;
   int use_ns = 1;
@@ -143,15 +144,17 @@ struct letkf_sweep_s {
   int tc_ns_max = 14;
 };
 
-static void dfree(void* p) {
-  if (p) cudaFree(p);
+// Stream-ordered allocation: no call of a handle synchronises the whole
+// device, so handles on other streams keep running (the serving slots).
+static void dfree(void* p, cudaStream_t s) {
+  if (p) cudaFreeAsync(p, s);
 }
 
 template <typename T>
-static int dalloc(T** p, size_t n) {
+static int dalloc(T** p, size_t n, cudaStream_t s) {
   *p = nullptr;
   if (n == 0) n = 1;
-  return cudaMalloc((void**)p, n * sizeof(T)) == cudaSuccess ? LETKF_OK : LETKF_ERR_CUDA;
+  return cudaMallocAsync((void**)p, n * sizeof(T), s) == cudaSuccess ? LETKF_OK : LETKF_ERR_CUDA;
 }
 
 static size_t elem(const letkf_sweep_s* h) { return h->d.precision == LETKF_PREC_F64 ? 8 : 4; }
@@ -173,46 +176,59 @@ int letkf_sweep_create(letkf_sweep_t* out, const letkf_sweep_desc* d) {
   h->d = *d;
   const size_t np = (size_t)d->npts;
   int st = LETKF_OK;
-  st |= dalloc(&h->pri, np);
-  st |= dalloc(&h->prj, np);
-  st |= dalloc(&h->prlev, np);
-  st |= dalloc(&h->prz, np);
-  st |= dalloc(&h->plogr, np);
-  st |= dalloc(&h->order, np);
-  st |= dalloc((char**)&h->xb, np * d->nv * d->ne * elem(h));
-  st |= dalloc((char**)&h->xa, np * d->nv * d->ne * elem(h));
-  st |= dalloc(&h->infl, np);
-  st |= dalloc(&h->status, np);
-  st |= dalloc(&h->nobsl, np);
-  st |= dalloc(&h->sweeps, np);
-  st |= dalloc(&h->counter, 1);
-  st |= dalloc(&h->defer_list, np);
-  st |= dalloc(&h->defer_count, 1);
-  st |= dalloc(&h->err_flag, 1);
-  st |= dalloc(&h->G, (size_t)(d->nlon + 1) * d->nlat);
-  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) st = LETKF_ERR_CUDA;
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->ran, cudaEventDisableTiming) != cudaSuccess) {
+    letkf_sweep_destroy(h);
+    return LETKF_ERR_CUDA;
+  }
+  cudaStream_t s = h->stream;
+  st |= dalloc(&h->pri, np, s);
+  st |= dalloc(&h->prj, np, s);
+  st |= dalloc(&h->prlev, np, s);
+  st |= dalloc(&h->prz, np, s);
+  st |= dalloc(&h->plogr, np, s);
+  st |= dalloc(&h->order, np, s);
+  st |= dalloc((char**)&h->xb, np * d->nv * d->ne * elem(h), s);
+  st |= dalloc((char**)&h->xa, np * d->nv * d->ne * elem(h), s);
+  st |= dalloc(&h->infl, np, s);
+  st |= dalloc(&h->status, np, s);
+  st |= dalloc(&h->nobsl, np, s);
+  st |= dalloc(&h->sweeps, np, s);
+  st |= dalloc(&h->counter, 1, s);
+  st |= dalloc(&h->defer_list, np, s);
+  st |= dalloc(&h->defer_count, 1, s);
+  st |= dalloc(&h->err_flag, 1, s);
+  st |= dalloc(&h->G, (size_t)(d->nlon + 1) * d->nlat, s);
   if (st != LETKF_OK) {
     letkf_sweep_destroy(h);
     return LETKF_ERR_CUDA;
   }
-  cudaMemset(h->prz, 0, np * sizeof(double));
-  cudaMemset(h->G, 0, sizeof(int) * (d->nlon + 1) * d->nlat);
-  cudaMemset(h->err_flag, 0, sizeof(int));
+  cudaMemsetAsync(h->prz, 0, np * sizeof(double), s);
+  cudaMemsetAsync(h->G, 0, sizeof(int) * (d->nlon + 1) * d->nlat, s);
+  cudaMemsetAsync(h->err_flag, 0, sizeof(int), s);
   std::vector<double> one(np, 1.0);
-  cudaMemcpy(h->infl, one.data(), np * sizeof(double), cudaMemcpyHostToDevice);
+  cudaMemcpyAsync(h->infl, one.data(), np * sizeof(double), cudaMemcpyHostToDevice, s);
+  st = cuda_status(cudaStreamSynchronize(s));
+  if (st != LETKF_OK) {
+    letkf_sweep_destroy(h);
+    return st;
+  }
   *out = h;
-  return cuda_status(cudaGetLastError());
+  return LETKF_OK;
 }
 
 int letkf_sweep_destroy(letkf_sweep_t h) {
   if (!h) return LETKF_OK;
-  if (h->stream) cudaStreamSynchronize(h->stream);
   void* ptrs[] = {h->pri,  h->prj,   h->prlev, h->prz,   h->plogr,   h->order, h->ori,     h->orj,    h->olev,
                   h->odat, h->oerr,  h->odep,  h->ocls,  h->ovarloc, h->G,     h->var_local, h->obsF,
                   h->obsA, h->meta,  h->ens32, h->ens64, h->xb,    h->xa,      h->infl,   h->status,
                   h->nobsl, h->sweeps, h->counter, h->defer_list, h->defer_count, h->err_flag};
-  for (void* p : ptrs) dfree(p);
-  if (h->stream) cudaStreamDestroy(h->stream);
+  if (h->stream) {
+    for (void* p : ptrs) dfree(p, h->stream);
+    cudaStreamSynchronize(h->stream);
+    cudaStreamDestroy(h->stream);
+  }
+  if (h->ran) cudaEventDestroy(h->ran);
   delete h;
   return LETKF_OK;
 }
@@ -262,8 +278,7 @@ int letkf_sweep_set_obs(letkf_sweep_t h, int nobs, const double* ri, const doubl
   cudaStream_t s = h->stream;
   void* old[] = {h->ori, h->orj, h->olev, h->odat, h->oerr, h->odep, h->ocls, h->ovarloc, h->var_local,
                  h->obsF, h->obsA, h->meta, h->ens32, h->ens64};
-  cudaStreamSynchronize(s);
-  for (void* p : old) dfree(p);
+  for (void* p : old) dfree(p, s);
   h->ori = h->orj = h->olev = h->odat = h->oerr = h->odep = nullptr;
   h->ocls = h->ovarloc = h->meta = nullptr;
   h->var_local = nullptr;
@@ -273,20 +288,20 @@ int letkf_sweep_set_obs(letkf_sweep_t h, int nobs, const double* ri, const doubl
   h->nobs = nobs;
   const size_t n = (size_t)nobs;
   int st = LETKF_OK;
-  st |= dalloc(&h->ori, n);
-  st |= dalloc(&h->orj, n);
-  st |= dalloc(&h->olev, n);
-  st |= dalloc(&h->odat, n);
-  st |= dalloc(&h->oerr, n);
-  st |= dalloc(&h->odep, n);
-  st |= dalloc(&h->ocls, n);
-  st |= dalloc(&h->ovarloc, n);
-  st |= dalloc(&h->obsF, n);
-  st |= dalloc(&h->obsA, n);
-  st |= dalloc(&h->meta, n);
-  if (h->d.precision == LETKF_PREC_MIXED) st |= dalloc(&h->ens32, n * ne);
-  else st |= dalloc(&h->ens64, n * ne);
-  if (var_local_row) st |= dalloc(&h->var_local, (size_t)nvarloc);
+  st |= dalloc(&h->ori, n, s);
+  st |= dalloc(&h->orj, n, s);
+  st |= dalloc(&h->olev, n, s);
+  st |= dalloc(&h->odat, n, s);
+  st |= dalloc(&h->oerr, n, s);
+  st |= dalloc(&h->odep, n, s);
+  st |= dalloc(&h->ocls, n, s);
+  st |= dalloc(&h->ovarloc, n, s);
+  st |= dalloc(&h->obsF, n, s);
+  st |= dalloc(&h->obsA, n, s);
+  st |= dalloc(&h->meta, n, s);
+  if (h->d.precision == LETKF_PREC_MIXED) st |= dalloc(&h->ens32, n * ne, s);
+  else st |= dalloc(&h->ens64, n * ne, s);
+  if (var_local_row) st |= dalloc(&h->var_local, (size_t)nvarloc, s);
   if (st != LETKF_OK) return LETKF_ERR_CUDA;
   if (var_local_row)
     cudaMemcpyAsync(h->var_local, var_local_row, sizeof(double) * nvarloc, cudaMemcpyHostToDevice, s);
@@ -301,21 +316,21 @@ int letkf_sweep_set_obs(letkf_sweep_t h, int nobs, const double* ri, const doubl
   void* t_ens;
   const size_t es = hdxf_f32 ? 4 : 8;
   const int ncell = nlon * nlat;
-  st |= dalloc(&t_ri, n);
-  st |= dalloc(&t_rj, n);
-  st |= dalloc(&t_lev, n);
-  st |= dalloc(&t_dat, n);
-  st |= dalloc(&t_err, n);
-  st |= dalloc(&t_dep, n);
-  st |= dalloc(&t_cls, n);
-  st |= dalloc(&t_vl, n);
-  st |= dalloc(&cell, n);
-  st |= dalloc(&perm, n);
-  st |= dalloc(&counts, (size_t)ncell);
-  st |= dalloc(&cursor, (size_t)ncell);
-  st |= dalloc(&start, (size_t)ncell + 1);
-  st |= dalloc(&scr, (size_t)ncell / 1024 + 2);
-  st |= dalloc((char**)&t_ens, n * ne * es);
+  st |= dalloc(&t_ri, n, s);
+  st |= dalloc(&t_rj, n, s);
+  st |= dalloc(&t_lev, n, s);
+  st |= dalloc(&t_dat, n, s);
+  st |= dalloc(&t_err, n, s);
+  st |= dalloc(&t_dep, n, s);
+  st |= dalloc(&t_cls, n, s);
+  st |= dalloc(&t_vl, n, s);
+  st |= dalloc(&cell, n, s);
+  st |= dalloc(&perm, n, s);
+  st |= dalloc(&counts, (size_t)ncell, s);
+  st |= dalloc(&cursor, (size_t)ncell, s);
+  st |= dalloc(&start, (size_t)ncell + 1, s);
+  st |= dalloc(&scr, (size_t)ncell / 1024 + 2, s);
+  st |= dalloc((char**)&t_ens, n * ne * es, s);
   if (st != LETKF_OK) return LETKF_ERR_CUDA;
   cudaMemcpyAsync(t_ri, ri, 8 * n, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(t_rj, rj, 8 * n, cudaMemcpyHostToDevice, s);
@@ -352,13 +367,12 @@ int letkf_sweep_set_obs(letkf_sweep_t h, int nobs, const double* ri, const doubl
       permute<float>(nobs, ne, perm, (const float*)t_ens, h->ens32, s);
     } else {
       float* tmp;
-      dalloc(&tmp, n * ne);
+      dalloc(&tmp, n * ne, s);
       f64_to_f32_kernel<<<(unsigned)((n * ne + 255) / 256), 256, 0, s>>>((int64_t)(n * ne), (const double*)t_ens,
                                                                          tmp);
       note_launch();
       permute<float>(nobs, ne, perm, tmp, h->ens32, s);
-      cudaStreamSynchronize(s);
-      cudaFree(tmp);
+      dfree(tmp, s);
     }
   } else {
     if (hdxf_f32) return LETKF_ERR_ARG;
@@ -366,10 +380,9 @@ int letkf_sweep_set_obs(letkf_sweep_t h, int nobs, const double* ri, const doubl
   }
   launch_sweep_prep_obs(nobs, h->ori, h->orj, h->olev, h->odat, h->oerr, h->odep, h->ocls, h->ovarloc, h->var_local,
                         h->d.params, h->obsF, h->obsA, h->meta, s);
-  cudaError_t e = cudaStreamSynchronize(s);
   void* tmpb[] = {t_ri, t_rj, t_lev, t_dat, t_err, t_dep, t_cls, t_vl, cell, perm, counts, cursor, start, scr, t_ens};
-  for (void* p : tmpb) cudaFree(p);
-  return cuda_status(e);
+  for (void* p : tmpb) dfree(p, s);
+  return cuda_status(cudaStreamSynchronize(s));
 }
 
 int letkf_sweep_set_background(letkf_sweep_t h, const void* xb, int on_device) {
@@ -427,11 +440,11 @@ static int run_f64(letkf_sweep_t h, cudaStream_t s) {
   int64_t *offs, *scr;
   double *rloc = nullptr, *rdiag = nullptr, *rows = nullptr, *dep = nullptr, *trans, *transm;
   int st = LETKF_OK;
-  st |= dalloc(&cnt, (size_t)chunk);
-  st |= dalloc(&offs, (size_t)chunk + 1);
-  st |= dalloc(&scr, (size_t)chunk / 1024 + 2);
-  st |= dalloc(&trans, (size_t)chunk * ne * ne);
-  st |= dalloc(&transm, (size_t)chunk * ne);
+  st |= dalloc(&cnt, (size_t)chunk, s);
+  st |= dalloc(&offs, (size_t)chunk + 1, s);
+  st |= dalloc(&scr, (size_t)chunk / 1024 + 2, s);
+  st |= dalloc(&trans, (size_t)chunk * ne * ne, s);
+  st |= dalloc(&transm, (size_t)chunk * ne, s);
   if (st != LETKF_OK) return LETKF_ERR_CUDA;
   size_t cap = 0;
   for (int p0 = 0; p0 < np && st == LETKF_OK; p0 += chunk) {
@@ -446,18 +459,17 @@ static int run_f64(letkf_sweep_t h, cudaStream_t s) {
     cudaStreamSynchronize(s);
     cudaMemcpyAsync(h->nobsl + p0, cnt, sizeof(int) * c, cudaMemcpyDeviceToDevice, s);
     if ((size_t)total > cap) {
-      cudaStreamSynchronize(s);
-      dfree(idx);
-      dfree(rloc);
-      dfree(rdiag);
-      dfree(rows);
-      dfree(dep);
+      dfree(idx, s);
+      dfree(rloc, s);
+      dfree(rdiag, s);
+      dfree(rows, s);
+      dfree(dep, s);
       cap = (size_t)total + (size_t)total / 4 + 1024;
-      st |= dalloc(&idx, cap);
-      st |= dalloc(&rloc, cap);
-      st |= dalloc(&rdiag, cap);
-      st |= dalloc(&rows, cap * ne);
-      st |= dalloc(&dep, cap);
+      st |= dalloc(&idx, cap, s);
+      st |= dalloc(&rloc, cap, s);
+      st |= dalloc(&rdiag, cap, s);
+      st |= dalloc(&rows, cap * ne, s);
+      st |= dalloc(&dep, cap, s);
       if (st) break;
     }
     st = launch_search_scale(h->d.nlon, h->d.nlat, h->G, nobs, h->ori, h->orj, h->olev, h->odat, h->oerr, h->ocls,
@@ -474,15 +486,31 @@ static int run_f64(letkf_sweep_t h, cudaStream_t s) {
     if (st) break;
     st = launch_update_f64_range(ne, np, p0, c, nv, (const double*)h->xb, trans, transm, (double*)h->xa, s);
   }
-  cudaStreamSynchronize(s);
   void* fr[] = {cnt, idx, offs, scr, rloc, rdiag, rows, dep, trans, transm};
-  for (void* p : fr) dfree(p);
+  for (void* p : fr) dfree(p, s);
   return st;
 }
+
+static int run_on(letkf_sweep_t h, cudaStream_t s);
 
 int letkf_sweep_run(letkf_sweep_t h, void* stream) {
   if (!h) return LETKF_ERR_ARG;
   cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+  if (s != h->stream) {
+    // the run reads what the handle's stream wrote; later calls on the
+    // handle (copies out, frees) wait for the run
+    cudaEventRecord(h->ran, h->stream);
+    cudaStreamWaitEvent(s, h->ran, 0);
+  }
+  const int st = run_on(h, s);
+  if (s != h->stream) {
+    cudaEventRecord(h->ran, s);
+    cudaStreamWaitEvent(h->stream, h->ran, 0);
+  }
+  return st;
+}
+
+static int run_on(letkf_sweep_t h, cudaStream_t s) {
   if (h->d.precision == LETKF_PREC_F64) return run_f64(h, s);
   SweepArgs a;
   memset(&a, 0, sizeof(a));
@@ -565,6 +593,26 @@ int letkf_sweep_get_diagnostics(letkf_sweep_t h, double* infl, int* nobsl, int* 
   if (sweeps) cudaMemcpy(sweeps, h->sweeps, sizeof(int) * np, cudaMemcpyDeviceToHost);
   const int st = cuda_status(cudaGetLastError());
   return st != LETKF_OK ? st : check_err(h);
+}
+
+int letkf_sweep_footprint(const letkf_sweep_desc* d, int nobs, size_t* bytes) {
+  if (!d || !bytes || nobs < 0 || d->npts < 0 || d->ne < 1 || d->nv < 1) return LETKF_ERR_ARG;
+  const size_t np = (size_t)d->npts, n = (size_t)nobs, ne = (size_t)d->ne;
+  const size_t es = d->precision == LETKF_PREC_F64 ? 8 : 4;
+  const size_t ncell = (size_t)d->nlon * d->nlat;
+  // resident: points, ensembles, per-point outputs, bucket table, sorted observations
+  size_t b = np * (6 * 8 + 4 * 5) + 2 * np * d->nv * ne * es + (ncell + d->nlat) * 4 + 64;
+  b += n * (6 * 8 + 2 * 4 + 2 * 16 + 4 + ne * es);
+  // set_obs staging (unsorted records, permutation, cell counts) while the above is live
+  size_t stage = n * (6 * 8 + 4 * 4 + ne * 8) + ncell * 16 + 64;
+  if (d->precision == LETKF_PREC_F64) {
+    // run_f64 chunk buffers with the local lists of one chunk (L <= nobs per point)
+    const size_t c = np < 16384 ? np : 16384;
+    const size_t run = c * (4 + 8 + ne * ne * 8 + ne * 8) + 4096;
+    stage = stage > run ? stage : run;
+  }
+  *bytes = b + stage;
+  return LETKF_OK;
 }
 
 int letkf_sweep_sorted_obs(letkf_sweep_t h, int* nobsgrd) {

@@ -27,7 +27,7 @@ def test_status_strings_and_version():
 
     lib = L.lib()
     assert b"sm_103a" in lib.letkf_version()
-    for code in range(7):
+    for code in range(8):
         assert lib.letkf_status_string(code)
 
 
@@ -43,4 +43,51 @@ def test_no_gpu_is_an_error_not_a_fallback():
 
     with pytest.raises(LetkfError) as e:
         letkf_core(4, 2, 2, np.ones((2, 4)), np.ones(2), np.ones(2), np.zeros(2), 1.0)
+    assert e.value.status == LETKF_ERR_NOGPU
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes mirrors of the server structs have the C layout (a probe
+    compiled by gcc against include/letkf_gpu.h prints sizes and offsets)."""
+    import os
+    import shutil
+
+    from letkf_gb300 import serve
+    from letkf_gb300.lib import HEADER
+
+    cc = shutil.which("gcc")
+    if cc is None:
+        pytest.skip("gcc not available")
+    structs = {"letkf_server_desc": serve.ServerDesc, "letkf_job_desc": serve.JobDesc,
+               "letkf_job_result": serve.JobResult, "letkf_server_stats": serve.ServerStats}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "letkf_gpu.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'  printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'  printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "probe.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "probe"
+    subprocess.run([cc, "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines():
+        c, f, v = line.split()
+        got[(c, f)] = int(v)
+    for cname, py in structs.items():
+        assert got[(cname, "sizeof")] == ctypes.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
+
+
+def test_server_without_gpu_is_an_error():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from letkf_gb300.lib import LETKF_ERR_NOGPU, LetkfError
+    from letkf_gb300.serve import Server
+
+    with pytest.raises(LetkfError) as e:
+        Server(nslots=2)
     assert e.value.status == LETKF_ERR_NOGPU

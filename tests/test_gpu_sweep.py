@@ -150,3 +150,49 @@ def test_tc_sweep_defers_points_to_the_jacobi_pass(cuda):
     spread = _spread(case["xb"].astype(np.float64))
     ok = ~neg
     assert np.abs(xa_tc[:, ok].astype(np.float64) - xa_j[:, ok]).max() < 1e-3 * spread
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_tile_handles_reproduce_the_single_domain_sweep(cuda, precision):
+    """The multi-GPU decomposition on one device: one handle per tile (its
+    points, the observations of its halo in global order) run one after the
+    other must reproduce the single-domain sweep exactly."""
+    from letkf_gb300 import shard
+    from letkf_gb300.sweep import PREC_MIXED, Sweep
+
+    case, prm, perm, grd, so, varloc, hdxf, dep = _setup(nlon=36, nlat=16, nlev=3, ne=32, nobs=3000,
+                                                         sigma_obs=5.0e3, f32=True)
+    npts = case["pri"].size
+    nlon, nlat, nlev = case["nlon"], case["nlat"], case["nlev"]
+    dt = np.float32 if precision == PREC_MIXED else np.float64
+
+    def run(pts, sel):
+        sw = Sweep(32, case["nvar"], nlon, nlat, pts.size, prm, precision=precision)
+        sw.set_points(case["pri"][pts], case["prj"][pts], case["prlev"][pts])
+        sw.set_obs(case["ri"][sel], case["rj"][sel], case["lev"][sel], case["dat"][sel], case["err"][sel],
+                   dep[sel], case["cls"][sel], hdxf[sel].astype(dt))
+        sw.set_background(case["xb"][:, pts, :].astype(dt))
+        sw.set_inflation(np.full(pts.size, 1.03))
+        sw.run()
+        out = sw.analysis(), sw.diagnostics()
+        sw.close()
+        return out
+
+    xa_all, dg_all = run(np.arange(npts), np.arange(case["ri"].size))
+    for world in (2, 3):
+        xa = np.zeros_like(xa_all)
+        infl = np.zeros(npts)
+        nobsl = np.zeros(npts, dtype=np.int64)
+        for r in range(world):
+            tile = shard.tile_of(r, world, nlon, nlat)
+            pts = shard.tile_points(tile, nlon, nlat, nlev)
+            sel = np.nonzero(shard.halo_mask(case["ri"], case["rj"], tile, nlon, nlat, prm["dlon_zero"],
+                                             prm["dlat_zero"]))[0]
+            assert sel.size < case["ri"].size
+            x, dg = run(pts, sel)
+            xa[:, pts] = x
+            infl[pts] = dg["infl"]
+            nobsl[pts] = dg["nobsl"]
+        np.testing.assert_array_equal(nobsl, dg_all["nobsl"])
+        np.testing.assert_array_equal(infl, dg_all["infl"])
+        np.testing.assert_array_equal(xa, xa_all)
