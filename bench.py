@@ -63,6 +63,11 @@ def parse():
     ap.add_argument("--tc", type=int, default=1, choices=[0, 1],
                     help="1: Gram and Newton-Schulz on the tcgen05 tensor cores (ne <= 64)")
     ap.add_argument("--tc-ns", type=int, default=None, help="tensor-core Newton-Schulz iterations before the FP32 ones")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--serve-requests", type=int, default=48, help="requests of the serving measurement")
+    ap.add_argument("--serve-slots", type=int, default=3, help="jobs on the device at once")
+    ap.add_argument("--serve-load", type=float, default=0.7,
+                    help="offered load: arrival rate x mean single-job service time")
     return ap.parse_args()
 
 
@@ -216,6 +221,80 @@ def config_block(args, wl):
             "local_obs": "0-2000 per point", "form": "mixed (FP32 ensemble, Gram and transform; FP64 mean and mean increment)",
             "l2": "inputs larger than L2 (background ensemble %.1f GB)" % (wl.npts * args.nv * args.ne * 4 / 1e9),
             "parallelism": f"dp{args.gpus} (independent domains per GPU)"}
+
+
+# ------------------------------------------------------------------ serving
+def run_serving(args, dev):
+    """Poisson stream of analysis requests over resident domains of mixed sizes
+    and ensemble sizes through the continuous-batching server: four regional
+    128x128x20 grids (2 variables, 250k clustered obs, k = 20, 32, 64, 128,
+    mixed precision) and three Lorenz-96 rings (N = 40, 1e4, 1e5; k = 20, 32,
+    64; mixed core with the FP64 update).  The arrival rate is the offered load over the mean service
+    time of a request alone.  Latency = submit -> analysis on the host."""
+    from letkf_gb300.serve import PREC_MIXED, Server
+    from letkf_gb300.workload import RegionalWorkload
+
+    specs = []
+    for i, ne in enumerate((20, 32, 64, 128)):
+        wl = RegionalWorkload(100 + i, 128, 128, 20, ne, 250_000, 2)
+        hdxf, dep, dat = wl.obs_torch(dev)  # host arrays (device evaluation)
+        xb = wl.background_torch(dev)
+        ri, rj, plev = wl.points()
+        specs.append(dict(kind="sweep", name=f"regional 128x128x20 k={ne}", domain=i, pts=(ri, rj, plev),
+                          params=wl.params, obs=dict(ri=wl.ri, rj=wl.rj, lev=wl.lev, dat=dat, err=wl.err,
+                                                     cls=wl.cls),
+                          hdxf=hdxf, dep=dep, xb=xb.cpu().numpy(), npts=wl.npts))
+        del hdxf, dep, dat, xb
+    for j, (nx, ne) in enumerate(((40, 20), (10_000, 32), (100_000, 64))):
+        rng = np.random.default_rng(200 + j)
+        xf = 8.0 + rng.standard_normal((nx, ne))
+        m = xf.sum(1) / ne
+        y = m + rng.standard_normal(nx)
+        specs.append(dict(kind="l96", name=f"lorenz96 N={nx} k={ne}", domain=10 + j, xf=xf, hdxf=xf - m[:, None],
+                          dep=y - m, cell=np.arange(1, nx + 1, dtype=np.int32), npts=nx))
+
+    def submit(srv, sp):
+        if sp["kind"] == "l96":
+            return srv.submit_l96(sp["xf"], sp["hdxf"], sp["dep"], sp["cell"], precision=PREC_MIXED,
+                                  domain=sp["domain"])
+        ri, rj, plev = sp["pts"]
+        return srv.submit_sweep(ri, rj, plev, sp["params"], 128, 128, sp["obs"], sp["hdxf"], sp["dep"], sp["xb"],
+                                precision=PREC_MIXED, domain=sp["domain"])
+
+    with Server(nslots=args.serve_slots) as srv:
+        alone = []
+        for sp in specs:  # each domain once, alone: service time, and the domain becomes resident
+            t0 = time.perf_counter()
+            srv.wait(submit(srv, sp))
+            alone.append(time.perf_counter() - t0)
+        mean_service = statistics.mean(alone)
+        rate = args.serve_load / mean_service
+        rng = np.random.default_rng(7)
+        gaps = rng.exponential(1.0 / rate, args.serve_requests)
+        picks = rng.integers(0, len(specs), args.serve_requests)
+        jobs = []
+        t0 = time.perf_counter()
+        t_next = 0.0
+        for g, k in zip(gaps, picks):
+            t_next += g
+            dt = t0 + t_next - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            jobs.append((k, submit(srv, specs[k])))
+        for _, j in jobs:
+            srv.wait(j)
+            j.xa = None
+        st = srv.stats()
+    lat = np.array([j.result["latency_s"] for _, j in jobs])
+    span = max(j.result["t_done"] for _, j in jobs) - min(j.result["t_submit"] for _, j in jobs)
+    points = sum(specs[k]["npts"] for k, _ in jobs)
+    return {"requests": int(args.serve_requests), "slots": int(args.serve_slots), "offered_load": args.serve_load,
+            "arrival_rate_hz": rate, "p50_latency_ms": float(np.percentile(lat, 50) * 1e3),
+            "p99_latency_ms": float(np.percentile(lat, 99) * 1e3), "points_per_s": points / span,
+            "jobs_per_s": len(jobs) / span,
+            "service_alone_ms": {sp["name"]: round(a * 1e3, 2) for sp, a in zip(specs, alone)},
+            "resident_domains": int(st["resident_domains"]), "peak_device_bytes": int(st["peak_bytes"]),
+            "host_buffers": "pageable numpy arrays (copied in the timed latency)"}
 
 
 # ----------------------------------------------------------------- GPU arm
@@ -378,6 +457,8 @@ def run_gpu(args, rank, world, dist):
     out["fp64_plain"] = {"value": v64, "unit": UNIT, "sample": f"every {args.fp64_stride}th point ({sub.size} points)",
                          "mixed_over_fp64": (value / world) / v64}
     s64.close()
+    if not args.no_serving:
+        out["serving"] = run_serving(args, dev)
     return out, sw
 
 
