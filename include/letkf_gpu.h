@@ -87,6 +87,35 @@ int letkf_core_batch_mixed(int ne, int npts, const int64_t* offs, const float* r
 int letkf_update_f64(int ne, int npts, int nv, const double* xb, const double* trans,
                      const double* transm, double* xa, void* stream);
 
+/* Relaxed update of the SCALE driver (scale/letkf/letkf_tools.f90:215-268),
+ * per point p and variable v:
+ *   mode 1 RTPP  W' = (1 - alpha) W + alpha I                  (:1224-1237)
+ *   mode 2 RTPS  W' = infl W, infl = alpha sqrt(var_g / (var_a (ne-1)))
+ *                - alpha + 1 with var_g = xb'.xb', var_a = xb' Pa xb'  (:1240-1268)
+ *   T = (W' + transm 1^T) beta + (1 - beta) I;  beta == 0: xa = mean + xb'
+ *   q_sprd_max > 0: the relative spread of variable q_var is clipped to it.
+ * beta[nv][npts] may be NULL (1); pao is required for RTPS; rtps_infl[nv][npts]
+ * may be NULL.  Mode 0 with beta = 1 equals letkf_update_f64 bit for bit. */
+typedef struct letkf_relax_desc {
+  int mode;              /* 0 none, 1 RTPP, 2 RTPS */
+  double alpha;          /* RELAX_ALPHA or RELAX_ALPHA_SPREAD */
+  const double* beta;    /* device [nv][npts] or NULL */
+  int q_var;             /* variable index of the spread clip, -1 none */
+  double q_sprd_max;     /* Q_SPRD_MAX, <= 0 off */
+} letkf_relax_desc;
+int letkf_update_relax_f64(int ne, int npts, int nv, const double* xb, const double* trans,
+                           const double* transm, const double* pao, const letkf_relax_desc* relax,
+                           double* xa, double* rtps_infl, void* stream);
+
+/* relax_beta (scale/letkf/letkf_tools.f90:1182-1220) for every point and
+ * variable: 0 for variables q_lo..q_hi where rlev < q_update_top, the
+ * boundary-buffer ramp min(dist_bdy, 1) (clipped at 0) when
+ * boundary_buffer_width > 0, else 1.  beta[nv][npts] on the device. */
+int letkf_relax_beta(int npts, int nv, const double* ri, const double* rj, const double* rlev,
+                     int q_lo, int q_hi, double q_update_top, double boundary_buffer_width,
+                     double dx, double dy, int nlong, int nlatg, int ihalo, int jhalo,
+                     double* beta, void* stream);
+
 /* ------------------------------------------------------------------------
  * Local observation search on DEVICE buffers.  Each search writes, per grid
  * point, the selected observations in the reference's order:

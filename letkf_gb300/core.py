@@ -117,6 +117,46 @@ def update_f64(xb, trans, transm=None, stream=None):
     return xa
 
 
+class RelaxDesc(C.Structure):
+    _fields_ = [("mode", C.c_int), ("alpha", C.c_double), ("beta", C.c_void_p), ("q_var", C.c_int),
+                ("q_sprd_max", C.c_double)]
+
+
+RELAX_NONE, RELAX_RTPP, RELAX_RTPS = 0, 1, 2
+
+
+def update_relax_f64(xb, trans, transm=None, pao=None, mode=RELAX_NONE, alpha=0.0, beta=None, q_var=-1,
+                     q_sprd_max=0.0, stream=None):
+    """Relaxed update (scale/letkf/letkf_tools.f90:215-268): RTPP / RTPS,
+    relax_beta weights and the q spread clip.  xb float64 [nv, npts, ne];
+    trans / pao [npts, ne, ne] column-major per point; beta [nv, npts] or
+    None.  Returns (xa, rtps_infl [nv, npts] or None)."""
+    import torch
+
+    nv, npts, ne = xb.shape
+    xa = torch.empty_like(xb)
+    infl = torch.empty((nv, npts), dtype=torch.float64, device=xb.device) if mode == RELAX_RTPS else None
+    rd = RelaxDesc(int(mode), float(alpha), None if beta is None else beta.data_ptr(), int(q_var), float(q_sprd_max))
+    st = lib().letkf_update_relax_f64(ne, npts, nv, _dptr(xb), _dptr(trans), _dptr(transm), _dptr(pao),
+                                      C.byref(rd), _dptr(xa), _dptr(infl), _stream(stream))
+    check(st, "letkf_update_relax_f64")
+    return xa, infl
+
+
+def relax_beta(ri, rj, rlev, nv, q_lo=-1, q_hi=-2, q_update_top=0.0, boundary_buffer_width=0.0, dx=1.0, dy=1.0,
+               nlong=1, nlatg=1, ihalo=0, jhalo=0, stream=None):
+    """relax_beta (scale/letkf/letkf_tools.f90:1182-1220) for every point and
+    variable (0-based variable indices q_lo..q_hi); returns beta [nv, npts]."""
+    import torch
+
+    npts = ri.numel()
+    beta = torch.empty((nv, npts), dtype=torch.float64, device=ri.device)
+    check(lib().letkf_relax_beta(npts, nv, _dptr(ri), _dptr(rj), _dptr(rlev), int(q_lo), int(q_hi),
+                                 float(q_update_top), float(boundary_buffer_width), float(dx), float(dy), int(nlong),
+                                 int(nlatg), int(ihalo), int(jhalo), _dptr(beta), _stream(stream)), "relax_beta")
+    return beta
+
+
 def exclusive_scan(counts, stream=None):
     import torch
 
@@ -255,4 +295,5 @@ def search_l96(nx, obs_cell, pix, xlocal=3.0, obserr=1.0, tdif=0.0, tlocal=-1.0,
 
 
 __all__ = ["letkf_core", "core_batch_f64", "core_batch_mixed", "update_f64", "exclusive_scan", "gather_rows",
-           "search_scale", "search_speedy", "search_l96", "l96_obs_cell", "obs_departure", "LETKF_OK"]
+           "search_scale", "search_speedy", "search_l96", "l96_obs_cell", "obs_departure", "update_relax_f64", "relax_beta", "RELAX_NONE", "RELAX_RTPP",
+           "RELAX_RTPS", "LETKF_OK"]

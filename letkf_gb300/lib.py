@@ -56,6 +56,8 @@ _SIGS = {
     "letkf_search_l96": (_i, [_i, _i, _vp, _i, _vp, _d, _d, _d, _d, _vp, _vp, _vp, _vp, _vp, _vp]),
     "letkf_l96_obs_cell": (_i, [_i, _i, _vp, _vp, _vp]),
     "letkf_obs_departure": (_i, [_i, _i, _vp, _vp, _vp, _d, _vp, _vp, _vp, _vp, _vp]),
+    "letkf_update_relax_f64": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "letkf_relax_beta": (_i, [_i, _i, _vp, _vp, _vp, _i, _i, _d, _d, _d, _d, _i, _i, _i, _i, _vp, _vp]),
 }
 
 
