@@ -145,8 +145,8 @@ def algorithmic_bytes(npts, nv, ne, nobs):
     return float(npts * nv * ne * 8 + nobs * ne * 4 + nobs * 48 + npts * nv * 8)
 
 
-def load_traffic():
-    p = os.path.join(ROOT, "profiles", "sweep_mixed_traffic.json")
+def load_traffic(kernel):
+    p = os.path.join(ROOT, "profiles", f"{kernel.split('<')[0]}_traffic.json")
     try:
         with open(p) as f:
             return json.load(f)
@@ -351,16 +351,18 @@ def run_gpu(args, rank, world, dist):
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded smooth random fields, clustered obs)",
            "config": config_block(args, wl), "gpu_launches": int(launches), "clocks": clk.summary()}
-    # roofline of the dominant (only) kernel: sweep_mixed_kernel
+    # roofline of the dominant kernel (the deferred-point pass is < 0.01 % of the step)
+    tc_on = bool(args.tc and args.ne <= 64 and args.eig == "newton-schulz")
+    kernel = "sweep_tc_kernel" if tc_on else f"sweep_mixed_kernel<{64 if args.ne <= 64 else 128}>"
     peaks, src = measured_peaks()
     flops = algorithmic_flops(nobsl, args.ne, args.nv)
     ach = flops / (t / args.steps) / 1e12
     pk = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
-    trf = load_traffic()
+    trf = load_traffic(kernel)
     traffic = None
     if trf and trf.get("per_point_bytes"):
         traffic = trf["per_point_bytes"] * wl.npts
-    out["roofline"] = {"bound": "tensor", "kernel": "sweep_mixed_kernel", "achieved": ach, "peak": pk,
+    out["roofline"] = {"bound": "tensor", "kernel": kernel, "achieved": ach, "peak": pk,
                        "unit": "TFLOP/s", "frac": ach / pk, "traffic": traffic,
                        "peak_source": f"bf16 dense sustained ({src})",
                        "algorithmic_flops_per_launch": flops,
