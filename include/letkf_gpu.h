@@ -76,6 +76,25 @@ int letkf_core_batch_mixed(int ne, int npts, const int64_t* offs, const float* r
                            double* parm_infl, float* trans, float* transm, int rdiag_wloc,
                            double minfl, int* status, void* stream);
 
+/* Large-ensemble core (ne up to LETKF_LARGEK_MAX_NE): same arguments, layout and
+ * semantics as letkf_core_batch_mixed, for ensembles whose ne x ne matrices
+ * live in HBM.  Gram and the Newton-Schulz products of A^(-1/2) run on the
+ * tensor cores with three-term TF32 splits; W = sqrt((ne-1)/s) Z, wbar = Pa
+ * Ywᵀ dep.  Points with c <= 0 or tr(G) >= 1e6 c (where mtx_eigen's
+ * truncation could act) get status LETKF_ERR_CAPACITY and an identity
+ * transform; a transform that does not converge gets LETKF_ERR_EIG. */
+#define LETKF_LARGEK_MAX_NE 1024
+int letkf_core_batch_largek(int ne, int npts, const int64_t* offs, const float* rows,
+                            const float* rdiag, const float* rloc, const float* dep,
+                            double* parm_infl, float* trans, float* transm, int rdiag_wloc,
+                            double minfl, int* status, void* stream);
+
+/* FP32 ensemble update for any ne <= 512: xb, xa [nv][npts][ne] float32,
+ * trans [npts][ne*ne] column-major, transm [npts][ne] or NULL; FP32 products,
+ * FP64 mean and mean increment (nv <= 8). */
+int letkf_update_mixed(int ne, int npts, int nv, const float* xb, const float* trans,
+                       const float* transm, float* xa, void* stream);
+
 /* ------------------------------------------------------------------------
  * Ensemble update on DEVICE buffers (speedy/letkf/letkf_tools.f90:164-170;
  * scale/letkf/letkf_tools.f90:237-251 with beta = 1):
@@ -95,7 +114,8 @@ int letkf_update_f64(int ne, int npts, int nv, const double* xb, const double* t
  *   T = (W' + transm 1^T) beta + (1 - beta) I;  beta == 0: xa = mean + xb'
  *   q_sprd_max > 0: the relative spread of variable q_var is clipped to it.
  * beta[nv][npts] may be NULL (1); pao is required for RTPS; rtps_infl[nv][npts]
- * may be NULL.  Mode 0 with beta = 1 equals letkf_update_f64 bit for bit. */
+ * may be NULL (1 where beta == 0, which skips the relaxation).  Mode 0 with
+ * beta = 1 equals letkf_update_f64 bit for bit. */
 typedef struct letkf_relax_desc {
   int mode;              /* 0 none, 1 RTPP, 2 RTPS */
   double alpha;          /* RELAX_ALPHA or RELAX_ALPHA_SPREAD */

@@ -105,6 +105,37 @@ def core_batch_mixed(ne, offs, rows, rdiag, rloc, dep, parm_infl, want_transm=Fa
     return dict(trans=trans, transm=tm, status=status, parm_infl=parm_infl)
 
 
+def core_batch_largek(ne, offs, rows, rdiag, rloc, dep, parm_infl, want_transm=False, rdiag_wloc=False, minfl=0.0,
+                      stream=None):
+    """Large-ensemble batched core (ne up to 1024; tensor-core Gram and
+    Newton-Schulz): float32 rows / rdiag / rloc / dep, float64 parm_infl (in
+    place).  Returns dict of tensors (float32 trans, transm, int32 status)."""
+    import torch
+
+    npts = offs.numel() - 1
+    dev = rows.device
+    trans = torch.empty((npts, ne, ne), dtype=torch.float32, device=dev)
+    tm = torch.empty((npts, ne), dtype=torch.float32, device=dev) if want_transm else None
+    status = torch.empty(npts, dtype=torch.int32, device=dev)
+    st = lib().letkf_core_batch_largek(ne, npts, _dptr(offs), _dptr(rows), _dptr(rdiag), _dptr(rloc), _dptr(dep),
+                                       _dptr(parm_infl), _dptr(trans), _dptr(tm), int(bool(rdiag_wloc)),
+                                       float(minfl), _dptr(status), _stream(stream))
+    check(st, "letkf_core_batch_largek")
+    return dict(trans=trans, transm=tm, status=status, parm_infl=parm_infl)
+
+
+def update_mixed(xb, trans, transm=None, stream=None):
+    """FP32 update for any ne <= 512: xb float32 [nv, npts, ne], trans float32
+    [npts, ne, ne] column-major per point; returns xa like xb."""
+    import torch
+
+    nv, npts, ne = xb.shape
+    xa = torch.empty_like(xb)
+    check(lib().letkf_update_mixed(ne, npts, nv, _dptr(xb), _dptr(trans), _dptr(transm), _dptr(xa),
+                                   _stream(stream)), "letkf_update_mixed")
+    return xa
+
+
 def update_f64(xb, trans, transm=None, stream=None):
     """xb float64 [nv, npts, ne] full members; trans [npts, ne, ne] (column-
     major per point); returns xa like xb."""
@@ -295,5 +326,5 @@ def search_l96(nx, obs_cell, pix, xlocal=3.0, obserr=1.0, tdif=0.0, tlocal=-1.0,
 
 
 __all__ = ["letkf_core", "core_batch_f64", "core_batch_mixed", "update_f64", "exclusive_scan", "gather_rows",
-           "search_scale", "search_speedy", "search_l96", "l96_obs_cell", "obs_departure", "update_relax_f64", "relax_beta", "RELAX_NONE", "RELAX_RTPP",
+           "search_scale", "search_speedy", "search_l96", "l96_obs_cell", "obs_departure", "update_relax_f64", "relax_beta", "core_batch_largek", "update_mixed", "RELAX_NONE", "RELAX_RTPP",
            "RELAX_RTPS", "LETKF_OK"]

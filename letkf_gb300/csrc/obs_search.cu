@@ -238,6 +238,16 @@ __global__ void search_speedy_kernel(SpeedyCtx c, int npts, const double* __rest
   if (!idx) nobsl[p] = cnt;
 }
 
+// one thread per point: CTAs small enough that the grid covers the SMs twice
+static int search_block(int npts) {
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (npts >= 2 * nsm * 128) return 128;
+  if (npts >= 2 * nsm * 64) return 64;
+  return 32;
+}
+
 int launch_search_scale(int nlon, int nlat, const int* G, int nobs, const double* ori, const double* orj,
                         const double* olev, const double* odat, const double* oerr, const int* ocls,
                         const int* ovarloc, int npts, const double* pri, const double* prj, const double* prlev,
@@ -247,7 +257,7 @@ int launch_search_scale(int nlon, int nlat, const int* G, int nobs, const double
   ScaleParams P;
   double* f = &P.dx;
   for (int i = 0; i < 15; i++) f[i] = params[i];
-  const int bs = 128;
+  const int bs = search_block(npts);
   search_scale_kernel<<<(npts + bs - 1) / bs, bs, 0, stream>>>(nlon, nlat, G, nobs, ori, orj, olev, odat, oerr,
                                                                  ocls, ovarloc, npts, pri, prj, prlev, prz,
                                                                  var_local, P, offs, nobsl, idx, rloc, rdiag);
@@ -280,7 +290,7 @@ int launch_search_speedy(int nlon, int nlat, const double* lon, const double* la
   c.sigma_obs = params[3];
   c.sigma_obsv = params[4];
   (void)nobs;
-  const int bs = 128;
+  const int bs = search_block(npts);
   search_speedy_kernel<<<(npts + bs - 1) / bs, bs, 0, stream>>>(c, npts, plon, plat, pdlon, pilev, plogp, params[2],
                                                                   offs, nobsl, idx, rloc, rdiag);
   note_launch();

@@ -135,19 +135,30 @@ __global__ void __launch_bounds__(UPD_NT) update_relax_f64_kernel(int n, int npt
     __syncthreads();
     for (int t = tid; t < nv * n; t += UPD_NT) xp[t] = xp[t] - mean[t / n];
     __syncthreads();
-    for (int v = tid; v < nv; v += UPD_NT) {
-      double f = 1.0;
-      if (r.mode == 2) {
-        const double* x = xp + v * n;
-        double var_g = 0.0, var_a = 0.0;
-        for (int m = 0; m < n; m++) {
-          var_g = var_g + x[m] * x[m];
-          for (int k = 0; k < n; k++) var_a = var_a + x[k] * Pa[(size_t)m * n + k] * x[m];
+    // RTPS factor, one warp per variable: lanes split k so the Pa(k, m) reads of
+    // a column are consecutive; beta == 0 skips weight_RTPS (factor 1)
+    {
+      const int lane = tid & 31;
+      for (int v = tid >> 5; v < nv; v += UPD_NT / 32) {
+        double f = 1.0;
+        if (r.mode == 2 && bet[v] != 0.0) {
+          const double* x = xp + v * n;
+          double var_a = 0.0, var_g = 0.0;
+          for (int m = 0; m < n; m++) {
+            double part = 0.0;
+            for (int k = lane; k < n; k += 32) part = part + x[k] * Pa[(size_t)m * n + k];
+            var_a = var_a + part * x[m];
+          }
+          for (int m = lane; m < n; m += 32) var_g = var_g + x[m] * x[m];
+          var_a = warp_sum(var_a);
+          var_g = warp_sum(var_g);
+          if (var_g > 0.0 && var_a > 0.0) f = r.alpha * sqrt(var_g / (var_a * (double)(n - 1))) - r.alpha + 1.0;
         }
-        f = (var_g > 0.0 && var_a > 0.0) ? r.alpha * sqrt(var_g / (var_a * (double)(n - 1))) - r.alpha + 1.0 : 1.0;
-        if (r.rtps_infl) r.rtps_infl[(size_t)v * npts + p] = f;
+        if (lane == 0) {
+          if (r.mode == 2 && r.rtps_infl) r.rtps_infl[(size_t)v * npts + p] = f;
+          fac[v] = f;
+        }
       }
-      fac[v] = f;
     }
     __syncthreads();
     for (int t = tid; t < nv * n; t += UPD_NT) {

@@ -19,6 +19,7 @@ LETKF_ERR_CAPACITY = 4
 LETKF_ERR_NOGPU = 5
 LETKF_ERR_TIMEOUT = 6
 LETKF_MAX_NE = 128
+LETKF_LARGEK_MAX_NE = 1024
 
 HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "letkf_gpu.h")
 
@@ -56,6 +57,8 @@ _SIGS = {
     "letkf_search_l96": (_i, [_i, _i, _vp, _i, _vp, _d, _d, _d, _d, _vp, _vp, _vp, _vp, _vp, _vp]),
     "letkf_l96_obs_cell": (_i, [_i, _i, _vp, _vp, _vp]),
     "letkf_obs_departure": (_i, [_i, _i, _vp, _vp, _vp, _d, _vp, _vp, _vp, _vp, _vp]),
+    "letkf_core_batch_largek": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _d, _vp, _vp]),
+    "letkf_update_mixed": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
     "letkf_update_relax_f64": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "letkf_relax_beta": (_i, [_i, _i, _vp, _vp, _vp, _i, _i, _d, _d, _d, _d, _i, _i, _i, _i, _vp, _vp]),
 }

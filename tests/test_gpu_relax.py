@@ -85,7 +85,7 @@ def test_relaxed_update_matches_reference(cuda, ne, mode, alpha):
     beta = rng.uniform(0, 1, (nv, npts))
     beta[:, ::5] = 1.0
     beta[:, 1::7] = 0.0
-    q_max = 0.05
+    q_max = 0.02
     t = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=cuda)
     xa, infl = update_relax_f64(t(xb), t(ref["trans"]), t(ref["transm"]), t(ref["pao"]), mode=mode, alpha=alpha,
                                 beta=t(beta), q_var=2, q_sprd_max=q_max)
