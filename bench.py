@@ -64,6 +64,8 @@ def parse():
                     help="1: Gram and Newton-Schulz on the tcgen05 tensor cores (ne <= 64)")
     ap.add_argument("--tc-ns", type=int, default=None, help="tensor-core Newton-Schulz iterations before the FP32 ones")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--no-largek", action="store_true", help="skip the large-ensemble measurement")
+    ap.add_argument("--largek-points", type=int, default=4096, help="sampled points of the large-ensemble sweep")
     ap.add_argument("--serve-requests", type=int, default=48, help="requests of the serving measurement")
     ap.add_argument("--serve-slots", type=int, default=3, help="jobs on the device at once")
     ap.add_argument("--serve-load", type=float, default=0.7,
@@ -297,6 +299,83 @@ def run_serving(args, dev):
             "host_buffers": "pageable numpy arrays (copied in the timed latency)"}
 
 
+# --------------------------------------------------------------- large k
+def run_largek(args, dev):
+    """Large-ensemble configuration on a sample of its points: 360x181x32
+    global grid, 6 variables, k = 512, 3e6 observations, SPEEDY lat/lon
+    search.  One step = search (count + fill), gather of the local rows, the
+    large-k core and the FP32 update of the 6 variables for the sampled
+    points; plus the analysis error of a few points against the FP64 oracle.
+    sigma_h = 60 km keeps the local counts in the O(1e2-1e3) range."""
+    import torch
+
+    from letkf_gb300.core import core_batch_largek, gather_rows, search_speedy, update_mixed
+    from letkf_gb300.workload import GlobalWorkload
+
+    wl = GlobalWorkload(21)
+    hdxf, dep, dat = wl.obs_torch(dev)
+    rng = np.random.default_rng(5)
+    idx = np.sort(rng.choice(wl.npts, args.largek_points, replace=False))
+    lon, lat, dlon, ilev, lnp = wl.points(idx)
+    f = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
+    grid = {"lon": f(wl.lon), "lat": f(wl.lat), "nobsgrd": torch.as_tensor(wl.nobsgrd, dtype=torch.int32, device=dev)}
+    obs = {"elm": f(wl.elm), "lon": f(wl.olon), "lat": f(wl.olat), "lev": f(wl.olev), "dat": dat, "err": f(wl.err)}
+    pts = {"lon": f(lon), "lat": f(lat), "dlon_zero": f(dlon), "ilev": torch.as_tensor(ilev, device=dev),
+           "logpfm": f(lnp)}
+    xb = wl.background_torch(dev, idx)
+    vl = np.ones(7)
+    infl0 = torch.full((idx.size,), 1.05, dtype=torch.float64, device=dev)
+
+    def step():
+        offs, oi, rloc, rdiag = search_speedy(grid, obs, pts, wl.params, vl)
+        rows, dl = gather_rows(oi, hdxf, dep.to(torch.float32))
+        infl = infl0.clone()
+        out = core_batch_largek(wl.ne, offs, rows, rdiag.to(torch.float32), rloc.to(torch.float32), dl, infl,
+                                want_transm=True)
+        xa = update_mixed(xb, out["trans"], out["transm"])
+        return offs, oi, rloc, rdiag, rows, dl, out, xa
+
+    step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    offs, oi, rloc, rdiag, rows, dl, out, xa = step()
+    e1.record()
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3
+    nl = np.diff(offs.cpu().numpy())
+    status = out["status"].cpu().numpy()
+    # FP64 oracle on a few points (the same float32 rows and weights)
+    from oracle import oracle as O
+
+    sub = np.arange(0, idx.size, max(1, idx.size // 6))[:6]
+    o = offs.cpu().numpy()
+    R = rows.double().cpu().numpy()
+    rd_, rl_, d_ = (x.double().cpu().numpy() for x in (rdiag.to(torch.float32), rloc.to(torch.float32), dl))
+    so = np.concatenate([[0], np.cumsum(nl[sub])]).astype(np.int64)
+    sel = np.concatenate([np.arange(o[p], o[p + 1]) for p in sub]) if nl[sub].sum() else np.zeros(0, np.int64)
+    ref = O.letkf_core_batch(wl.ne, so, R[sel] if sel.size else np.zeros((1, wl.ne)), rd_[sel] if sel.size else
+                             np.ones(1), rl_[sel] if sel.size else np.ones(1), d_[sel] if sel.size else np.zeros(1),
+                             np.full(sub.size, 1.05), want_transm=True)
+    x64 = xb[:, sub, :].double().cpu().numpy()
+    xp = x64 - x64.mean(-1, keepdims=True)
+    want = x64.mean(-1, keepdims=True) + np.einsum("vpk,pmk->vpm", xp, ref["trans"] + ref["transm"][:, None, :])
+    got = xa[:, sub, :].double().cpu().numpy()
+    spread = np.sqrt((xp ** 2).sum(-1) / (wl.ne - 1)).mean()
+    em = float(np.sqrt(np.mean((got.mean(-1) - want.mean(-1)) ** 2)) / spread)
+    pert = lambda x: x - x.mean(-1, keepdims=True)
+    ep = float(np.sqrt(np.mean((pert(got) - pert(want)) ** 2)) / spread)
+    return {"workload": f"global {wl.nlon}x{wl.nlat}x{wl.nlev}, {wl.nvar} vars, k={wl.ne}, {wl.nobs} obs, "
+                        f"sigma_h={wl.sigma_obs:.0f} m, sigma_v={wl.sigma_obsv} ln p (SPEEDY lat/lon search)",
+            "sample_points": int(idx.size), "value": idx.size / t, "unit": UNIT, "ms_per_sample": t * 1e3,
+            "step": "search + gather + large-k core (tensor-core Gram and Newton-Schulz) + FP32 update, CUDA events",
+            "local_obs": {"min": int(nl.min()), "mean": float(nl.mean()), "p50": float(np.median(nl)),
+                          "max": int(nl.max())},
+            "status_ok": int((status == 0).sum()),
+            "error_vs_fp64_oracle": {"analysis_mean_rms_over_spread": em, "perturbation_rms_over_spread": ep,
+                                     "points": int(sub.size), "target": 1e-4}}
+
+
 # ----------------------------------------------------------------- GPU arm
 def run_gpu(args, rank, world, dist):
     import torch
@@ -461,6 +540,8 @@ def run_gpu(args, rank, world, dist):
     s64.close()
     if not args.no_serving:
         out["serving"] = run_serving(args, dev)
+    if not args.no_largek:
+        out["large_k"] = run_largek(args, dev)
     return out, sw
 
 

@@ -13,6 +13,8 @@ where the kernel streams the ensemble):
   l96           Lorenz-96 ring of 100,000 variables, k = 32: departures,
                 selection, mixed core, update
   relax         RTPS update with relax_beta weights of 50,000 points, k = 64
+  largek        large-ensemble core of 512 points, k = 512, 100-900 local obs
+                each, and the FP32 update of 6 variables
 Used for the ncu summaries under profiles/; prints one line per case.
 """
 from __future__ import annotations
@@ -115,8 +117,35 @@ def case_relax(dev):
     return f"{npts} points, {(time.perf_counter() - t0) * 1e3:.1f} ms"
 
 
+def case_largek(dev):
+    import torch
+
+    from .core import core_batch_largek, update_mixed
+
+    rng = np.random.default_rng(6)
+    ne, npts = 512, 512
+    Ls = rng.integers(100, 900, npts)
+    offs = torch.as_tensor(np.concatenate([[0], np.cumsum(Ls)]), dtype=torch.int64, device=dev)
+    n = int(Ls.sum())
+    rows = torch.randn((n, ne), device=dev)
+    rows -= rows.mean(1, keepdim=True)
+    rd = torch.rand(n, device=dev) * 2.7 + 0.3
+    rl = torch.rand(n, device=dev) * 0.99 + 0.01
+    dep = torch.randn(n, device=dev)
+    infl = torch.full((npts,), 1.1, dtype=torch.float64, device=dev)
+    xb = torch.randn((6, npts, ne), device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = core_batch_largek(ne, offs, rows, rd, rl, dep, infl, want_transm=True)
+    update_mixed(xb, out["trans"], out["transm"])
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    ok = int((out["status"] == 0).sum())
+    return f"{npts} points (k = {ne}, mean L = {Ls.mean():.0f}), {dt * 1e3:.1f} ms, {npts / dt:.0f} points/s, {ok} ok"
+
+
 CASES = {"sweep_tc": lambda d: case_sweep(d, True), "sweep_simt": lambda d: case_sweep(d, False),
-         "f64": case_f64, "l96": case_l96, "relax": case_relax}
+         "f64": case_f64, "l96": case_l96, "relax": case_relax, "largek": case_largek}
 
 
 def main():

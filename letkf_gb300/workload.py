@@ -115,3 +115,101 @@ class RegionalWorkload:
 
     def local_count_hint(self):
         return "0-2000 local obs per point (clustered density, sigma_h = %.0f m)" % self.sigma_obs
+
+
+class GlobalWorkload:
+    """The large-ensemble configuration: a 360 x 181 x 32 global lat/lon grid
+    (1 degree, poles included, pressure levels uniform in ln p from 1000 to
+    10 hPa), 6 variables, k = 512 members, 3e6 observations (u, v, t, q at
+    positions uniform on the sphere and pressures uniform in ln p) searched
+    with the SPEEDY lat/lon rule (speedy/letkf/letkf_tools.f90:272-603).
+    Members and truth are smooth random fields on the sphere x ln p evaluated
+    on the device; the obs are bucket-sorted (speedy/letkf/letkf_obs.f90:
+    243-313).  Point p = lev * nlon * nlat + j * nlon + i."""
+
+    def __init__(self, seed=0, nlon=360, nlat=181, nlev=32, ne=512, nobs=3_000_000, nvar=6, sigma_obs=60.0e3,
+                 sigma_obsv=0.4):
+        from .drivers import speedy_sort_obs
+
+        rng = np.random.default_rng(seed)
+        self.nlon, self.nlat, self.nlev, self.ne, self.nvar = nlon, nlat, nlev, ne, nvar
+        self.lon = 360.0 / nlon * np.arange(nlon)
+        self.lat = np.linspace(-90.0, 90.0, nlat)
+        self.plev = np.exp(np.linspace(math.log(1.0e5), math.log(1.0e3), nlev))
+        olon = rng.uniform(0.0, 360.0, nobs)
+        olat = np.degrees(np.arcsin(rng.uniform(-1.0, 1.0, nobs)))
+        olev = np.exp(rng.uniform(math.log(1.0e3), math.log(1.0e5), nobs))
+        ovar = rng.integers(0, 4, nobs)
+        elm = np.array([S.ID_U, S.ID_V, S.ID_T, S.ID_Q], dtype=np.float64)[ovar]
+        err = np.array([1.0, 1.0, 1.0, 1.0e-3])[ovar]
+        noise = rng.standard_normal(nobs)
+        perm, self.nobsgrd = speedy_sort_obs(self.lon, self.lat, olon, olat)
+        self.olon, self.olat, self.olev, self.elm, self.err = olon[perm], olat[perm], olev[perm], elm[perm], err[perm]
+        self.ovar, self.noise = ovar[perm], noise[perm]
+        self.nobs = perm.size
+        amp = np.array([5.0, 5.0, 2.0, 1.0e-3, 3.0, 3.0])[:nvar] if nvar <= 6 else None
+        self.fields = S.SmoothFields(rng, ne + 1, nvar, 6, wavenum_scale=6371.3e3 / 2.0e6, dims=4, amp=amp)
+        self.sigma_obs, self.sigma_obsv = sigma_obs, sigma_obsv
+        dist_zero = sigma_obs * math.sqrt(10.0 / 3.0) * 2.0
+        dist_zerov = sigma_obsv * math.sqrt(10.0 / 3.0) * 2.0
+        dlat_zero = dist_zero / 3.1415926535 / 6371.3e3 * 180.0   # speedy/letkf/letkf_obs.f90:82-88
+        self.params = (dist_zero, dist_zerov, dlat_zero, sigma_obs, sigma_obsv)
+        self.npts = nlon * nlat * nlev
+
+    @staticmethod
+    def _xyz(lon, lat, lnp):
+        lo, la = np.radians(lon), np.radians(lat)
+        return np.stack([np.cos(la) * np.cos(lo), np.cos(la) * np.sin(lo), np.sin(la), (lnp - math.log(1.0e5)) / 2.0],
+                        -1)
+
+    def obs_torch(self, device, chunk=20_000):
+        """hdxf float32 [nobs, ne], dep float64 [nobs], dat float64 (sorted order), on the device."""
+        import torch
+
+        ne = self.ne
+        xyz = torch.as_tensor(self._xyz(self.olon, self.olat, np.log(self.olev)), device=device)
+        var = torch.as_tensor(self.ovar, device=device)
+        k = torch.as_tensor(self.fields.k, device=device)
+        a = torch.as_tensor(self.fields.a, device=device)
+        ph = torch.as_tensor(self.fields.phi, device=device)
+        hdxf = torch.empty((self.nobs, ne), dtype=torch.float32, device=device)
+        dep = torch.empty(self.nobs, dtype=torch.float64, device=device)
+        dat = torch.empty(self.nobs, dtype=torch.float64, device=device)
+        err = torch.as_tensor(self.err, device=device)
+        noise = torch.as_tensor(self.noise, device=device)
+        for c in range(0, self.nobs, chunk):
+            s = slice(c, min(self.nobs, c + chunk))
+            arg = torch.einsum("nqd,nd->nq", k[var[s]], xyz[s])
+            hx = (a[:, var[s], :] * torch.cos(arg[None] + ph[:, var[s], :])).sum(-1)  # (ne+1, n)
+            hx32 = hx[:ne].to(torch.float32).to(torch.float64)
+            m = hx32.sum(0) / ne
+            hdxf[s] = (hx32 - m).T.to(torch.float32)
+            y = hx[ne] + err[s] * noise[s]
+            dep[s] = y - m
+            dat[s] = y
+        return hdxf, dep, dat
+
+    def points(self, idx):
+        """lon, lat, dlon_zero, ilev (1-based), log p of the points idx."""
+        idx = np.asarray(idx)
+        nij = self.nlon * self.nlat
+        lev, ij = idx // nij, idx % nij
+        j, i = ij // self.nlon, ij % self.nlon
+        lat = self.lat[j]
+        dlon = self.params[2] / np.maximum(np.cos(3.1415926535 * lat / 180.0), 1e-12)
+        return self.lon[i], lat, dlon, (lev + 1).astype(np.int32), np.log(self.plev[lev])
+
+    def background_torch(self, device, idx):
+        """xb float32 [nv, len(idx), ne] at the points idx."""
+        import torch
+
+        lon, lat, _, ilev, lnp = self.points(idx)
+        xyz = torch.as_tensor(self._xyz(lon, lat, lnp), device=device)
+        k = torch.as_tensor(self.fields.k, device=device)
+        a = torch.as_tensor(self.fields.a[: self.ne], device=device)
+        ph = torch.as_tensor(self.fields.phi[: self.ne], device=device)
+        out = torch.empty((self.nvar, len(idx), self.ne), dtype=torch.float32, device=device)
+        for v in range(self.nvar):
+            arg = xyz @ k[v].T
+            out[v] = (a[:, v, None, :] * torch.cos(arg[None] + ph[:, v, None, :])).sum(-1).T.to(torch.float32)
+        return out
