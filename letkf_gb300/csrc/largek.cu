@@ -6,8 +6,10 @@
 // batch of points the matrices live in HBM (k padded to kp, a multiple of 128)
 // and every dense product runs on the tensor cores (largek_gemm.cuh):
 //   1. G = Ywᵀ Y            (tcgen05, three-term TF32, K = the point's L)
-//   2. A = G + (k-1)/rho I, padded with the same diagonal; scale s from a
-//      power iteration guarded by the Gershgorin bound; Y0 = A/s, Z0 = I
+//   2. A = G + (k-1)/rho I, padded with the same diagonal; scale s = 1.05 x a
+//      power-iteration estimate of lambda_max (tight: fewer iterations); a
+//      point whose residual grows restarts once from the Gershgorin bound,
+//      which always converges; Y0 = A/s, Z0 = I
 //   3. coupled Newton-Schulz  T = Z Y, Y <- 1.5 Y - 0.5 Y T,
 //      Z <- 1.5 Z - 0.5 T Z  until ||T - I||² < tol (per-point active flags)
 //   4. two uncoupled steps anchored to A:  Z <- 1.5 Z - 0.5 (Z (A/s) Z) Z,
@@ -30,8 +32,10 @@ constexpr int LK_POLISH = 2;
 
 struct LkPoint {  // per-point scalars of a batch
   double s, c, p1, p3, trace, infl;
+  float gmax;     // Gershgorin bound of lambda_max
+  float e2_prev;  // residual of the previous iteration
   int kind;       // 0 transform, 1 no observations, 2 unsupported spectrum, 3 no convergence
-  int pad;
+  int restarted;  // 1 after the restart from the Gershgorin scale
 };
 
 __global__ void lk_weights_kernel(int64_t n, const float* __restrict__ rdiag, const float* __restrict__ rloc,
@@ -101,8 +105,10 @@ __global__ void __launch_bounds__(LKP_NT) lk_prep_kernel(int ne, int kp, const i
     q.p3 = p3;
     q.trace = tr;
     q.infl = infl;
+    q.gmax = 0.f;
+    q.e2_prev = INFINITY;
     q.kind = kind;
-    q.pad = 0;
+    q.restarted = 0;
     pt[b] = q;
     active[b] = kind == 0;
   }
@@ -143,10 +149,11 @@ __global__ void __launch_bounds__(LKP_NT) lk_prep_kernel(int ne, int kp, const i
     for (int m = tid; m < kp; m += LKP_NT) xv[m] = yv[m] * inv;
     __syncthreads();
   }
-  const float s = fmaxf(1.05f * lam, 0.5f * gmax);
+  const float s = lam > 0.f ? 1.05f * lam : gmax;
   const float is = 1.f / s;
   if (tid == 0) {
     pt[b].s = (double)s;
+    pt[b].gmax = gmax;
     inv_s[b] = is;
   }
   float* Yb = Y + mo;
@@ -158,20 +165,50 @@ __global__ void __launch_bounds__(LKP_NT) lk_prep_kernel(int ne, int kp, const i
   }
 }
 
-// converged points leave the coupled phase; a non-finite residual (or, with
-// last != 0, a point still iterating at the cap) fails the point
-__global__ void lk_check_kernel(int nb, const float* __restrict__ e2, int* active, int* count, LkPoint* pt,
-                                int last) {
+// Converged points leave the coupled phase.  A residual that is not finite or
+// grows (after the first steps) restarts the point once from the Gershgorin
+// scale (counts[1]); a second failure, or a point still iterating at the cap
+// (last != 0), fails the point.  counts[0] = points still iterating.
+__global__ void lk_check_kernel(int nb, int it, const float* __restrict__ e2, int* active, int* counts, LkPoint* pt,
+                                int* restart, int last) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nb || !active[b]) return;
   const float r = e2[b];
-  if (!isfinite(r) || (last && !(r < LK_NS_TOL))) {
+  const float prev = pt[b].e2_prev;
+  const bool grows = !isfinite(r) || (it >= 2 && r > prev) || r > 4.f * prev;
+  if (grows && !pt[b].restarted) {
+    pt[b].restarted = 1;
+    pt[b].e2_prev = INFINITY;
+    restart[b] = 1;
+    atomicAdd(&counts[0], 1);
+    atomicAdd(&counts[1], 1);
+  } else if (grows || (last && !(r < LK_NS_TOL))) {
     pt[b].kind = 3;
     active[b] = 0;
   } else if (r < LK_NS_TOL) {
     active[b] = 0;
   } else {
-    atomicAdd(count, 1);
+    pt[b].e2_prev = r;
+    atomicAdd(&counts[0], 1);
+  }
+}
+
+// restart flagged points from s = Gershgorin bound: Y = A/s, Z = I
+__global__ void lk_restart_kernel(int kp, const float* __restrict__ G, float* Y, float* Z, float* inv_s, LkPoint* pt,
+                                  int* restart) {
+  const int b = blockIdx.y;
+  if (!restart[b]) return;
+  const size_t mo = (size_t)b * kp * kp;
+  const float s = pt[b].gmax, is = 1.f / s;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < (int64_t)kp * kp;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(idx / kp), j = (int)(idx - (int64_t)i * kp);
+    Y[mo + idx] = G[mo + idx] * is;
+    Z[mo + idx] = i == j ? 1.f : 0.f;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    pt[b].s = (double)s;
+    inv_s[b] = is;
   }
 }
 
@@ -370,7 +407,7 @@ extern "C" int letkf_core_batch_largek(int ne, int npts, const int64_t* offs, co
     return LETKF_ERR_CUDA;
   float *w = nullptr, *G = nullptr, *Y = nullptr, *Z = nullptr, *Yn = nullptr, *Zn = nullptr, *T = nullptr;
   float *bvec = nullptr, *e2 = nullptr, *inv_s = nullptr;
-  int *active = nullptr, *count = nullptr, *err = nullptr;
+  int *active = nullptr, *count = nullptr, *err = nullptr, *restart = nullptr;
   LkPoint* pt = nullptr;
   bool ok = true;
   auto A = [&](auto** p, size_t bytes) { ok = ok && cudaMallocAsync((void**)p, bytes, s) == cudaSuccess; };
@@ -385,7 +422,8 @@ extern "C" int letkf_core_batch_largek(int ne, int npts, const int64_t* offs, co
   A(&e2, sizeof(float) * B);
   A(&inv_s, sizeof(float) * B);
   A(&active, sizeof(int) * B);
-  A(&count, sizeof(int));
+  A(&count, 2 * sizeof(int));
+  A(&restart, sizeof(int) * B);
   A(&err, sizeof(int));
   A(&pt, sizeof(LkPoint) * B);
   int st = ok ? LETKF_OK : LETKF_ERR_CUDA;
@@ -418,9 +456,10 @@ extern "C" int letkf_core_batch_largek(int ne, int npts, const int64_t* offs, co
     g.wts = nullptr;
     g.offs = nullptr;
     g.active = active;
+    cudaMemsetAsync(restart, 0, sizeof(int) * nb, s);
     for (int it = 0; it < LK_NS_MAX && st == LETKF_OK; it++) {
       cudaMemsetAsync(e2, 0, sizeof(float) * nb, s);
-      cudaMemsetAsync(count, 0, sizeof(int), s);
+      cudaMemsetAsync(count, 0, 2 * sizeof(int), s);
       g.X = Z;
       g.Y = Y;
       g.D = nullptr;
@@ -428,12 +467,19 @@ extern "C" int letkf_core_batch_largek(int ne, int npts, const int64_t* offs, co
       g.e2 = e2;
       st = lk_gemm<LK_T>(g, nb, s);
       if (st) break;
-      lk_check_kernel<<<(nb + 127) / 128, 128, 0, s>>>(nb, e2, active, count, pt, it == LK_NS_MAX - 1);
+      lk_check_kernel<<<(nb + 127) / 128, 128, 0, s>>>(nb, it, e2, active, count, pt, restart, it == LK_NS_MAX - 1);
       note_launch();
-      int h_count = 0;
-      cudaMemcpyAsync(&h_count, count, sizeof(int), cudaMemcpyDeviceToHost, s);
+      int h_count[2] = {0, 0};
+      cudaMemcpyAsync(h_count, count, 2 * sizeof(int), cudaMemcpyDeviceToHost, s);
       st = cuda_status(cudaStreamSynchronize(s));
-      if (st || h_count == 0) break;
+      if (st || h_count[0] == 0) break;
+      if (h_count[1] > 0) {  // restart, then iterate again from Y0, Z0
+        dim3 rg(64, nb);
+        lk_restart_kernel<<<rg, 256, 0, s>>>(kp, G, Y, Z, inv_s, pt, restart);
+        note_launch();
+        cudaMemsetAsync(restart, 0, sizeof(int) * nb, s);
+        continue;
+      }
       g.alpha = -0.5f;
       g.beta = 1.5f;
       g.X = Y;  // Y <- 1.5 Y - 0.5 Y T
@@ -492,7 +538,7 @@ extern "C" int letkf_core_batch_largek(int ne, int npts, const int64_t* offs, co
     st = cuda_status(cudaStreamSynchronize(s));
     if (st == LETKF_OK && h_err) st = LETKF_ERR_TIMEOUT;
   }
-  void* fr[] = {w, G, Y, Z, Yn, Zn, T, bvec, e2, inv_s, active, count, err, pt};
+  void* fr[] = {w, G, Y, Z, Yn, Zn, T, bvec, e2, inv_s, active, count, err, pt, restart};
   for (void* p : fr)
     if (p) cudaFreeAsync(p, s);
   return st;

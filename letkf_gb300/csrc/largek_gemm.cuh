@@ -6,7 +6,9 @@
 // (x = hi + lo, hi = x with the low 13 mantissa bits cleared):
 //   acc = A_hi B_hi + A_hi B_lo + A_lo B_hi        (about 1e-6 relative)
 // staged K-major (SWIZZLE_NONE core matrices of 8 rows x 16 bytes) in two
-// 64 KB stages so the staging of stage c+1 overlaps the MMAs of stage c.
+// 32 KB stages (K = 16) so the staging of stage c+1 overlaps the MMAs of
+// stage c; 64 KB per CTA lets three CTAs share an SM (384 TMEM columns), so
+// one CTA's MMAs also overlap another's global loads.
 //
 // Modes:
 //   LK_GRAM   out = Ywᵀ Y over the point's local rows (K = its L, rows of the
@@ -25,8 +27,8 @@ namespace letkf {
 
 constexpr int LK_NT = 256;
 constexpr int LK_TILE = 128;
-constexpr int LK_KC = 32;                // K per stage
-constexpr int LK_OPER = 16384;           // one 128 x 32 TF32 operand
+constexpr int LK_KC = 16;                // K per stage
+constexpr int LK_OPER = 8192;            // one 128 x 16 TF32 operand
 constexpr int LK_STAGE = 4 * LK_OPER;    // A_hi, A_lo, B_hi, B_lo
 constexpr int LK_SMEM = 2 * LK_STAGE + 64;
 constexpr uint32_t LK_TMEM_COLS = 128;
@@ -72,7 +74,7 @@ __device__ __forceinline__ void lk_store(unsigned char* hi_base, unsigned char* 
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(LK_NT, 1) largek_gemm_kernel(LkGemmArgs a) {
+__global__ void __launch_bounds__(LK_NT, 3) largek_gemm_kernel(LkGemmArgs a) {
   extern __shared__ __align__(1024) unsigned char sm[];
   uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + 2 * LK_STAGE);
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(sm + 2 * LK_STAGE + 16);
@@ -117,7 +119,7 @@ __global__ void __launch_bounds__(LK_NT, 1) largek_gemm_kernel(LkGemmArgs a) {
   uint32_t par[2] = {0u, 0u};
   bool outst[2] = {false, false};
   int tmo = 0;
-  const int r = tid & 127, h = tid >> 7;  // staging: row r, K half h (16 values)
+  const int r = tid & 127, h = tid >> 7;  // staging: row r, K half h (8 values)
 
   for (int c = 0; c < nk; c++) {
     const int buf = c & 1;
@@ -130,8 +132,8 @@ __global__ void __launch_bounds__(LK_NT, 1) largek_gemm_kernel(LkGemmArgs a) {
     unsigned char* st = sm + buf * LK_STAGE;
     const int k0 = c * LK_KC;
 #pragma unroll
-    for (int g = 0; g < 4; g++) {
-      const int kk = h * 16 + g * 4;
+    for (int g = 0; g < 2; g++) {
+      const int kk = h * 8 + g * 4;
       float va[4], vb[4];
       if (MODE == LK_GRAM) {
         // A(m, l) = w_l y_l[m], B(n, l) = y_l[n]; rows beyond L or members beyond ne are 0
@@ -174,9 +176,9 @@ __global__ void __launch_bounds__(LK_NT, 1) largek_gemm_kernel(LkGemmArgs a) {
         const uint32_t sa = s0 + (pass == 2 ? LK_OPER : 0);
         const uint32_t sb = s0 + 2 * LK_OPER + (pass == 1 ? LK_OPER : 0);
 #pragma unroll
-        for (int s = 0; s < 4; s++)
-          tc::mma_tf32(tacc, tc::smem_desc(sa + s * 256, 128, 1024), tc::smem_desc(sb + s * 256, 128, 1024), idesc,
-                       (c == 0 && pass == 0 && s == 0) ? 0u : 1u);
+        for (int s = 0; s < LK_KC / 8; s++)
+          tc::mma_tf32(tacc, tc::smem_desc(sa + s * 256, 128, LK_KC * 32), tc::smem_desc(sb + s * 256, 128, LK_KC * 32),
+                       idesc, (c == 0 && pass == 0 && s == 0) ? 0u : 1u);
       }
       tc::mma_commit(&mbar[buf]);
     }
