@@ -2,21 +2,22 @@
 //
 // Same work as sweep_mixed.cu (search, Gram, transform, update per grid point,
 // one persistent launch), for ensembles up to 64 members, with the two
-// contraction stages issued as tcgen05.mma (kind::f16, bf16 operands, FP32
-// accumulation in tensor memory) from shared-memory descriptors:
+// contraction stages issued as tcgen05.mma from shared-memory descriptors
+// and FP32 accumulation in tensor memory:
 //
-//  * Gram  G = Ywᵀ Y (common/common_letkf.f90:101-118): every chunk of 32
-//    accepted observations is staged as A = [Yw_hiᵀ ; Yw_loᵀ] (128 x 32) and
-//    B = Y_hi, Y_lo (64 x 32, K-major), where x_hi = bf16(x) and
-//    x_lo = bf16(x - x_hi).  Two M=128 MMAs accumulate D0 = A Y_hiᵀ and
-//    D1 = A Y_loᵀ in TMEM; G is the sum of their four 64 x 64 blocks, i.e. the
-//    product of the two-term splits (about 16 significant bits per factor).
-//    Staging of chunk c+1 overlaps the MMAs of chunk c (two buffers, one
-//    mbarrier each).
+//  * Gram  G = Ywᵀ Y (common/common_letkf.f90:101-118): every stage of 24
+//    accepted observations is staged K-major as A = [Yw_hi; Yw_lo] (128 x 24
+//    TF32) with B = Y_hi and B = Y_lo (64 x 24); two M=128 MMAs accumulate
+//    D0 = A Y_hiᵀ and D1 = A Y_loᵀ in tensor memory, and G is the sum of their
+//    four 64 x 64 blocks, i.e. the product of the two-term TF32 splits (about
+//    1e-6 relative).  Staging of stage c+1 overlaps the MMAs of stage c (two
+//    24 KB buffers, one mbarrier each).
 //  * Newton-Schulz  A^(-1/2): the iterates Y, Z commute, so one iteration is
-//    T = Z Y and [Y;Z] <- 1.5 [Y;Z] - 0.5 [Y;Z] T: two M=128 MMAs with the
-//    stacked operand S = [Y;Z] (128 x 64) and B = Y or T (64 x 64), each as
-//    the three split products hi.hi + hi.lo + lo.hi.
+//    T = Z Y and [Y;Z] <- 1.5 [Y;Z] - 0.5 [Y;Z] T: two M=128 MMA groups with
+//    the stacked operand S = [Y;Z] (128 x 64) and B = Y or T (64 x 64), each
+//    as the three split products hi.hi + hi.lo + lo.hi of BF16 splits.
+//  * An uncoupled FP32 step anchored to the exact A (kept in tensor memory)
+//    restores FP32 accuracy after the 16-bit phase.
 //
 // Points where the transform needs mtx_eigen's truncation semantics (c <= 0 or
 // tr(G) >= 1e6 c) are appended to a deferred list for the Jacobi pass.
@@ -29,7 +30,7 @@
 namespace letkf {
 
 constexpr int TC_NT = 128;
-constexpr int TC_CH = 16;  // observations per Gram stage
+constexpr int TC_CH = 24;  // observations per Gram stage
 constexpr int TC_NP = 64;
 constexpr uint32_t TC_TMEM_COLS = 128;
 constexpr uint32_t TC_WAIT = 1u << 22;
@@ -38,11 +39,11 @@ constexpr int TC_POLISH_MAX = 8;  // FP32 iterations at most
 // byte offsets in dynamic shared memory
 struct TcLayout {
   // operand region, 48 KB, reused by phase
-  static constexpr int STG = 0;           // two Gram stages of 16 KB
-  static constexpr int STG_A = 0;         //   A = [Yw_hi^T; Yw_lo^T]: 128 x 16 tf32 (8 KB)
-  static constexpr int STG_BH = 8192;     //   Y_hi^T: 64 x 16 tf32 (4 KB)
-  static constexpr int STG_BL = 12288;    //   Y_lo^T
-  static constexpr int STG_SIZE = 16384;
+  static constexpr int STG = 0;           // two Gram stages of 24 KB
+  static constexpr int STG_A = 0;         //   A = [Yw_hi^T; Yw_lo^T]: 128 x 24 tf32 (12 KB)
+  static constexpr int STG_BH = 12288;    //   Y_hi^T: 64 x 24 tf32 (6 KB)
+  static constexpr int STG_BL = 18432;    //   Y_lo^T
+  static constexpr int STG_SIZE = 24576;
   static constexpr int S_HI = 0;          // Newton-Schulz S = [Y; Z]: 128 x 64 bf16 (16 KB)
   static constexpr int S_LO = 16384;
   static constexpr int B_HI = 32768;      // B = Y or T: 64 x 64 bf16 (8 KB)
@@ -205,10 +206,11 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
       }
       tc::fence_after_sync();
       unsigned char* stg = sm + L::STG + buf * L::STG_SIZE;
-      float yv[8], wv[8];
+      constexpr int KH = TC_CH / 2;  // observations per thread: member m, half hh
+      float yv[KH], wv[KH];
 #pragma unroll
-      for (int kk = 0; kk < 8; kk++) {
-        const int k = hh * 8 + kk;
+      for (int kk = 0; kk < KH; kk++) {
+        const int k = hh * KH + kk;
         float y = 0.f, w = 0.f, dd = 0.f;
         if (k < nr) {
           w = ss.pw[k];
@@ -220,20 +222,20 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
         bpart = fmaf(wv[kk], dd, bpart);
       }
 #pragma unroll
-      for (int g = 0; g < 2; g++) {
+      for (int g = 0; g < KH / 4; g++) {
         float4 h, l;
-        const uint32_t off = tc::kmajor_off(m, hh * 8 + g * 4, TC_CH);
+        const uint32_t off = tc::kmajor_off(m, hh * KH + g * 4, TC_CH);
         split4_tf32(wv + 4 * g, h, l);
         *reinterpret_cast<float4*>(stg + L::STG_A + off) = h;
-        *reinterpret_cast<float4*>(stg + L::STG_A + tc::kmajor_off(64 + m, hh * 8 + g * 4, TC_CH)) = l;
+        *reinterpret_cast<float4*>(stg + L::STG_A + tc::kmajor_off(64 + m, hh * KH + g * 4, TC_CH)) = l;
         split4_tf32(yv + 4 * g, h, l);
         *reinterpret_cast<float4*>(stg + L::STG_BH + off) = h;
         *reinterpret_cast<float4*>(stg + L::STG_BL + off) = l;
       }
-      if (tid < nr) {
-        const float dd = ss.pd[tid];
-        p1 = fmaf(dd * dd, ss.pw[tid], p1);
-        p3 += ss.pr[tid];
+      for (int k = tid; k < nr; k += TC_NT) {
+        const float dd = ss.pd[k];
+        p1 = fmaf(dd * dd, ss.pw[k], p1);
+        p3 += ss.pr[k];
       }
       tc::fence_smem_async();
       tc::fence_before_sync();
@@ -241,14 +243,15 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
       if (tid == 0) {
         tc::fence_after_sync();
         const uint32_t sa = sbase + L::STG + buf * L::STG_SIZE;
+        constexpr uint32_t SBO = TC_CH * 32;  // bytes between 8-row core-matrix groups
 #pragma unroll
-        for (int s = 0; s < 2; s++)
-          tc::mma_tf32(D0, tc::smem_desc(sa + L::STG_A + s * 256, 128, 512),
-                       tc::smem_desc(sa + L::STG_BH + s * 256, 128, 512), idesc_g, (first && s == 0) ? 0u : 1u);
+        for (int s = 0; s < TC_CH / 8; s++)
+          tc::mma_tf32(D0, tc::smem_desc(sa + L::STG_A + s * 256, 128, SBO),
+                       tc::smem_desc(sa + L::STG_BH + s * 256, 128, SBO), idesc_g, (first && s == 0) ? 0u : 1u);
 #pragma unroll
-        for (int s = 0; s < 2; s++)
-          tc::mma_tf32(D1, tc::smem_desc(sa + L::STG_A + s * 256, 128, 512),
-                       tc::smem_desc(sa + L::STG_BL + s * 256, 128, 512), idesc_g, (first && s == 0) ? 0u : 1u);
+        for (int s = 0; s < TC_CH / 8; s++)
+          tc::mma_tf32(D1, tc::smem_desc(sa + L::STG_A + s * 256, 128, SBO),
+                       tc::smem_desc(sa + L::STG_BL + s * 256, 128, SBO), idesc_g, (first && s == 0) ? 0u : 1u);
         tc::mma_commit(&mbar[buf]);
       }
       outst[buf] = true;
