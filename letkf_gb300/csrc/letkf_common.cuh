@@ -49,6 +49,27 @@ __device__ __forceinline__ T block_sum(T v, T* red) {
   return s;
 }
 
+// Block-wide sums of K values at once (two barriers instead of three per
+// value); `red` holds >= K * NT / 32 elements.  Every thread gets the sums.
+template <typename T, int NT, int K>
+__device__ __forceinline__ void block_sum_k(T (&v)[K], T* red) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < K; i++) v[i] = warp_sum(v[i]);
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int i = 0; i < K; i++) red[w * K + i] = v[i];
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < K; i++) {
+    T s = T(0);
+#pragma unroll
+    for (int q = 0; q < NT / 32; q++) s += red[q * K + i];
+    v[i] = s;
+  }
+}
+
 // Fortran SIGN(a,b)
 __device__ __forceinline__ double fsign(double a, double b) { return copysign(fabs(a), b); }
 __device__ __forceinline__ float fsignf(float a, float b) { return copysignf(fabsf(a), b); }

@@ -423,14 +423,24 @@ __device__ int ns_polish(const float* As, float* Z, float* P, float* redf, int m
 #pragma unroll
       for (int b = 0; b < C::TC; b++) Z[(i0 + a) * NP + j0 + b] = acc[a][b];
     __syncthreads();
-    for (int idx = tid; idx < NP * NP; idx += C::NT) {
-      const int i = idx / NP, j = idx - i * NP;
-      if (i < j) {
-        const float v = 0.5f * (Z[i * NP + j] + Z[j * NP + i]);
-        Z[i * NP + j] = v;
-        Z[j * NP + i] = v;
+    // symmetrise: the mirror of this thread's tile is TC rows of TR contiguous
+    // values (float4 reads, no bank conflicts); Z <- (Z + Z^T) / 2
+    float mir[C::TR][C::TC];
+#pragma unroll
+    for (int b = 0; b < C::TC; b++)
+#pragma unroll
+      for (int t = 0; t < C::TR; t += 4) {
+        const float4 x = *reinterpret_cast<const float4*>(Z + (j0 + b) * NP + i0 + t);
+        mir[t][b] = x.x;
+        mir[t + 1][b] = x.y;
+        mir[t + 2][b] = x.z;
+        mir[t + 3][b] = x.w;
       }
-    }
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < C::TR; a++)
+#pragma unroll
+      for (int b = 0; b < C::TC; b++) Z[(i0 + a) * NP + j0 + b] = 0.5f * (acc[a][b] + mir[a][b]);
     __syncthreads();
     if (last) {
       it++;

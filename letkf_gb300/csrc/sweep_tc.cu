@@ -315,9 +315,11 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
         }
       }
       __syncthreads();
-      const float trace = block_sum<float, TC_NT>(tid < 64 ? Gt[tid * 64 + tid] : 0.f, red);
-      p1 = block_sum<float, TC_NT>(p1, red);
-      p3 = block_sum<float, TC_NT>(p3, red);
+      float sums[3] = {tid < 64 ? Gt[tid * 64 + tid] : 0.f, p1, p3};
+      block_sum_k<float, TC_NT, 3>(sums, red);
+      const float trace = sums[0];
+      p1 = sums[1];
+      p3 = sums[2];
       if (!(cdiag > 0.f) || !((double)trace < 1.0e6 * (double)cdiag)) {
         deferred = true;  // needs the eigensolver with mtx_eigen's truncation
       } else {
@@ -357,8 +359,9 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
             part = acc * acc;
             xx = vx[tid] * vx[tid];
           }
-          const float nrm2 = block_sum<float, TC_NT>(part, red);
-          const float x2 = block_sum<float, TC_NT>(xx, red);
+          float q2[2] = {part, xx};
+          block_sum_k<float, TC_NT, 2>(q2, red);
+          const float nrm2 = q2[0], x2 = q2[1];
           lam = sqrtf(nrm2 / fmaxf(x2, 1e-30f));
           const float inv = rsqrtf(fmaxf(nrm2, 1e-30f));
           if (tid < 64) vx[tid] = vy[tid] * inv;
