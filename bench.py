@@ -498,7 +498,7 @@ def run_gpu(args, rank, world, dist):
     nthreads = os.cpu_count() or 1
     probe = sample_points(wl, 64, seed=99)
     dtp, *_ = cpu_oracle_run(wl, so, hd, dp, probe, nthreads)
-    nsample = int(max(256, min(16384, 64 * args.cpu_seconds / max(dtp, 1e-6))))
+    nsample = int(max(256, min(131072, 64 * args.cpu_seconds / max(dtp, 1e-6))))
     idx = sample_points(wl, nsample, seed=7)
     dtc, xb_s, xa_ref, inf_ref, nl_ref = cpu_oracle_run(wl, so, hd, dp, idx, nthreads)
     out["cpu_baseline"] = {"value": idx.size / dtc, "unit": UNIT, "cores": nthreads, "kind": "port",
