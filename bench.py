@@ -472,19 +472,22 @@ def run_gpu(args, rank, world, dist):
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
+    step_ms = []
     for _ in range(e2e_steps):
+        ts = time.perf_counter()
         L.check(_L().letkf_sweep_set_background(sw.h, C.c_void_p(xb_host.data_ptr()), 0), "set_background")
         sw.set_obs(wl.ri, wl.rj, wl.lev, dat, wl.err, dep, wl.cls, hdxf)
         sw.run(stream.cuda_stream)
         torch.cuda.synchronize()
         sw.analysis_into(xa_host.data_ptr())
+        step_ms.append(round(1e3 * (time.perf_counter() - ts), 1))
     torch.cuda.synchronize()
     te = time.perf_counter() - t0
     if dist:
         tt = torch.tensor([te], device=dev)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         te = float(tt.item())
-    out["e2e"] = {"value": world * wl.npts * e2e_steps / te, "unit": UNIT, "steps": e2e_steps,
+    out["e2e"] = {"value": world * wl.npts * e2e_steps / te, "unit": UNIT, "steps": e2e_steps, "step_ms": step_ms,
                   "h2d_bytes_per_step": int(xb.numel() * 4 + obs_bytes), "d2h_bytes_per_step": int(xb.numel() * 4)}
     if rank != 0:
         return out, sw
