@@ -182,6 +182,33 @@ int letkf_obs_departure(int ne, int nobs, const double* hx, const double* y, con
                         double gross_error, const int* qc_in, double* hdxf, double* dep, int* qc_out,
                         void* stream);
 
+/* ------------------------------------------------------------------------
+ * Obs-space clients of the core (GFS driver), DEVICE buffers.
+ * Analysis ensemble at n observation locations (gfs/letkf/letkf_tools.f90:
+ * 466-497): trans[n][ne*ne] the merged transforms (T + wbar 1^T, column-
+ * major) from a core run at the observation locations, ybar = obsdat -
+ * obsdep, hdxf [n][ne] the observations' own perturbations; relax_alpha != 0
+ * applies weight_RTPP (:959-970); mode[n] (NULL: all 0) is 0 update, 1 no
+ * update (q above the update level: anal = ybar + hdxf), 2 update and clip
+ * the relative spread to q_sprd_max.  anal [n][ne], anal_mean [n] (may be NULL). */
+int letkf_obs_analysis(int ne, int n, const double* trans, const double* ybar, const double* hdxf,
+                       double relax_alpha, const int* mode, double q_sprd_max, double* anal,
+                       double* anal_mean, void* stream);
+
+/* Ensemble forecast sensitivity to observations (EFSO, gfs/letkf/letkf_tools.f90:
+ * 547-679) over npts grid points with their local lists offs/idx/rdiag/rloc
+ * (a search's output): work1(t,m) = sum_v [term[v] == t] fcst(v,p,m) fcer(v,p),
+ * djdy(n,t) = sum over the points that select n of sum_m work1(t,m)
+ * hdxa(n,m) / rdiag * rloc, obsense(n,t) = djdy(n,t) obsdep(n).  fcst
+ * [nv][npts][ne] (C^1/2 X^f_t), fcer [nv][npts] (C^1/2 (e^f_t + e^g_t) /
+ * 2(K-1)), hdxa [nobs][ne] (Y^a_0), djdy and obsense [nobs][nterm].  term[nv]
+ * is a HOST array (term index or -1); nv <= 16, nterm <= 8.  djdy is
+ * accumulated with atomics (sum order differs from the serial loop by rounding). */
+int letkf_efso(int ne, int npts, int nv, int nterm, const int* term, const int64_t* offs,
+               const int* idx, const double* rdiag, const double* rloc, int nobs, const double* hdxa,
+               const double* fcst, const double* fcer, const double* obsdep, double* djdy,
+               double* obsense, void* stream);
+
 /* Lorenz-96 selection (lorenz96/letkf/letkf.f90:220-254).  obs_cell[ny] is
  * the 1-based grid index of each observation (first maximum of its row of H,
  * see letkf_l96_obs_cell); pix[npts] are 1-based grid indices.  An

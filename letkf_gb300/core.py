@@ -188,6 +188,40 @@ def relax_beta(ri, rj, rlev, nv, q_lo=-1, q_hi=-2, q_update_top=0.0, boundary_bu
     return beta
 
 
+def obs_analysis(trans, ybar, hdxf, relax_alpha=0.0, mode=None, q_sprd_max=0.0, stream=None):
+    """Analysis ensemble at observation locations (gfs/letkf/letkf_tools.f90:
+    466-497).  trans float64 [n, ne, ne] (merged T + wbar, column-major per
+    point), ybar [n], hdxf [n, ne]; mode int32 [n] or None.  Returns (anal
+    [n, ne], mean [n])."""
+    import torch
+
+    n, ne = hdxf.shape
+    anal = torch.empty_like(hdxf)
+    mean = torch.empty(n, dtype=torch.float64, device=hdxf.device)
+    check(lib().letkf_obs_analysis(ne, n, _dptr(trans), _dptr(ybar), _dptr(hdxf), float(relax_alpha), _dptr(mode),
+                                   float(q_sprd_max), _dptr(anal), _dptr(mean), _stream(stream)), "letkf_obs_analysis")
+    return anal, mean
+
+
+def efso(ne, offs, idx, rdiag, rloc, hdxa, fcst, fcer, term, obsdep, stream=None):
+    """Observation sensitivity (gfs/letkf/letkf_tools.f90:547-679) on device
+    tensors: local lists offs/idx/rdiag/rloc, hdxa [nobs, ne], fcst [nv, npts,
+    ne], fcer [nv, npts], term (host list, one entry per variable), obsdep
+    [nobs].  Returns (djdy, obsense), each [nobs, nterm]."""
+    import torch
+
+    nv, npts, _ = fcst.shape
+    term = np.ascontiguousarray(term, dtype=np.int32)
+    nterm = int(term.max()) + 1
+    nobs = hdxa.shape[0]
+    djdy = torch.empty((nobs, nterm), dtype=torch.float64, device=hdxa.device)
+    obsense = torch.empty_like(djdy)
+    check(lib().letkf_efso(ne, npts, nv, nterm, term.ctypes.data_as(C.c_void_p), _dptr(offs), _dptr(idx),
+                           _dptr(rdiag), _dptr(rloc), nobs, _dptr(hdxa), _dptr(fcst), _dptr(fcer), _dptr(obsdep),
+                           _dptr(djdy), _dptr(obsense), _stream(stream)), "letkf_efso")
+    return djdy, obsense
+
+
 def exclusive_scan(counts, stream=None):
     import torch
 
@@ -326,5 +360,5 @@ def search_l96(nx, obs_cell, pix, xlocal=3.0, obserr=1.0, tdif=0.0, tlocal=-1.0,
 
 
 __all__ = ["letkf_core", "core_batch_f64", "core_batch_mixed", "update_f64", "exclusive_scan", "gather_rows",
-           "search_scale", "search_speedy", "search_l96", "l96_obs_cell", "obs_departure", "update_relax_f64", "relax_beta", "core_batch_largek", "update_mixed", "RELAX_NONE", "RELAX_RTPP",
+           "search_scale", "search_speedy", "search_l96", "l96_obs_cell", "obs_departure", "update_relax_f64", "relax_beta", "core_batch_largek", "update_mixed", "obs_analysis", "efso", "RELAX_NONE", "RELAX_RTPP",
            "RELAX_RTPS", "LETKF_OK"]

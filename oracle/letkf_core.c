@@ -464,3 +464,75 @@ void oracle_weight_rtps(int ne, const double* w, const double* pa, const double*
     *infl = 1.0;
   }
 }
+
+/* Observation-space analysis at one observation location
+ * (gfs/letkf/letkf_tools.f90:466-497): trans (ne x ne, column-major, mean
+ * weights merged, RTPP already applied by the caller), ybar = obsdat - obsdep,
+ * hdxf = obshdxf(nn,:).  mode 0: update; 1: no update (q above the update
+ * level); 2: update and relative-spread clip (q).  Writes anal[ne] and
+ * returns the mean. */
+double oracle_obs_analysis(int ne, const double* trans, double ybar, const double* hdxf, int mode,
+                           double q_sprd_max, double* anal) {
+  int m, k;
+  double mean = 0.0;
+  if (mode == 1) {
+    for (m = 0; m < ne; m++) anal[m] = ybar + hdxf[m];
+    return ybar;
+  }
+  for (m = 0; m < ne; m++) {
+    anal[m] = ybar;
+    for (k = 0; k < ne; k++) anal[m] = anal[m] + hdxf[k] * trans[(size_t)m * ne + k];
+    mean = mean + anal[m];
+  }
+  mean = mean / (double)ne;
+  if (mode == 2) {
+    double sp = 0.0;
+    double* qa = (double*)malloc(sizeof(double) * (size_t)ne);
+    for (m = 0; m < ne; m++) {
+      qa[m] = anal[m] - mean;
+      sp = sp + qa[m] * qa[m];
+    }
+    sp = sqrt(sp / (double)(ne - 1)) / mean;
+    if (sp > q_sprd_max)
+      for (m = 0; m < ne; m++) anal[m] = mean + qa[m] * q_sprd_max / sp;
+    free(qa);
+  }
+  return mean;
+}
+
+/* Observation sensitivity (EFSO, gfs/letkf/letkf_tools.f90:547-679) over
+ * npts grid points with local lists offs/idx/rdiag/rloc (from obs_local):
+ *   work1(t,m) = sum_v [term(v) == t] fcst(v,p,m) * fcer(v,p)
+ *   djdy(t, idx) += sum_m work1(t,m) * hdxa(idx,m) / rdiag * rloc
+ *   obsense(t, n) = djdy(t, n) * obsdep(n)
+ * fcst [nv][npts][ne], fcer [nv][npts], term[nv] in 0..nterm-1 or -1,
+ * hdxa [nobs][ne]; djdy and obsense [nobs][nterm] (zeroed here).  Points are
+ * visited in order (the reference accumulates djdy in its loop order). */
+void oracle_efso(int ne, int npts, int nv, int nterm, const int64_t* offs, const int* idx, const double* rdiag,
+                 const double* rloc, const double* hdxa, const double* fcst, const double* fcer, const int* term,
+                 int nobs, const double* obsdep, double* djdy, double* obsense) {
+  int p, v, m, t;
+  int64_t l;
+  double* work1 = (double*)malloc(sizeof(double) * (size_t)nterm * ne);
+  for (l = 0; l < (int64_t)nobs * nterm; l++) djdy[l] = 0.0;
+  for (p = 0; p < npts; p++) {
+    if (offs[p + 1] == offs[p]) continue;
+    for (l = 0; l < (int64_t)nterm * ne; l++) work1[l] = 0.0;
+    for (v = 0; v < nv; v++) {
+      t = term[v];
+      if (t < 0) continue;
+      for (m = 0; m < ne; m++)
+        work1[(size_t)t * ne + m] = work1[(size_t)t * ne + m] +
+                                    fcst[((size_t)v * npts + p) * ne + m] * fcer[(size_t)v * npts + p];
+    }
+    for (l = offs[p]; l < offs[p + 1]; l++) {
+      const int ob = idx[l];
+      for (m = 0; m < ne; m++) {
+        const double hr = hdxa[(size_t)ob * ne + m] / rdiag[l] * rloc[l];
+        for (t = 0; t < nterm; t++) djdy[(size_t)ob * nterm + t] = djdy[(size_t)ob * nterm + t] + work1[(size_t)t * ne + m] * hr;
+      }
+    }
+  }
+  for (l = 0; l < (int64_t)nobs * nterm; l++) obsense[l] = djdy[l] * obsdep[l / nterm];
+  free(work1);
+}

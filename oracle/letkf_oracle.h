@@ -149,6 +149,11 @@ int oracle_scale_sweep(const oracle_scale_obs* o, const double* hdxf, const doub
 void oracle_weight_rtpp(int ne, const double* w, double alpha, double* wrlx);
 void oracle_weight_rtps(int ne, const double* w, const double* pa, const double* xb, double alpha,
                         double* wrlx, double* infl);
+double oracle_obs_analysis(int ne, const double* trans, double ybar, const double* hdxf, int mode,
+                           double q_sprd_max, double* anal);
+void oracle_efso(int ne, int npts, int nv, int nterm, const int64_t* offs, const int* idx, const double* rdiag,
+                 const double* rloc, const double* hdxa, const double* fcst, const double* fcer, const int* term,
+                 int nobs, const double* obsdep, double* djdy, double* obsense);
 
 #ifdef __cplusplus
 }

@@ -52,6 +52,10 @@ def lib():
                                             pd, pd, pd, pd, pi, d, C.c_int]
         _lib.oracle_weight_rtpp.argtypes = [C.c_int, pd, d, pd]
         _lib.oracle_weight_rtps.argtypes = [C.c_int, pd, pd, pd, d, pd, pd]
+        _lib.oracle_obs_analysis.restype = d
+        _lib.oracle_obs_analysis.argtypes = [C.c_int, pd, d, pd, C.c_int, d, pd]
+        _lib.oracle_efso.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int64), pi, pd, pd, pd, pd,
+                                     pd, pi, C.c_int, pd, pd, pd]
     return _lib
 
 
@@ -297,3 +301,32 @@ def weight_rtps(w, pa, xb, alpha):
     infl = np.zeros(1)
     lib().oracle_weight_rtps(w.shape[0], _pd(w), _pd(pa), _pd(_f64(xb)), float(alpha), _pd(out), _pd(infl))
     return out, float(infl[0])
+
+
+def obs_analysis(trans, ybar, hdxf, mode=0, q_sprd_max=0.0):
+    """gfs/letkf/letkf_tools.f90:466-497 at one observation location.  trans is
+    (ne, ne) with trans[k, m] = trans(k+1, m+1).  Returns (anal[ne], mean)."""
+    t = _f64(trans, "F")
+    ne = t.shape[0]
+    anal = np.zeros(ne)
+    mean = lib().oracle_obs_analysis(ne, _pd(t), float(ybar), _pd(_f64(hdxf)), int(mode), float(q_sprd_max),
+                                     _pd(anal))
+    return anal, mean
+
+
+def efso(ne, offs, idx, rdiag, rloc, hdxa, fcst, fcer, term, obsdep):
+    """gfs/letkf/letkf_tools.f90:547-679.  fcst (nv, npts, ne), fcer (nv, npts),
+    hdxa (nobs, ne).  Returns (djdy, obsense), each (nobs, nterm)."""
+    offs = np.ascontiguousarray(offs, dtype=np.int64)
+    fcst = _f64(fcst)
+    nv, npts, _ = fcst.shape
+    term = np.ascontiguousarray(term, dtype=np.int32)
+    nterm = int(term.max()) + 1
+    hdxa = _f64(hdxa)
+    nobs = hdxa.shape[0]
+    djdy = np.zeros((nobs, nterm))
+    obsense = np.zeros((nobs, nterm))
+    lib().oracle_efso(ne, npts, nv, nterm, offs.ctypes.data_as(C.POINTER(C.c_int64)),
+                      _pi(np.ascontiguousarray(idx, dtype=np.int32)), _pd(_f64(rdiag)), _pd(_f64(rloc)), _pd(hdxa),
+                      _pd(fcst), _pd(_f64(fcer)), _pi(term), nobs, _pd(_f64(obsdep)), _pd(djdy), _pd(obsense))
+    return djdy, obsense
