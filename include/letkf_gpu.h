@@ -209,6 +209,34 @@ int letkf_efso(int ne, int npts, int nv, int nterm, const int* term, const int64
                const double* fcst, const double* fcer, const double* obsdep, double* djdy,
                double* obsense, void* stream);
 
+/* SPEEDY observation operator H(x) for every member, replacing the obsope
+ * program (speedy/letkf/obsope.f90:53-104) run once per member:
+ * phys2ijk (speedy/common/common_obs_speedy.f90:137-206) against the member's
+ * p_full = ps sig(k), the driver's range rules (CEILING(rk) > nlev rejected;
+ * below the lowest level u/v use rk = 1.00001, others are rejected; ps with
+ * odat < -100 rejected) and Trans_XtoY (:29-80: itpl_3d of u/v/t/q, itpl_2d
+ * of ps/rain, calc_rh at the eight corners for RH).  Element codes are the
+ * NINT of the reference's elm (2819 u, 2820 v, 3073 t, 3330 q, 3331 rh,
+ * 14593 ps, 9999 rain); an unknown code gives hx = 0 with qc 1, like the
+ * driver's zero-initialised ohx.  A non-positive level of a non-ps
+ * observation is rejected (its log is undefined).
+ * Fields (device, FP64): v3d(i,j,k,n) of member m at
+ * v3d[m*v3d_mem_stride + (n*nlev + k)*v3d_rec_stride + j*nlon + i] (n = 0 u,
+ * 1 v, 2 t, 3 q; 0-based), v2d(i,j,n) at v2d[m*v2d_mem_stride +
+ * n*v2d_rec_stride + j*nlon + i] (n = 0 ps, 1 rain).  A grd file per member
+ * is rec stride nlat*nlon, member stride (4 nlev + 2) nlat nlon.  lat[nlat]
+ * (degrees, searched in order like the reference), sig[nlev] on the device.
+ * Observations (device): elem[nobs] int, rlon/rlat/rlev/odat[nobs].
+ * Outputs: hx[nobs][ne] (0 where rejected), qc_member[nobs][ne] (may be
+ * NULL) and qc[nobs] = min over members (may be NULL), as set_letkf_obs
+ * combines the members (speedy/letkf/letkf_obs.f90:157-158).
+ * nlat >= 2, nlev >= 2. */
+int letkf_speedy_obsope(int nlon, int nlat, int nlev, int ne, const double* lat, const double* sig,
+                        const double* v3d, int64_t v3d_mem_stride, int64_t v3d_rec_stride,
+                        const double* v2d, int64_t v2d_mem_stride, int64_t v2d_rec_stride, int nobs,
+                        const int* elem, const double* rlon, const double* rlat, const double* rlev,
+                        const double* odat, double* hx, int* qc_member, int* qc, void* stream);
+
 /* Lorenz-96 selection (lorenz96/letkf/letkf.f90:220-254).  obs_cell[ny] is
  * the 1-based grid index of each observation (first maximum of its row of H,
  * see letkf_l96_obs_cell); pix[npts] are 1-based grid indices.  An

@@ -59,6 +59,14 @@ def _dptr(t):
     return C.c_void_p(t.data_ptr())
 
 
+def _viewptr(t):
+    """Pointer to the first element of a strided CUDA view (the callee takes
+    the strides separately)."""
+    if not t.is_cuda:
+        raise ValueError("expected a CUDA tensor")
+    return C.c_void_p(t.data_ptr())
+
+
 def _stream(stream):
     import torch
 
@@ -220,6 +228,40 @@ def efso(ne, offs, idx, rdiag, rloc, hdxa, fcst, fcer, term, obsdep, stream=None
                            _dptr(rdiag), _dptr(rloc), nobs, _dptr(hdxa), _dptr(fcst), _dptr(fcer), _dptr(obsdep),
                            _dptr(djdy), _dptr(obsense), _stream(stream)), "letkf_efso")
     return djdy, obsense
+
+
+SPEEDY_ELEM = {"u": 2819, "v": 2820, "t": 3073, "q": 3330, "rh": 3331, "ps": 14593, "rain": 9999}
+
+
+def speedy_obsope(lat, sig, v3d, v2d, elem, rlon, rlat, rlev, odat, want_member_qc=False, stream=None):
+    """SPEEDY observation operator for all members (speedy/letkf/obsope.f90:
+    53-104 with phys2ijk / Trans_XtoY of speedy/common/common_obs_speedy.f90).
+    v3d: float64 view shaped [ne, 4, nlev, nlat, nlon] (u, v, t, q) whose two
+    last dims are contiguous and whose variable stride is nlev times the level
+    stride (a stack of grd files, or the analysis layout [4, nlev, ne, nij]
+    permuted); v2d: [ne, 2, nlat, nlon] (ps, rain) likewise.  lat [nlat], sig
+    [nlev], observations elem (int32 codes) / rlon / rlat / rlev / odat [nobs],
+    all on the device.  Returns (hx [nobs, ne], qc [nobs] int32) and, with
+    want_member_qc, qc per member [nobs, ne]."""
+    import torch
+
+    ne, nv3, nlev, nlat, nlon = v3d.shape
+    if nv3 != 4 or v2d.shape[0] != ne or v2d.shape[1] < 2 or tuple(v2d.shape[2:]) != (nlat, nlon):
+        raise ValueError("speedy_obsope: v3d [ne, 4, nlev, nlat, nlon] and v2d [ne, 2, nlat, nlon] expected")
+    for t, rs in ((v3d, v3d.stride(2)), (v2d, v2d.stride(1))):
+        if t.dtype != torch.float64 or t.stride(-1) != 1 or t.stride(-2) != nlon:
+            raise ValueError("speedy_obsope: float64 fields with contiguous (lat, lon) planes expected")
+    if v3d.stride(1) != nlev * v3d.stride(2):
+        raise ValueError("speedy_obsope: v3d variable stride must be nlev times its level stride")
+    nobs = elem.numel()
+    hx = torch.empty((nobs, ne), dtype=torch.float64, device=v3d.device)
+    qc = torch.empty(nobs, dtype=torch.int32, device=v3d.device)
+    qcm = torch.empty((nobs, ne), dtype=torch.int32, device=v3d.device) if want_member_qc else None
+    check(lib().letkf_speedy_obsope(nlon, nlat, nlev, ne, _dptr(lat), _dptr(sig), _viewptr(v3d), v3d.stride(0),
+                                    v3d.stride(2), _viewptr(v2d), v2d.stride(0), v2d.stride(1), nobs, _dptr(elem),
+                                    _dptr(rlon), _dptr(rlat), _dptr(rlev), _dptr(odat), _dptr(hx), _dptr(qcm),
+                                    _dptr(qc), _stream(stream)), "letkf_speedy_obsope")
+    return (hx, qc, qcm) if want_member_qc else (hx, qc)
 
 
 def exclusive_scan(counts, stream=None):

@@ -160,6 +160,73 @@ def speedy_case(seed=0, ne=40, nstations=600, nlon=96, nlat=48, nlev=7, sigma_ob
                 gues3d=gues3d, ne=ne, nlev=nlev, var_local=np.ones(7))
 
 
+def speedy_members(rng, ne, nlon=96, nlat=48, nlev=7):
+    """Member states on the SPEEDY grid in grd-file order: v3d [ne, 4, nlev,
+    nlat, nlon] (u, v m/s; t K, a troposphere-like profile crossing 0 C and
+    -15 C so every calc_rh branch is met; q kg/kg, positive) and v2d [ne, 2,
+    nlat, nlon] (ps Pa around 1e5, rain >= 0)."""
+    shape3 = (ne, nlev, nlat, nlon)
+    u = 10.0 * rng.standard_normal(shape3)
+    v = 10.0 * rng.standard_normal(shape3)
+    tprof = np.linspace(295.0, 215.0, nlev)[None, :, None, None]
+    t = tprof + 8.0 * rng.standard_normal(shape3)
+    qprof = np.geomspace(1.5e-2, 2.0e-5, nlev)[None, :, None, None]
+    q = qprof * rng.uniform(0.2, 1.2, shape3)
+    ps = 1.0e5 + 1.5e3 * rng.standard_normal((ne, nlat, nlon))
+    rain = np.maximum(rng.standard_normal((ne, nlat, nlon)), 0.0) * 1.0e-4
+    v3d = np.stack([u, v, t, q], axis=1)
+    v2d = np.stack([ps, rain], axis=1)
+    return np.ascontiguousarray(v3d), np.ascontiguousarray(v2d)
+
+
+def speedy_obs_records(rng, nobs, lon, lat, nlon=96, with_edges=True):
+    """Observation records (elem, rlon, rlat, rlev, odat) over the SPEEDY grid
+    for the observation operator: all seven element codes, levels from above
+    the model top to below the surface, and with_edges adds the corner cases
+    (longitude 0 / 360 / grid-aligned / negative, latitudes on the table, past
+    the outermost rows and at the poles, missing ps, non-positive levels and
+    an unknown element code)."""
+    codes = np.array([ID_U, ID_V, ID_T, ID_Q, ID_RH, ID_PS, ID_RAIN])
+    elem = codes[rng.integers(0, codes.size, nobs)]
+    rlon = rng.uniform(0.0, 360.0, nobs)
+    rlat = np.degrees(np.arcsin(rng.uniform(-1.0, 1.0, nobs)))
+    rlev = np.exp(rng.uniform(np.log(3.0e3), np.log(1.08e5), nobs))
+    odat = rng.standard_normal(nobs)
+    if with_edges:
+        m = min(nobs, 64)
+        pick = rng.choice(nobs, m, replace=False)
+        kinds = np.arange(m) % 12
+        for p, kd in zip(pick, kinds):
+            if kd == 0:
+                rlon[p] = 0.0
+            elif kd == 1:
+                rlon[p] = 360.0
+            elif kd == 2:
+                rlon[p] = 360.0 / nlon * rng.integers(0, nlon)
+            elif kd == 3:
+                rlon[p] = -rng.uniform(0.1, 10.0)
+            elif kd == 4:
+                rlat[p] = lat[rng.integers(0, lat.size)]
+            elif kd == 5:
+                rlat[p] = rng.choice([-90.0, 90.0, lat[0] - 0.5, lat[-1] + 0.5, lat[-1]])
+            elif kd == 6:
+                elem[p] = ID_PS
+                odat[p] = -999.0
+            elif kd == 7:
+                rlev[p] = rng.choice([0.0, -5.0])
+            elif kd == 8:
+                elem[p] = 1234
+            elif kd == 9:
+                elem[p] = rng.choice([ID_U, ID_V])
+                rlev[p] = 1.1e5
+            elif kd == 10:
+                elem[p] = rng.choice([ID_T, ID_Q, ID_RH])
+                rlev[p] = 1.1e5
+            else:
+                rlev[p] = 5.0e2
+    return elem.astype(np.int32), rlon, rlat, rlev, odat
+
+
 # --------------------------------------------------------------------- regional
 REGIONAL_P_TOP = 1.0e4
 REGIONAL_P_BOT = 1.0e5

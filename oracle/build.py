@@ -15,7 +15,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
-SOURCES = ["letkf_core.c", "obs_local.c", "sweep.c"]
+SOURCES = ["letkf_core.c", "obs_local.c", "sweep.c", "obs_operator.c"]
 
 
 def build(force: bool = False) -> str:

@@ -155,6 +155,15 @@ void oracle_efso(int ne, int npts, int nv, int nterm, const int64_t* offs, const
                  const double* rloc, const double* hdxa, const double* fcst, const double* fcer, const int* term,
                  int nobs, const double* obsdep, double* djdy, double* obsense);
 
+
+/* SPEEDY observation operator (speedy/letkf/obsope.f90:53-104 with phys2ijk,
+ * Trans_XtoY, calc_rh, itpl_2d/3d of speedy/common/common_obs_speedy.f90) */
+double oracle_speedy_calc_rh(double t, double q, double p);
+int oracle_speedy_obsope(int nlon, int nlat, int nlev, int ne, const double* lat, const double* sig,
+                         const double* v3d, int64_t v3d_mem, int64_t v3d_rec, const double* v2d, int64_t v2d_mem,
+                         int64_t v2d_rec, int nobs, const int* elem, const double* rlon, const double* rlat,
+                         const double* rlev, const double* odat, double* hx, int* qc_member, int* qc);
+
 #ifdef __cplusplus
 }
 #endif

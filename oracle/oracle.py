@@ -56,6 +56,12 @@ def lib():
         _lib.oracle_obs_analysis.argtypes = [C.c_int, pd, d, pd, C.c_int, d, pd]
         _lib.oracle_efso.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int64), pi, pd, pd, pd, pd,
                                      pd, pi, C.c_int, pd, pd, pd]
+        i64 = C.c_int64
+        _lib.oracle_speedy_calc_rh.restype = d
+        _lib.oracle_speedy_calc_rh.argtypes = [d, d, d]
+        _lib.oracle_speedy_obsope.restype = C.c_int
+        _lib.oracle_speedy_obsope.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, pd, pd, pd, i64, i64, pd, i64, i64,
+                                              C.c_int, pi, pd, pd, pd, pd, pd, pi, pi]
     return _lib
 
 
@@ -330,3 +336,27 @@ def efso(ne, offs, idx, rdiag, rloc, hdxa, fcst, fcer, term, obsdep):
                       _pi(np.ascontiguousarray(idx, dtype=np.int32)), _pd(_f64(rdiag)), _pd(_f64(rloc)), _pd(hdxa),
                       _pd(fcst), _pd(_f64(fcer)), _pi(term), nobs, _pd(_f64(obsdep)), _pd(djdy), _pd(obsense))
     return djdy, obsense
+
+
+def speedy_calc_rh(t, q, p):
+    """speedy/common/common_obs_speedy.f90:84-109."""
+    return lib().oracle_speedy_calc_rh(float(t), float(q), float(p))
+
+
+def speedy_obsope(lat, sig, v3d, v2d, elem, rlon, rlat, rlev, odat):
+    """SPEEDY H(x) for every member (speedy/letkf/obsope.f90:53-104).
+    v3d [ne, 4, nlev, nlat, nlon], v2d [ne, 2, nlat, nlon] (C order).
+    Returns (hx [nobs, ne], qc [nobs], qc_member [nobs, ne])."""
+    v3d = _f64(v3d)
+    v2d = _f64(v2d)
+    ne, _, nlev, nlat, nlon = v3d.shape
+    elem = np.ascontiguousarray(elem, dtype=np.int32)
+    nobs = elem.size
+    hx = np.zeros((nobs, ne))
+    qcm = np.zeros((nobs, ne), dtype=np.int32)
+    qc = np.zeros(nobs, dtype=np.int32)
+    nij = nlat * nlon
+    lib().oracle_speedy_obsope(nlon, nlat, nlev, ne, _pd(_f64(lat)), _pd(_f64(sig)), _pd(v3d), 4 * nlev * nij, nij,
+                               _pd(v2d), 2 * nij, nij, nobs, _pi(elem), _pd(_f64(rlon)), _pd(_f64(rlat)),
+                               _pd(_f64(rlev)), _pd(_f64(odat)), _pd(hx), _pi(qcm), _pi(qc))
+    return hx, qc, qcm
