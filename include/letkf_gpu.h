@@ -237,6 +237,29 @@ int letkf_speedy_obsope(int nlon, int nlat, int nlev, int ne, const double* lat,
                         const int* elem, const double* rlon, const double* rlat, const double* rlev,
                         const double* odat, double* hx, int* qc_member, int* qc, void* stream);
 
+/* SPEEDY grid-file records (speedy/common/common_speedy.f90:163-287): a file
+ * is nrec records of nij = nlon*nlat REAL(4) (u levels, v, t, q, ps, rain),
+ * big-endian as the reference's -byteswapio build writes them.  raw holds ne
+ * members' files back to back on the device (member m at m*nrec*nij floats,
+ * 4-byte aligned).  Decode: records r0..r0+nr-1 of every member -> out
+ * element (m, r, ij) at out[m*out_mem_stride + r*out_rec_stride + ij] (FP64
+ * when out_f64, else FP32), byte-swapping when byteswap; this is
+ * read_grd4 + the REAL(4) -> r_size widening of read_ens_mpi
+ * (speedy/common/common_mpi_speedy.f90:354-382).  Encode: the reverse, FP64
+ * rounded to nearest REAL(4) (write_ens_mpi, :386-414). */
+int letkf_grd_decode(int64_t nij, int nrec, int ne, const void* raw, int byteswap, int r0, int nr, int out_f64,
+                     void* out, int64_t out_mem_stride, int64_t out_rec_stride, void* stream);
+int letkf_grd_encode(int64_t nij, int nrec, int ne, const void* in, int in_f64, int64_t in_mem_stride,
+                     int64_t in_rec_stride, int r0, int nr, int byteswap, void* raw, void* stream);
+
+/* Ensemble mean and spread per (record, point) (ensmean_grd,
+ * speedy/common/common_speedy.f90:335-370; spread of write_ensmspr_mpi,
+ * speedy/common/common_mpi_speedy.f90:461-515): x(m, r, ij) at
+ * x[m*mem_stride + r*rec_stride + ij]; mean and sprd [nrec][nij] (either may
+ * be NULL), sums in member order, sprd = sqrt(sum (x - mean)^2 / (ne - 1)). */
+int letkf_ens_mean_spread(int64_t nij, int nrec, int ne, const double* x, int64_t mem_stride, int64_t rec_stride,
+                          double* mean, double* sprd, void* stream);
+
 /* Lorenz-96 selection (lorenz96/letkf/letkf.f90:220-254).  obs_cell[ny] is
  * the 1-based grid index of each observation (first maximum of its row of H,
  * see letkf_l96_obs_cell); pix[npts] are 1-based grid indices.  An

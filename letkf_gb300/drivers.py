@@ -4,12 +4,18 @@ the device path of this library (search -> gather -> batched core -> update).
 * ``l96_letkf``   -- lorenz96/letkf/letkf.f90:180-265 (one time slot)
 * ``speedy_letkf`` -- speedy/letkf/letkf_tools.f90:44-203 (das_letkf)
 * ``speedy_sort_obs`` -- speedy/letkf/letkf_obs.f90:243-313 (bucket sort)
+* ``speedy_obs_setup`` -- set_letkf_obs (speedy/letkf/letkf_obs.f90:48-313) with
+  H(x) of every member computed on the device (obsope.f90)
+* ``speedy_cycle`` -- the letkf program (speedy/letkf/letkf.f90) from member grd
+  files and an observation file to analysis files
 
 The regional SCALE-style driver is the resident ``sweep.Sweep`` handle.  All
 compute runs in libletkf_gpu.so; torch only holds device memory and does
 layout transposes.
 """
 from __future__ import annotations
+
+import os
 
 import numpy as np
 
@@ -138,6 +144,115 @@ def speedy_letkf(grid, obs, hdxf, dep, gues3d, logpfm, dlon_zero, params, var_lo
             xa2[n] = K.update_f64(xb2[n:n + 1], tr.contiguous(), None, stream)[0]
         anal2d = xa2.permute(0, 2, 1).contiguous()
     return anal3d, anal2d
+
+
+PI = 3.1415926535      # common/common.f90:28
+RE = 6371.3e3          # common/common.f90:35
+GROSS_ERROR = 10.0     # speedy/letkf/letkf_obs.f90:50
+
+
+def speedy_localization(lat, sigma_obs=1000.0e3, sigma_obsv=0.1, nlon=96):
+    """dist_zero, dist_zerov, dlat_zero and dlon_zero per grid point
+    (speedy/letkf/letkf_obs.f90:82-88); grid points are lon fastest."""
+    dist_zero = sigma_obs * np.sqrt(10.0 / 3.0) * 2.0
+    dist_zerov = sigma_obsv * np.sqrt(10.0 / 3.0) * 2.0
+    dlat_zero = dist_zero / PI / RE * 180.0
+    glat = np.repeat(np.asarray(lat, dtype=np.float64), nlon)
+    dlon_zero = dlat_zero / np.cos(PI * glat / 180.0)
+    return (dist_zero, dist_zerov, dlat_zero, sigma_obs, sigma_obsv), dlon_zero
+
+
+def speedy_obs_setup(lon, lat, sig, g3, g2, obs, gross_error=GROSS_ERROR, stream=None):
+    """set_letkf_obs (speedy/letkf/letkf_obs.f90:48-313) for one time slot with
+    H(x) computed on the device for every member (obsope.f90) instead of read
+    from per-member obs2 files: qc = min over members, member mean, hdxf = Hx
+    - mean, dep = y - mean, the gross-error check |dep| > 10 err, selection of
+    qc = 1 and the bucket sort.  obs: host dict elem, lon, lat, lev, dat, err
+    (SI units, as read_obs gives).  Returns (grid, obs_dev, hdxf, dep) ready
+    for ``speedy_letkf`` (all on the device) and the host qc before
+    selection."""
+    import torch
+
+    dev = g3.device
+    nv3d, nlev, ne, nij = g3.shape
+    nlon, nlat = len(lon), len(lat)
+    t = lambda a, dt=torch.float64: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
+    elem_i = (np.sign(obs["elem"]) * np.floor(np.abs(obs["elem"]) + 0.5)).astype(np.int32)
+    v3 = g3.reshape(nv3d, nlev, ne, nlat, nlon).permute(2, 0, 1, 3, 4)
+    v2 = g2.reshape(g2.shape[0], ne, nlat, nlon).permute(1, 0, 2, 3)
+    hx, qc = K.speedy_obsope(t(lat), t(sig), v3, v2, t(elem_i, torch.int32), t(obs["lon"]), t(obs["lat"]),
+                             t(obs["lev"]), t(obs["dat"]), stream=stream)
+    hdxf, dep, qc2 = K.obs_departure(hx, t(obs["dat"]), t(obs["err"]), gross_error, qc, stream)
+    qc_h = qc2.cpu().numpy()
+    keep = np.nonzero(qc_h == 1)[0]
+    perm, grd = speedy_sort_obs(lon, lat, obs["lon"][keep], obs["lat"][keep])
+    order = keep[perm]
+    idx = t(order, torch.int64)
+    obs_dev = {"elm": t(obs["elem"][order]), "lon": t(obs["lon"][order]), "lat": t(obs["lat"][order]),
+               "lev": t(obs["lev"][order]), "dat": t(obs["dat"][order]), "err": t(obs["err"][order])}
+    grid = {"lon": t(lon), "lat": t(lat), "nobsgrd": t(grd, torch.int32)}
+    return grid, obs_dev, hdxf.index_select(0, idx).contiguous(), dep.index_select(0, idx).contiguous(), qc_h
+
+
+def speedy_cycle(gues_paths, obs_path, anal_paths, lon, lat, sig, infl_path=None, cov_infl_mul=-1.01,
+                 sigma_obs=1000.0e3, sigma_obsv=0.1, var_local=None, gross_error=GROSS_ERROR, mean_spread_prefix=None,
+                 byteorder=">", device=None, stream=None):
+    """The SPEEDY letkf program (speedy/letkf/letkf.f90) on the device:
+    read_ens_mpi of the background members, set_letkf_obs with H(x) from the
+    device, write_ensmspr_mpi('gues'), das_letkf (speedy/letkf/letkf_tools.f90:
+    44-212, the inflation field from infl_mul.grd when cov_infl_mul < 0 and it
+    exists, else |cov_infl_mul|; written back when cov_infl_mul < 0),
+    write_ens_mpi('anal') and write_ensmspr_mpi('anal').  mean_spread_prefix
+    is a directory/name prefix for the gues/anal _me/_sp files (None: not
+    written).  Returns a summary dict."""
+    import torch
+
+    from . import speedy_io as IO
+
+    device = device or torch.device("cuda")
+    nlon, nlat, nlev = len(lon), len(lat), len(sig)
+    nij = nlon * nlat
+    g3, g2 = IO.load_ensemble(gues_paths, nlon, nlat, nlev, byteorder=byteorder, device=device, stream=stream)
+    nv3d, _, ne, _ = g3.shape
+    nv2d = g2.shape[0]
+    obs = IO.read_obs(obs_path, byteorder)
+    if mean_spread_prefix is not None:
+        IO.write_mean_spread(mean_spread_prefix + "gues", g3, g2, nlon, nlat, byteorder, stream)
+    if var_local is None:
+        var_local = np.ones((nv3d + nv2d, 7))
+    params, dlon_zero = speedy_localization(lat, sigma_obs, sigma_obsv, nlon)
+    nobs_used = 0
+    if obs["elem"].size:
+        grid, obs_dev, hdxf, dep, qc = speedy_obs_setup(lon, lat, sig, g3, g2, obs, gross_error, stream)
+        nobs_used = int(obs_dev["elm"].numel())
+    # multiplicative inflation (speedy/letkf/letkf_tools.f90:114-140)
+    if cov_infl_mul > 0.0:
+        infl3d = torch.full((nv3d, nlev, nij), cov_infl_mul, dtype=torch.float64, device=device)
+        infl3d[:, nlev - 1, :] = 1.01
+        infl2d = torch.full((nv2d, nij), cov_infl_mul, dtype=torch.float64, device=device)
+    elif infl_path is not None and os.path.exists(infl_path):
+        w3, w2 = IO.read_grd4(infl_path, nlon, nlat, nlev, nv3d, nv2d, byteorder)
+        infl3d = torch.as_tensor(w3.reshape(nv3d, nlev, nij).astype(np.float64), device=device)
+        infl2d = torch.as_tensor(w2.reshape(nv2d, nij).astype(np.float64), device=device)
+    else:
+        infl3d = torch.full((nv3d, nlev, nij), -cov_infl_mul, dtype=torch.float64, device=device)
+        infl2d = torch.full((nv2d, nij), -cov_infl_mul, dtype=torch.float64, device=device)
+    if nobs_used == 0:
+        a3, a2 = g3, g2                                    # no observation assimilated (:73-78)
+    else:
+        mean_ps = IO.mean_spread(g3, g2, stream)[1][0]      # ensemble-mean ps
+        sigt = torch.as_tensor(np.asarray(sig, dtype=np.float64), device=device)
+        logpfm = torch.log(mean_ps[None, :] * sigt[:, None]).contiguous()   # calc_pfull + DLOG (:143-145)
+        a3, a2 = speedy_letkf(grid, obs_dev, hdxf, dep, g3, logpfm, torch.as_tensor(dlon_zero, device=device),
+                              params, var_local, infl3d, g2, infl2d, stream=stream)
+    IO.store_ensemble(anal_paths, a3, a2, byteorder, stream)
+    if mean_spread_prefix is not None:
+        IO.write_mean_spread(mean_spread_prefix + "anal", a3, a2, nlon, nlat, byteorder, stream)
+    if cov_infl_mul < 0.0 and infl_path is not None:
+        IO.write_grd4(infl_path, infl3d.cpu().numpy().reshape(nv3d, nlev, nlat, nlon),
+                      infl2d.cpu().numpy().reshape(nv2d, nlat, nlon), byteorder)
+    return {"ne": ne, "nobs_input": int(obs["elem"].size), "nobs_assimilated": nobs_used,
+            "infl3d": infl3d, "infl2d": infl2d, "anal3d": a3, "anal2d": a2}
 
 
 # -------------------------------------------------------------------- Lorenz-96

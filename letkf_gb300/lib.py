@@ -61,6 +61,9 @@ _SIGS = {
     "letkf_update_mixed": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
     "letkf_obs_analysis": (_i, [_i, _i, _vp, _vp, _vp, _d, _vp, _d, _vp, _vp, _vp]),
     "letkf_efso": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "letkf_grd_decode": (_i, [_i64, _i, _i, _vp, _i, _i, _i, _i, _vp, _i64, _i64, _vp]),
+    "letkf_grd_encode": (_i, [_i64, _i, _i, _vp, _i, _i64, _i64, _i, _i, _i, _vp, _vp]),
+    "letkf_ens_mean_spread": (_i, [_i64, _i, _i, _vp, _i64, _i64, _vp, _vp, _vp]),
     "letkf_speedy_obsope": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _i64, _i64, _vp, _i64, _i64, _i, _vp, _vp, _vp, _vp,
                                  _vp, _vp, _vp, _vp, _vp]),
     "letkf_update_relax_f64": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
