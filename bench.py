@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--tc", type=int, default=1, choices=[0, 1],
                     help="1: Gram and Newton-Schulz on the tcgen05 tensor cores (ne <= 64)")
     ap.add_argument("--tc-ns", type=int, default=None, help="tensor-core Newton-Schulz iterations before the FP32 ones")
+    ap.add_argument("--tc-scaling", type=int, default=1, choices=[0, 1],
+                    help="1: spectrum-scaled tensor-core Newton-Schulz steps; 0: plain steps")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
     ap.add_argument("--no-largek", action="store_true", help="skip the large-ensemble measurement")
     ap.add_argument("--largek-points", type=int, default=4096, help="sampled points of the large-ensemble sweep")
@@ -381,7 +383,8 @@ def run_gpu(args, rank, world, dist):
     import torch
 
     from letkf_gb300 import lib as L
-    from letkf_gb300.sweep import OPT_EIGENSOLVER, OPT_TC_NS_ITERS, OPT_TENSOR_CORES, PREC_F64, PREC_MIXED, Sweep
+    from letkf_gb300.sweep import (OPT_EIGENSOLVER, OPT_TC_NS_ITERS, OPT_TC_NS_SCALING, OPT_TENSOR_CORES, PREC_F64,
+                                   PREC_MIXED, Sweep)
     from letkf_gb300.workload import RegionalWorkload
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
@@ -397,6 +400,7 @@ def run_gpu(args, rank, world, dist):
     sw.set_option(OPT_TENSOR_CORES, args.tc)
     if args.tc_ns is not None:
         sw.set_option(OPT_TC_NS_ITERS, args.tc_ns)
+    sw.set_option(OPT_TC_NS_SCALING, args.tc_scaling)
     sw.set_background_device(xb.data_ptr())
     infl0 = np.ones(wl.npts)
     sw.set_inflation(infl0)
@@ -455,6 +459,7 @@ def run_gpu(args, rank, world, dist):
     out["local_obs"] = {"min": int(nl.min()), "mean": float(nl.mean()), "p50": float(np.median(nl)),
                         "p99": float(np.percentile(nl, 99)), "max": int(nl.max()), "zero_frac": float((nl == 0).mean())}
     out["transform"] = {"method": args.eig, "tensor_cores": bool(args.tc and args.ne <= 64 and args.eig == "newton-schulz"),
+                        "scaled_steps": bool(args.tc_scaling),
                         "iterations_mean": float(dg["sweeps"][nobsl > 0].mean()) if (nobsl > 0).any() else 0.0,
                         "iterations_max": int(dg["sweeps"].max())}
     if args.no_extras:

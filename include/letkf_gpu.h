@@ -297,6 +297,7 @@ int letkf_l96_obs_cell(int nx, int ny, const double* h, int* cell, void* stream)
 #define LETKF_EIG_JACOBI 1        /*   eigen-decomposition by parallel Jacobi */
 #define LETKF_OPT_TENSOR_CORES 4  /* 1 (default): Gram and Newton-Schulz on tcgen05 for ne <= 64 */
 #define LETKF_OPT_TC_NS_ITERS 5   /* tensor-core Newton-Schulz iterations before the FP32 ones (default 14) */
+#define LETKF_OPT_TC_NS_SCALING 6 /* 1 (default): spectrum-scaled tensor-core Newton-Schulz steps; 0: plain */
 
 typedef struct letkf_sweep_desc {
   int ne;           /* ensemble size (MEMBER) */

@@ -142,6 +142,7 @@ struct letkf_sweep_s {
   int use_ns = 1;
   int use_tc = 1;
   int tc_ns_max = 14;
+  int tc_ns_scaled = 1;
 };
 
 // Stream-ordered allocation: no call of a handle synchronises the whole
@@ -424,6 +425,10 @@ int letkf_sweep_set_option(letkf_sweep_t h, int option, int value) {
       if (value < 0 || value > 64) return LETKF_ERR_ARG;
       h->tc_ns_max = value;
       return LETKF_OK;
+    case LETKF_OPT_TC_NS_SCALING:
+      if (value != 0 && value != 1) return LETKF_ERR_ARG;
+      h->tc_ns_scaled = value;
+      return LETKF_OK;
     case LETKF_OPT_EIGENSOLVER:
       if (value != LETKF_EIG_NEWTON_SCHULZ && value != LETKF_EIG_JACOBI) return LETKF_ERR_ARG;
       h->use_ns = value == LETKF_EIG_NEWTON_SCHULZ;
@@ -551,6 +556,7 @@ static int run_on(letkf_sweep_t h, cudaStream_t s) {
   a.use_ns = h->use_ns;
   a.err_flag = h->err_flag;
   a.tc_ns_max = h->tc_ns_max;
+  a.tc_ns_scaled = h->tc_ns_scaled;
   cudaMemsetAsync(h->counter, 0, sizeof(int), s);
   if (h->use_tc && h->use_ns && h->d.ne <= 64) {
     // tensor-core sweep, then the Jacobi pass over the points it deferred

@@ -38,6 +38,7 @@ struct SweepArgs {
   int* defer_count;
   int* err_flag;        // set when a bounded wait gave up
   int tc_ns_max;        // tensor-core Newton-Schulz iterations before the FP32 polish
+  int tc_ns_scaled;     // spectrum-scaled tensor-core steps (1) or plain ones (0)
 };
 
 }  // namespace letkf

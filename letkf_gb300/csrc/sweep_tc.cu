@@ -77,6 +77,21 @@ struct TcLayout {
   static constexpr int TOTAL = CTRL + 16;
 };
 
+// Newton-Schulz map of one eigenvalue of ZY, x (3 - x)^2 / 4
+__device__ __forceinline__ float f_ns(float x) {
+  const float t = 3.f - x;
+  return 0.25f * x * t * t;
+}
+
+// step scale a >= 1 for a spectrum in [lo, 1 + d], d = 0.02: f(a lo) = f(a (1 + d))
+__device__ __forceinline__ float ns_scale(float lo) {
+  const float d1 = 1.02f;
+  const float l = fminf(fmaxf(lo / d1, 0.f), 0.999f);
+  const float r = sqrtf(l);
+  const float al = 3.f * (1.f - r) / ((1.f - l * r) * d1);
+  return fmaxf(al, 1.f);
+}
+
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
   const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
   return *reinterpret_cast<const uint32_t*>(&v);
@@ -399,7 +414,19 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
         __syncthreads();
         const float coef = sqrtf((float)(n - 1) / s);
         // tensor-core phase: the iterations that move the small eigenvalues of
-        // ZY towards 1; stop once ||ZY - I||_F^2 < 1e-3 (or after TC_NS_MAX)
+        // ZY towards 1; stop once ||ZY - I||_F^2 < 1e-3 (or after TC_NS_MAX).
+        // Spectrum scaling: with X = ZY = (A/s) Z^2 and f(x) = x (3 - x)^2 / 4,
+        // the step S <- sqrt(a) S (3I - aX) / 2 maps every eigenvalue x of X to
+        // f(a x).  The first step is plain (a = 1; x <= gmax / s <= 2), which
+        // leaves the spectrum in [lo, 1]; later steps take the a that balances
+        // f(a lo) = f(a (1 + d)), a = 3 (1 - sqrt(l)) / (1 - l^1.5) / (1 + d)
+        // with l = lo / (1 + d), which multiplies the small eigenvalues by about
+        // 6.75 per step instead of 2.25.  lo starts from the diagonal shift
+        // (A >= c I; 0.9 c covers the Gram's rounding) and follows f; an
+        // eigenvalue below lo only converges later, and the margin d = 0.02
+        // keeps a x < 3 for the rounding of the 16-bit products.
+        float lo = 0.9f * cdiag * inv_s;
+        const float lo_top = f_ns(fminf(gmax * inv_s, 2.f));
         int it = 0;
         const int tc_max = a.tc_ns_max;
         for (bool done = tc_max <= 0; !done; it++) {
@@ -451,7 +478,19 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
             tmo = 1;
             break;
           }
-          // S <- 1.5 S - 0.5 S T (each thread rewrites only its own row)
+          // S <- sqrt(a) (1.5 S - 0.5 a S X) (each thread rewrites only its own row)
+          float ka = 1.5f, kb = 0.5f;
+          if (it == 0) {
+            lo = fminf(f_ns(lo), lo_top);
+          } else if (a.tc_ns_scaled) {
+            const float al = ns_scale(lo);
+            const float sa = sqrtf(al);
+            ka = 1.5f * sa;
+            kb = 0.5f * al * sa;
+            lo = f_ns(al * lo);
+          } else {
+            lo = f_ns(lo);
+          }
 #pragma unroll
           for (int c0 = 0; c0 < 64; c0 += 16) {
             float v[16];
@@ -463,7 +502,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
               unpack8(*reinterpret_cast<const uint4*>(sm + L::S_HI + off), sh);
               unpack8(*reinterpret_cast<const uint4*>(sm + L::S_LO + off), sl);
 #pragma unroll
-              for (int j = 0; j < 8; j++) sn[j] = 1.5f * (sh[j] + sl[j]) - 0.5f * v[8 * g + j];
+              for (int j = 0; j < 8; j++) sn[j] = ka * (sh[j] + sl[j]) - kb * v[8 * g + j];
               uint4 h, l;
               split8(sn, h, l);
               *reinterpret_cast<uint4*>(sm + L::S_HI + off) = h;

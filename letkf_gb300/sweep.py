@@ -24,6 +24,7 @@ EIG_NEWTON_SCHULZ = 0
 EIG_JACOBI = 1
 OPT_TENSOR_CORES = 4
 OPT_TC_NS_ITERS = 5
+OPT_TC_NS_SCALING = 6
 
 
 class SweepDesc(C.Structure):

@@ -33,11 +33,13 @@ def _spread(xb):
     return np.sqrt(((xb - xb.mean(-1, keepdims=True)) ** 2).sum(-1) / (xb.shape[-1] - 1)).mean()
 
 
-@pytest.mark.parametrize("ne,var_local,eig,tc", [(40, None, 0, 1), (64, [1.0, 0.5, 0.0], 0, 1), (20, None, 0, 1),
-                                               (64, None, 0, 0), (100, None, 0, 1), (64, None, 1, 1)])
-def test_mixed_sweep_against_oracle(cuda, ne, var_local, eig, tc):
-    """tc=1, eig=0 and ne <= 64 runs the tcgen05 sweep; otherwise the SIMT sweep."""
-    from letkf_gb300.sweep import OPT_EIGENSOLVER, OPT_TENSOR_CORES, PREC_MIXED, Sweep
+@pytest.mark.parametrize("ne,var_local,eig,tc,scaled", [(40, None, 0, 1, 1), (64, [1.0, 0.5, 0.0], 0, 1, 1),
+                                                      (20, None, 0, 1, 1), (64, None, 0, 1, 0), (64, None, 0, 0, 1),
+                                                      (100, None, 0, 1, 1), (64, None, 1, 1, 1)])
+def test_mixed_sweep_against_oracle(cuda, ne, var_local, eig, tc, scaled):
+    """tc=1, eig=0 and ne <= 64 runs the tcgen05 sweep (spectrum-scaled or
+    plain Newton-Schulz steps); otherwise the SIMT sweep."""
+    from letkf_gb300.sweep import OPT_EIGENSOLVER, OPT_TC_NS_SCALING, OPT_TENSOR_CORES, PREC_MIXED, Sweep
 
     case, prm, perm, grd, so, varloc, hdxf, dep = _setup(ne=ne, f32=True, var_local=var_local)
     xb = case["xb"].astype(np.float64)
@@ -52,6 +54,7 @@ def test_mixed_sweep_against_oracle(cuda, ne, var_local, eig, tc):
     np.testing.assert_array_equal(sw.nobsgrd(), grd)
     sw.set_option(OPT_EIGENSOLVER, eig)
     sw.set_option(OPT_TENSOR_CORES, tc)
+    sw.set_option(OPT_TC_NS_SCALING, scaled)
     sw.set_background(case["xb"])
     sw.set_inflation(infl0)
     sw.run()
