@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--tc-ns", type=int, default=None, help="tensor-core Newton-Schulz iterations before the FP32 ones")
     ap.add_argument("--tc-scaling", type=int, default=1, choices=[0, 1],
                     help="1: spectrum-scaled tensor-core Newton-Schulz steps; 0: plain steps")
+    ap.add_argument("--tc-tol", type=int, default=None, help="tensor-core phase exit at ||ZY-I||^2 < 10^-v")
+    ap.add_argument("--polish-tol", type=int, default=None, help="FP32 polish last step at ||ZAZ/s-I||^2 < 10^-v")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
     ap.add_argument("--no-largek", action="store_true", help="skip the large-ensemble measurement")
     ap.add_argument("--largek-points", type=int, default=4096, help="sampled points of the large-ensemble sweep")
@@ -383,8 +385,8 @@ def run_gpu(args, rank, world, dist):
     import torch
 
     from letkf_gb300 import lib as L
-    from letkf_gb300.sweep import (OPT_EIGENSOLVER, OPT_TC_NS_ITERS, OPT_TC_NS_SCALING, OPT_TENSOR_CORES, PREC_F64,
-                                   PREC_MIXED, Sweep)
+    from letkf_gb300.sweep import (OPT_EIGENSOLVER, OPT_POLISH_TOL, OPT_TC_NS_ITERS, OPT_TC_NS_SCALING, OPT_TC_NS_TOL,
+                                   OPT_TENSOR_CORES, PREC_F64, PREC_MIXED, Sweep)
     from letkf_gb300.workload import RegionalWorkload
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
@@ -401,6 +403,10 @@ def run_gpu(args, rank, world, dist):
     if args.tc_ns is not None:
         sw.set_option(OPT_TC_NS_ITERS, args.tc_ns)
     sw.set_option(OPT_TC_NS_SCALING, args.tc_scaling)
+    if args.tc_tol is not None:
+        sw.set_option(OPT_TC_NS_TOL, args.tc_tol)
+    if args.polish_tol is not None:
+        sw.set_option(OPT_POLISH_TOL, args.polish_tol)
     sw.set_background_device(xb.data_ptr())
     infl0 = np.ones(wl.npts)
     sw.set_inflation(infl0)

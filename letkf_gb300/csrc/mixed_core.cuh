@@ -381,7 +381,7 @@ __device__ int ns_iterate(float* Y, float* Z, float* T, float* redf, int max_ite
 // symmetrised.  Stops after the step following ||Q - I||_F < 1e-4 or after
 // max_iter; returns the iterations done.  P is scratch (NP x NP).
 template <int NP>
-__device__ int ns_polish(const float* As, float* Z, float* P, float* redf, int max_iter) {
+__device__ int ns_polish(const float* As, float* Z, float* P, float* redf, int max_iter, float tol = 1.0e-8f) {
   using C = MixedCfg<NP>;
   constexpr int NTI = NP / C::TR;
   const int tid = threadIdx.x;
@@ -411,7 +411,7 @@ __device__ int ns_polish(const float* As, float* Z, float* P, float* redf, int m
 #pragma unroll
       for (int b = 0; b < C::TC; b++) P[(i0 + a) * NP + j0 + b] = acc[a][b];
     e2 = block_sum<float, C::NT>(e2, redf);  // also publishes Q
-    if (e2 < 1.0e-8f) last = true;
+    if (e2 < tol) last = true;
     sym_gemm_tile<NP>(P, Z, i0, j0, acc);   // Q Z
 #pragma unroll
     for (int a = 0; a < C::TR; a++)

@@ -143,6 +143,8 @@ struct letkf_sweep_s {
   int use_tc = 1;
   int tc_ns_max = 14;
   int tc_ns_scaled = 1;
+  int tc_ns_tol_exp = 3;
+  int polish_tol_exp = 7;
 };
 
 // Stream-ordered allocation: no call of a handle synchronises the whole
@@ -429,6 +431,14 @@ int letkf_sweep_set_option(letkf_sweep_t h, int option, int value) {
       if (value != 0 && value != 1) return LETKF_ERR_ARG;
       h->tc_ns_scaled = value;
       return LETKF_OK;
+    case LETKF_OPT_TC_NS_TOL:
+      if (value < 1 || value > 7) return LETKF_ERR_ARG;
+      h->tc_ns_tol_exp = value;
+      return LETKF_OK;
+    case LETKF_OPT_POLISH_TOL:
+      if (value < 4 || value > 12) return LETKF_ERR_ARG;
+      h->polish_tol_exp = value;
+      return LETKF_OK;
     case LETKF_OPT_EIGENSOLVER:
       if (value != LETKF_EIG_NEWTON_SCHULZ && value != LETKF_EIG_JACOBI) return LETKF_ERR_ARG;
       h->use_ns = value == LETKF_EIG_NEWTON_SCHULZ;
@@ -557,6 +567,8 @@ static int run_on(letkf_sweep_t h, cudaStream_t s) {
   a.err_flag = h->err_flag;
   a.tc_ns_max = h->tc_ns_max;
   a.tc_ns_scaled = h->tc_ns_scaled;
+  a.tc_ns_tol = (float)std::pow(10.0, -h->tc_ns_tol_exp);
+  a.polish_tol = (float)std::pow(10.0, -h->polish_tol_exp);
   cudaMemsetAsync(h->counter, 0, sizeof(int), s);
   if (h->use_tc && h->use_ns && h->d.ne <= 64) {
     // tensor-core sweep, then the Jacobi pass over the points it deferred

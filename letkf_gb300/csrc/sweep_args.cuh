@@ -39,6 +39,8 @@ struct SweepArgs {
   int* err_flag;        // set when a bounded wait gave up
   int tc_ns_max;        // tensor-core Newton-Schulz iterations before the FP32 polish
   int tc_ns_scaled;     // spectrum-scaled tensor-core steps (1) or plain ones (0)
+  float tc_ns_tol;      // tensor-core phase ends once ||ZY - I||_F^2 < tc_ns_tol
+  float polish_tol;     // FP32 polish: last step once ||Z A Z / s - I||_F^2 < polish_tol
 };
 
 }  // namespace letkf

@@ -414,7 +414,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
         __syncthreads();
         const float coef = sqrtf((float)(n - 1) / s);
         // tensor-core phase: the iterations that move the small eigenvalues of
-        // ZY towards 1; stop once ||ZY - I||_F^2 < 1e-3 (or after TC_NS_MAX).
+        // ZY towards 1; stop once ||ZY - I||_F^2 < tc_ns_tol (or after TC_NS_MAX).
         // Spectrum scaling: with X = ZY = (A/s) Z^2 and f(x) = x (3 - x)^2 / 4,
         // the step S <- sqrt(a) S (3I - aX) / 2 maps every eigenvalue x of X to
         // f(a x).  The first step is plain (a = 1; x <= gmax / s <= 2), which
@@ -462,7 +462,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
           }
           tc::fence_before_sync();
           e2 = block_sum<float, TC_NT>(e2, red);
-          if (e2 < 1.0e-3f) done = true;
+          if (e2 < a.tc_ns_tol) done = true;
           tc::fence_smem_async();
           tc::fence_before_sync();
           __syncthreads();
@@ -562,7 +562,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
         }
         tc::fence_before_sync();
         __syncthreads();
-        it += ns_polish<TC_NP>(Af, Zf, Pf, red, tc_max > 0 ? TC_POLISH_MAX : a.max_ns_iter);
+        it += ns_polish<TC_NP>(Af, Zf, Pf, red, tc_max > 0 ? TC_POLISH_MAX : a.max_ns_iter, a.polish_tol);
         for (int idx = tid; idx < 64 * 64; idx += TC_NT) Wm[idx] = coef * Zf[idx];
         __syncthreads();
         if (tmo) break;

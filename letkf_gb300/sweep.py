@@ -25,6 +25,8 @@ EIG_JACOBI = 1
 OPT_TENSOR_CORES = 4
 OPT_TC_NS_ITERS = 5
 OPT_TC_NS_SCALING = 6
+OPT_TC_NS_TOL = 7
+OPT_POLISH_TOL = 8
 
 
 class SweepDesc(C.Structure):
