@@ -554,6 +554,7 @@ static int run_on(letkf_sweep_t h, cudaStream_t s) {
   a.prz = h->prz;
   a.plogr = h->plogr;
   a.xb = (const float*)h->xb;
+  a.xb_bulk = (h->d.ne % 4 == 0) && (reinterpret_cast<uintptr_t>(h->xb) % 16 == 0);
   a.xa = (float*)h->xa;
   a.infl = h->infl;
   a.nobsl_out = h->nobsl;

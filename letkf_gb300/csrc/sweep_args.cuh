@@ -23,6 +23,7 @@ struct SweepArgs {
   const double *pri, *prj, *prlev, *prz;
   const double* plogr;    // [npts] log(rlev)
   const float* xb;        // [nv][npts][n]
+  int xb_bulk;            // rows of xb may be fetched with TMA bulk copies (16-byte rows and base)
   float* xa;
   double* infl;           // [npts] in/out
   int* nobsl_out;         // [npts] or NULL

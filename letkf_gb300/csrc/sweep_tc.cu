@@ -71,8 +71,8 @@ struct TcLayout {
   static constexpr int ROWPRE = ROWIB + 4 * SW_MAXROWS;
   static constexpr int WCNT = ROWPRE + 4 * (SW_MAXROWS + 1);
   static constexpr int MEAN = ((WCNT + 4 * (TC_NT / 32 + 2)) + 7) & ~7;  // double[16]
-  static constexpr int MBAR = MEAN + 128;        // uint64[3]
-  static constexpr int TMEMH = MBAR + 24;        // uint32
+  static constexpr int MBAR = MEAN + 128;        // uint64[4]: Gram stages 0/1, products, background rows
+  static constexpr int TMEMH = MBAR + 32;        // uint32
   static constexpr int CTRL = TMEMH + 8;         // int[4]
   static constexpr int TOTAL = CTRL + 16;
 };
@@ -178,6 +178,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
     tc::mbar_init(&mbar[0], 1);
     tc::mbar_init(&mbar[1], 1);
     tc::mbar_init(&mbar[2], 1);
+    tc::mbar_init(&mbar[3], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (wid == 0) tc::tmem_alloc(tmem_holder, TC_TMEM_COLS);
@@ -188,7 +189,8 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
   const uint32_t D0 = tbase, D1 = tbase + 64;
   const uint32_t lane_off = (uint32_t)(wid * 32) << 16;
   const int r = tid;  // the tile row this thread owns in TMEM / S
-  uint32_t par[3] = {0u, 0u, 0u};
+  uint32_t par[4] = {0u, 0u, 0u, 0u};
+  bool xb_outst = false;  // a TMA copy of background rows is in flight
   bool outst[2] = {false, false};
   int tmo = 0;  // this thread saw a bounded wait give up
   const int npts_work = a.npts_dev ? *a.npts_dev : a.npts;
@@ -283,6 +285,20 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
     if (__syncthreads_or(tmo)) {
       tmo = 1;
       break;
+    }
+    // TMA: fetch this point's background rows (nv x n floats) into the
+    // search's pending-list area, which is free until the next point; the
+    // copy overlaps the transform and is consumed by the update
+    if (a.xb_bulk) {
+      tc::fence_smem_async();
+      __syncthreads();
+      if (tid == 0) {
+        const uint32_t row = (uint32_t)n * 4u;
+        tc::mbar_arrive_expect_tx(&mbar[3], row * (uint32_t)nv);
+        for (int v = 0; v < nv; v++)
+          tc::bulk_g2s(sbase + L::PIDX + v * row, a.xb + ((size_t)v * a.npts + pt) * n, row, &mbar[3]);
+      }
+      xb_outst = true;
     }
 
     double infl = a.infl[pt];
@@ -596,13 +612,27 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
     if (tid == 0 && a.nobsl_out) a.nobsl_out[pt] = Lp;
     if (deferred) {
       if (tid == 0) a.defer_list[atomicAdd(a.defer_count, 1)] = pt;
+      if (xb_outst) {
+        wait_bar(3);
+        xb_outst = false;
+      }
       continue;
     }
     __syncthreads();
     // ---- update: xa = mean + xp (W + wbar 1^T); FP64 mean and mean increment ----
-    for (int t = tid; t < nv * n; t += TC_NT) {
-      const int v = t / n, mm = t - v * n;
-      xs[v * 64 + mm] = a.xb[((size_t)v * a.npts + pt) * n + mm];
+    if (xb_outst) {
+      wait_bar(3);
+      xb_outst = false;
+      const float* xin = reinterpret_cast<const float*>(sm + L::PIDX);
+      for (int t = tid; t < nv * n; t += TC_NT) {
+        const int v = t / n, mm = t - v * n;
+        xs[v * 64 + mm] = xin[t];
+      }
+    } else {
+      for (int t = tid; t < nv * n; t += TC_NT) {
+        const int v = t / n, mm = t - v * n;
+        xs[v * 64 + mm] = a.xb[((size_t)v * a.npts + pt) * n + mm];
+      }
     }
     __syncthreads();
     for (int v = wid; v < nv; v += TC_NT / 32) {
@@ -630,6 +660,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
   // drain (bounded), report, release tensor memory
   for (int b = 0; b < 2; b++)
     if (outst[b]) wait_bar(b);
+  if (xb_outst) wait_bar(3);
   if (__syncthreads_or(tmo) && tid == 0 && a.err_flag) atomicExch(a.err_flag, 1);
   tc::fence_before_sync();
   __syncthreads();

@@ -34,11 +34,13 @@ def _spread(xb):
 
 
 @pytest.mark.parametrize("ne,var_local,eig,tc,scaled", [(40, None, 0, 1, 1), (64, [1.0, 0.5, 0.0], 0, 1, 1),
-                                                      (20, None, 0, 1, 1), (64, None, 0, 1, 0), (64, None, 0, 0, 1),
+                                                      (20, None, 0, 1, 1), (50, None, 0, 1, 1), (64, None, 0, 1, 0),
+                                                      (64, None, 0, 0, 1),
                                                       (100, None, 0, 1, 1), (64, None, 1, 1, 1)])
 def test_mixed_sweep_against_oracle(cuda, ne, var_local, eig, tc, scaled):
     """tc=1, eig=0 and ne <= 64 runs the tcgen05 sweep (spectrum-scaled or
-    plain Newton-Schulz steps); otherwise the SIMT sweep."""
+    plain Newton-Schulz steps; background rows by TMA bulk copy when ne is a
+    multiple of 4, by plain loads for ne = 50); otherwise the SIMT sweep."""
     from letkf_gb300.sweep import OPT_EIGENSOLVER, OPT_TC_NS_SCALING, OPT_TENSOR_CORES, PREC_MIXED, Sweep
 
     case, prm, perm, grd, so, varloc, hdxf, dep = _setup(ne=ne, f32=True, var_local=var_local)
