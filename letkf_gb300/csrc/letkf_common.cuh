@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "../../include/letkf_gpu.h"
 
 namespace letkf {
@@ -10,6 +12,19 @@ namespace letkf {
 // launch bookkeeping shared by every translation unit (defined in abi.cu)
 void note_launch();
 int cuda_status(cudaError_t e);
+
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) once per kernel and device:
+// later launches (including those recorded into a CUDA graph) skip the call.
+template <typename K>
+inline cudaError_t set_smem_once(K kern, size_t bytes, std::atomic<uint32_t>& done) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const uint32_t bit = 1u << (dev & 31);
+  if (done.load(std::memory_order_acquire) & bit) return cudaSuccess;
+  const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) done.fetch_or(bit, std::memory_order_release);
+  return e;
+}
 
 constexpr double kSigmaB = 0.04;  // common/common_letkf.f90:75 error stdev of parm_infl
 

@@ -22,6 +22,8 @@ struct SweepScaleParams;
 struct SweepArgs;
 int launch_sweep_mixed(const SweepArgs& a, cudaStream_t stream, int grid_cap);
 int launch_sweep_tc(const SweepArgs& a, cudaStream_t stream, int grid_cap);
+int prepare_sweep_mixed(int n);
+int prepare_sweep_tc();
 int launch_sweep_prep_obs(int, const double*, const double*, const double*, const double*, const double*,
                           const double*, const int*, const int*, const double*, const double*, float4*, float4*, int*,
                           cudaStream_t);
@@ -145,6 +147,12 @@ struct letkf_sweep_s {
   int tc_ns_scaled = 1;
   int tc_ns_tol_exp = 3;
   int polish_tol_exp = 7;
+  // CUDA graph of the mixed-form run: replayed while the kernel arguments,
+  // launch choices and stream stay the same, captured again otherwise
+  int use_graph = 1;
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<unsigned char> gkey;
+  int64_t glaunches = 0;  // kernels in the captured graph
 };
 
 // Stream-ordered allocation: no call of a handle synchronises the whole
@@ -232,6 +240,7 @@ int letkf_sweep_destroy(letkf_sweep_t h) {
     cudaStreamDestroy(h->stream);
   }
   if (h->ran) cudaEventDestroy(h->ran);
+  if (h->gexec) cudaGraphExecDestroy(h->gexec);
   delete h;
   return LETKF_OK;
 }
@@ -439,6 +448,10 @@ int letkf_sweep_set_option(letkf_sweep_t h, int option, int value) {
       if (value < 4 || value > 12) return LETKF_ERR_ARG;
       h->polish_tol_exp = value;
       return LETKF_OK;
+    case LETKF_OPT_GRAPH:
+      if (value != 0 && value != 1) return LETKF_ERR_ARG;
+      h->use_graph = value;
+      return LETKF_OK;
     case LETKF_OPT_EIGENSOLVER:
       if (value != LETKF_EIG_NEWTON_SCHULZ && value != LETKF_EIG_JACOBI) return LETKF_ERR_ARG;
       h->use_ns = value == LETKF_EIG_NEWTON_SCHULZ;
@@ -525,9 +538,7 @@ int letkf_sweep_run(letkf_sweep_t h, void* stream) {
   return st;
 }
 
-static int run_on(letkf_sweep_t h, cudaStream_t s) {
-  if (h->d.precision == LETKF_PREC_F64) return run_f64(h, s);
-  SweepArgs a;
+static void build_args(letkf_sweep_t h, SweepArgs& a) {
   memset(&a, 0, sizeof(a));
   a.n = h->d.ne;
   a.nv = h->d.nv;
@@ -570,11 +581,16 @@ static int run_on(letkf_sweep_t h, cudaStream_t s) {
   a.tc_ns_scaled = h->tc_ns_scaled;
   a.tc_ns_tol = (float)std::pow(10.0, -h->tc_ns_tol_exp);
   a.polish_tol = (float)std::pow(10.0, -h->polish_tol_exp);
+  a.defer_list = h->defer_list;  // read by the tensor-core sweep only
+  a.defer_count = h->defer_count;
+}
+
+static bool tc_path(letkf_sweep_t h) { return h->use_tc && h->use_ns && h->d.ne <= 64; }
+
+static int launch_mixed_run(letkf_sweep_t h, const SweepArgs& a, cudaStream_t s) {
   cudaMemsetAsync(h->counter, 0, sizeof(int), s);
-  if (h->use_tc && h->use_ns && h->d.ne <= 64) {
+  if (tc_path(h)) {
     // tensor-core sweep, then the Jacobi pass over the points it deferred
-    a.defer_list = h->defer_list;
-    a.defer_count = h->defer_count;
     cudaMemsetAsync(h->defer_count, 0, sizeof(int), s);
     int st = launch_sweep_tc(a, s, h->grid_cap);
     if (st != LETKF_OK) return st;
@@ -586,6 +602,53 @@ static int run_on(letkf_sweep_t h, cudaStream_t s) {
     return launch_sweep_mixed(b, s, h->grid_cap);
   }
   return launch_sweep_mixed(a, s, h->grid_cap);
+}
+
+static int run_on(letkf_sweep_t h, cudaStream_t s) {
+  if (h->d.precision == LETKF_PREC_F64) return run_f64(h, s);
+  SweepArgs a;
+  build_args(h, a);
+  if (!h->use_graph) return launch_mixed_run(h, a, s);
+  // key: kernel arguments, launch choices and stream
+  std::vector<unsigned char> key(sizeof(a) + 3 * sizeof(int) + sizeof(s));
+  unsigned char* k = key.data();
+  memcpy(k, &a, sizeof(a));
+  const int extra[3] = {h->grid_cap, h->use_tc, h->use_ns};
+  memcpy(k + sizeof(a), extra, sizeof(extra));
+  memcpy(k + sizeof(a) + sizeof(extra), &s, sizeof(s));
+  if (!h->gexec || key != h->gkey) {
+    if (h->gexec) {
+      cudaGraphExecDestroy(h->gexec);
+      h->gexec = nullptr;
+    }
+    // kernel attributes are set before the capture, not inside it
+    int st = tc_path(h) ? prepare_sweep_tc() : LETKF_OK;
+    if (st == LETKF_OK) st = prepare_sweep_mixed(h->d.ne);
+    if (st != LETKF_OK) return st;
+    const int64_t n0 = letkf_launch_count();
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_status(e);
+    st = launch_mixed_run(h, a, s);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(s, &g);
+    if (st == LETKF_OK && e != cudaSuccess) st = cuda_status(e);
+    if (st == LETKF_OK) {
+      e = cudaGraphInstantiate(&h->gexec, g, 0);
+      if (e != cudaSuccess) {
+        h->gexec = nullptr;
+        st = cuda_status(e);
+      }
+    }
+    if (g) cudaGraphDestroy(g);
+    if (st != LETKF_OK) return st;
+    h->gkey = key;
+    h->glaunches = letkf_launch_count() - n0;
+    const cudaError_t r = cudaGraphLaunch(h->gexec, s);
+    return cuda_status(r);
+  }
+  const cudaError_t r = cudaGraphLaunch(h->gexec, s);
+  for (int64_t i = 0; i < h->glaunches; i++) note_launch();
+  return cuda_status(r);
 }
 
 static int check_err(letkf_sweep_t h) {

@@ -370,10 +370,27 @@ __global__ void __launch_bounds__(MixedCfg<NP>::NT, MixedCfg<NP>::MINB) sweep_mi
 }
 
 template <int NP>
+static std::atomic<uint32_t>& mixed_attr() {
+  static std::atomic<uint32_t> done{0};
+  return done;
+}
+
+template <int NP>
+static int prepare_np() {
+  return cuda_status(set_smem_once(sweep_mixed_kernel<NP>, SweepSmem<NP>::BYTES, mixed_attr<NP>()));
+}
+
+int prepare_sweep_mixed(int n) {
+  if (n <= 32) return prepare_np<32>();
+  if (n <= 64) return prepare_np<64>();
+  return prepare_np<128>();
+}
+
+template <int NP>
 static int launch_sweep_np(const SweepArgs& a, cudaStream_t stream, int grid_cap) {
   auto kern = sweep_mixed_kernel<NP>;
   constexpr size_t bytes = SweepSmem<NP>::BYTES;
-  cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  cudaError_t err = set_smem_once(kern, bytes, mixed_attr<NP>());
   if (err != cudaSuccess) return cuda_status(err);
   int dev = 0, nsm = 0, per_sm = 0;
   cudaGetDevice(&dev);

@@ -670,11 +670,17 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
   }
 }
 
+static std::atomic<uint32_t> g_tc_attr{0};
+
+int prepare_sweep_tc() {
+  return cuda_status(set_smem_once(sweep_tc_kernel, TcLayout::TOTAL, g_tc_attr));
+}
+
 int launch_sweep_tc(const SweepArgs& a, cudaStream_t stream, int grid_cap) {
   if (a.n < 2 || a.n > TC_NP || a.nv < 1 || a.nv > 8) return LETKF_ERR_ARG;
   if (a.npts == 0) return LETKF_OK;
   constexpr size_t bytes = TcLayout::TOTAL;
-  cudaError_t err = cudaFuncSetAttribute(sweep_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  cudaError_t err = set_smem_once(sweep_tc_kernel, bytes, g_tc_attr);
   if (err != cudaSuccess) return cuda_status(err);
   int dev = 0, nsm = 0, per_sm = 0;
   cudaGetDevice(&dev);

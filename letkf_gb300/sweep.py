@@ -27,6 +27,7 @@ OPT_TC_NS_ITERS = 5
 OPT_TC_NS_SCALING = 6
 OPT_TC_NS_TOL = 7
 OPT_POLISH_TOL = 8
+OPT_GRAPH = 9
 
 
 class SweepDesc(C.Structure):

@@ -157,6 +157,56 @@ def test_tc_sweep_defers_points_to_the_jacobi_pass(cuda):
     assert np.abs(xa_tc[:, ok].astype(np.float64) - xa_j[:, ok]).max() < 1e-3 * spread
 
 
+@pytest.mark.parametrize("tc", [1, 0])
+def test_graph_replay_equals_eager_runs(cuda, tc):
+    """The mixed-form run as a CUDA graph: replays give the eager run's bits;
+    new background data is read by the replay; a new stream or a changed
+    option captures again."""
+    import torch
+
+    from letkf_gb300 import lib as L
+    from letkf_gb300.sweep import OPT_GRAPH, OPT_TENSOR_CORES, OPT_TC_NS_SCALING, PREC_MIXED, Sweep
+
+    case, prm, perm, grd, so, varloc, hdxf, dep = _setup(ne=64, f32=True)
+    npts = case["pri"].size
+    xb2 = (case["xb"] * 1.01 + 0.1).astype(np.float32)
+
+    def make(graph):
+        sw = Sweep(64, case["nvar"], case["nlon"], case["nlat"], npts, prm, precision=PREC_MIXED)
+        sw.set_points(case["pri"], case["prj"], case["prlev"])
+        sw.set_obs(case["ri"], case["rj"], case["lev"], case["dat"], case["err"], dep, case["cls"],
+                   hdxf.astype(np.float32))
+        sw.set_option(OPT_TENSOR_CORES, tc)
+        sw.set_option(OPT_GRAPH, graph)
+        return sw
+
+    def run(sw, xb, stream=None):
+        sw.set_background(xb)
+        sw.set_inflation(np.full(npts, 1.05))
+        sw.run(stream)
+        torch.cuda.synchronize()
+        return sw.analysis().copy(), sw.diagnostics()["infl"].copy()
+
+    ref = make(0)
+    e1, i1 = run(ref, case["xb"])
+    e2, i2 = run(ref, xb2)
+    ref.close()
+    sw = make(1)
+    st = torch.cuda.Stream()
+    n0 = L.launch_count()
+    for xb, (e, i) in ((case["xb"], (e1, i1)), (case["xb"], (e1, i1)), (xb2, (e2, i2))):
+        g, gi = run(sw, xb, st.cuda_stream)
+        np.testing.assert_array_equal(g, e)
+        np.testing.assert_array_equal(gi, i)
+    assert L.launch_count() - n0 == 3 * (2 if tc else 1)      # replays count their kernels
+    g, _ = run(sw, case["xb"])                                 # the handle's own stream: a new capture
+    np.testing.assert_array_equal(g, e1)
+    sw.set_option(OPT_TC_NS_SCALING, 0)                        # new kernel arguments: a new capture
+    g, _ = run(sw, case["xb"], st.cuda_stream)
+    assert np.abs(g.astype(np.float64) - e1).max() < 1e-3 * _spread(case["xb"].astype(np.float64))
+    sw.close()
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_tile_handles_reproduce_the_single_domain_sweep(cuda, precision):
     """The multi-GPU decomposition on one device: one handle per tile (its
