@@ -67,6 +67,8 @@ def parse():
                     help="1: spectrum-scaled tensor-core Newton-Schulz steps; 0: plain steps")
     ap.add_argument("--tc-tol", type=int, default=None, help="tensor-core phase exit at ||ZY-I||^2 < 10^-v")
     ap.add_argument("--polish-tol", type=int, default=None, help="FP32 polish last step at ||ZAZ/s-I||^2 < 10^-v")
+    ap.add_argument("--tune-points", type=int, default=32768,
+                    help="run the autotuner on this many points before timing (0: the options given)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
     ap.add_argument("--no-largek", action="store_true", help="skip the large-ensemble measurement")
     ap.add_argument("--largek-points", type=int, default=4096, help="sampled points of the large-ensemble sweep")
@@ -410,6 +412,7 @@ def run_gpu(args, rank, world, dist):
     sw.set_background_device(xb.data_ptr())
     infl0 = np.ones(wl.npts)
     sw.set_inflation(infl0)
+    tuned = sw.autotune(args.tune_points) if args.tune_points > 0 else None
     stream = torch.cuda.Stream(device=dev)
     for _ in range(args.warmup):
         sw.run(stream.cuda_stream)
@@ -442,6 +445,8 @@ def run_gpu(args, rank, world, dist):
            "config": config_block(args, wl), "gpu_launches": int(launches), "clocks": clk.summary()}
     # roofline of the dominant kernel (the deferred-point pass is < 0.01 % of the step)
     tc_on = bool(args.tc and args.ne <= 64 and args.eig == "newton-schulz")
+    if tuned is not None:
+        tc_on = tuned["tensor_cores"]
     kernel = "sweep_tc_kernel" if tc_on else f"sweep_mixed_kernel<{64 if args.ne <= 64 else 128}>"
     peaks, src = measured_peaks()
     flops = algorithmic_flops(nobsl, args.ne, args.nv)
@@ -465,7 +470,7 @@ def run_gpu(args, rank, world, dist):
     out["local_obs"] = {"min": int(nl.min()), "mean": float(nl.mean()), "p50": float(np.median(nl)),
                         "p99": float(np.percentile(nl, 99)), "max": int(nl.max()), "zero_frac": float((nl == 0).mean())}
     out["transform"] = {"method": args.eig, "tensor_cores": bool(args.tc and args.ne <= 64 and args.eig == "newton-schulz"),
-                        "scaled_steps": bool(args.tc_scaling),
+                        "scaled_steps": bool(args.tc_scaling), "autotune": tuned,
                         "iterations_mean": float(dg["sweeps"][nobsl > 0].mean()) if (nobsl > 0).any() else 0.0,
                         "iterations_max": int(dg["sweeps"].max())}
     if args.no_extras:

@@ -335,6 +335,16 @@ int letkf_sweep_set_inflation(letkf_sweep_t h, const double* infl, int on_device
 int letkf_sweep_set_option(letkf_sweep_t h, int option, int value);
 /* analyse every point; asynchronous on `stream` (NULL: the handle's stream) */
 int letkf_sweep_run(letkf_sweep_t h, void* stream);
+/* Autotuner of the mixed form: times every kernel / eigensolver variant the
+ * handle can run (tensor-core sweep with spectrum-scaled or plain
+ * Newton-Schulz steps when ne <= 64; SIMT sweep with Newton-Schulz or
+ * parallel Jacobi) on the first `sample_points` points of the processing
+ * order, with the points, observations and background already set, and
+ * keeps the fastest.  The inflation field is restored afterwards; the
+ * analysis buffer is overwritten.  choice[4] (may be NULL) receives
+ * {tensor cores, Newton-Schulz (0: Jacobi), scaled steps, microseconds per
+ * 1000 points of the winner}.  The plain form has nothing to tune. */
+int letkf_sweep_autotune(letkf_sweep_t h, int sample_points, int* choice);
 int letkf_sweep_get_analysis(letkf_sweep_t h, void* xa, int on_device);
 /* per-point updated inflation, local obs count, status and Jacobi sweeps (any may be NULL) */
 int letkf_sweep_get_diagnostics(letkf_sweep_t h, double* infl, int* nobsl, int* status, int* sweeps);

@@ -520,6 +520,7 @@ static int run_f64(letkf_sweep_t h, cudaStream_t s) {
 }
 
 static int run_on(letkf_sweep_t h, cudaStream_t s);
+static int check_err(letkf_sweep_t h);
 
 int letkf_sweep_run(letkf_sweep_t h, void* stream) {
   if (!h) return LETKF_ERR_ARG;
@@ -649,6 +650,84 @@ static int run_on(letkf_sweep_t h, cudaStream_t s) {
   const cudaError_t r = cudaGraphLaunch(h->gexec, s);
   for (int64_t i = 0; i < h->glaunches; i++) note_launch();
   return cuda_status(r);
+}
+
+int letkf_sweep_autotune(letkf_sweep_t h, int sample_points, int* choice) {
+  if (!h || sample_points < 1) return LETKF_ERR_ARG;
+  if (h->d.precision == LETKF_PREC_F64 || h->d.npts == 0) {
+    if (choice) {
+      choice[0] = 0;
+      choice[1] = 0;
+      choice[2] = 0;
+      choice[3] = 0;
+    }
+    return LETKF_OK;
+  }
+  cudaStream_t s = h->stream;
+  const size_t np = (size_t)h->d.npts;
+  const int sample = sample_points < h->d.npts ? sample_points : h->d.npts;
+  double* keep = nullptr;
+  if (dalloc(&keep, np, s) != LETKF_OK) return LETKF_ERR_CUDA;
+  cudaMemcpyAsync(keep, h->infl, np * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  struct Cand {
+    int tc, ns, scaled;
+  };
+  std::vector<Cand> cands;
+  if (h->d.ne <= 64) {
+    cands.push_back({1, 1, 1});
+    cands.push_back({1, 1, 0});
+  }
+  cands.push_back({0, 1, 1});
+  cands.push_back({0, 0, 1});
+  const Cand was = {h->use_tc, h->use_ns, h->tc_ns_scaled};
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int st = LETKF_OK, best = -1;
+  float best_ms = 0.f;
+  for (size_t c = 0; c < cands.size() && st == LETKF_OK; c++) {
+    h->use_tc = cands[c].tc;
+    h->use_ns = cands[c].ns;
+    h->tc_ns_scaled = cands[c].scaled;
+    SweepArgs a;
+    build_args(h, a);
+    a.npts = sample;  // the first `sample` points of the processing order
+    float ms = 0.f;
+    for (int rep = 0; rep < 2 && st == LETKF_OK; rep++) {  // warm-up, then timed
+      cudaMemcpyAsync(h->infl, keep, np * sizeof(double), cudaMemcpyDeviceToDevice, s);
+      cudaEventRecord(e0, s);
+      st = launch_mixed_run(h, a, s);
+      cudaEventRecord(e1, s);
+      if (st == LETKF_OK) st = cuda_status(cudaEventSynchronize(e1));
+      if (st == LETKF_OK) st = cuda_status(cudaEventElapsedTime(&ms, e0, e1));
+    }
+    if (st == LETKF_OK && (best < 0 || ms < best_ms)) {
+      best = (int)c;
+      best_ms = ms;
+    }
+  }
+  cudaMemcpyAsync(h->infl, keep, np * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  dfree(keep, s);
+  const int st2 = cuda_status(cudaStreamSynchronize(s));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st == LETKF_OK) st = st2;
+  if (st == LETKF_OK) st = check_err(h);
+  const Cand pick = (st == LETKF_OK && best >= 0) ? cands[best] : was;
+  h->use_tc = pick.tc;
+  h->use_ns = pick.ns;
+  h->tc_ns_scaled = pick.scaled;
+  if (h->gexec) {
+    cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+  }
+  if (choice) {
+    choice[0] = pick.tc;
+    choice[1] = pick.ns;
+    choice[2] = pick.scaled;
+    choice[3] = best >= 0 ? (int)(1e3f * best_ms * 1000.f / (float)sample) : 0;
+  }
+  return st;
 }
 
 static int check_err(letkf_sweep_t h) {

@@ -44,6 +44,7 @@ _SIGS = {
     "letkf_sweep_set_inflation": [C.c_void_p, C.c_void_p, C.c_int],
     "letkf_sweep_set_option": [C.c_void_p, C.c_int, C.c_int],
     "letkf_sweep_run": [C.c_void_p, C.c_void_p],
+    "letkf_sweep_autotune": [C.c_void_p, C.c_int, C.c_void_p],
     "letkf_sweep_get_analysis": [C.c_void_p, C.c_void_p, C.c_int],
     "letkf_sweep_get_diagnostics": [C.c_void_p] * 5,
     "letkf_sweep_sorted_obs": [C.c_void_p, C.c_void_p],
@@ -126,6 +127,16 @@ class Sweep:
     def run(self, stream=None):
         s = None if stream is None else C.c_void_p(stream)
         check(_L().letkf_sweep_run(self.h, s), "letkf_sweep_run")
+
+    def autotune(self, sample_points=32768):
+        """Time the kernel / eigensolver variants on the first sample_points
+        points (letkf_sweep_autotune) and keep the fastest; returns the
+        choice as a dict.  Points, observations and background must be set;
+        the inflation field is restored."""
+        ch = np.zeros(4, dtype=np.int32)
+        check(_L().letkf_sweep_autotune(self.h, int(sample_points), _p(ch)), "letkf_sweep_autotune")
+        return {"tensor_cores": bool(ch[0]), "eigensolver": "newton-schulz" if ch[1] else "jacobi",
+                "scaled_steps": bool(ch[2]), "us_per_1000_points": int(ch[3])}
 
     def analysis(self):
         d = self.desc

@@ -207,6 +207,39 @@ def test_graph_replay_equals_eager_runs(cuda, tc):
     sw.close()
 
 
+@pytest.mark.parametrize("ne", [40, 100])
+def test_autotune_keeps_inflation_and_picks_a_valid_variant(cuda, ne):
+    """letkf_sweep_autotune times the variants on a sample of points, keeps
+    the fastest and restores the inflation field; the tuned run still meets
+    the mixed-form bar against the oracle."""
+    from letkf_gb300.sweep import PREC_MIXED, Sweep
+
+    case, prm, perm, grd, so, varloc, hdxf, dep = _setup(ne=ne, f32=True)
+    xb = case["xb"].astype(np.float64)
+    npts = case["pri"].size
+    infl0 = np.linspace(1.0, 1.2, npts)
+    xa_ref, infl_ref, nl_ref = so.sweep(hdxf[perm], dep[perm], xb, case["pri"], case["prj"], case["prlev"], infl0)
+    sw = Sweep(ne, case["nvar"], case["nlon"], case["nlat"], npts, prm, precision=PREC_MIXED)
+    sw.set_points(case["pri"], case["prj"], case["prlev"])
+    sw.set_obs(case["ri"], case["rj"], case["lev"], case["dat"], case["err"], dep, case["cls"],
+               hdxf.astype(np.float32))
+    sw.set_background(case["xb"])
+    sw.set_inflation(infl0)
+    choice = sw.autotune(sample_points=npts // 2)
+    assert choice["us_per_1000_points"] > 0
+    if ne > 64:
+        assert not choice["tensor_cores"]
+    np.testing.assert_array_equal(sw.diagnostics()["infl"], infl0)
+    sw.run()
+    xa = sw.analysis().astype(np.float64)
+    dg = sw.diagnostics()
+    sw.close()
+    np.testing.assert_array_equal(dg["nobsl"], nl_ref)
+    spread = _spread(xb)
+    em = np.sqrt(np.mean((xa.mean(-1) - xa_ref.mean(-1)) ** 2)) / spread
+    assert em < 1e-4, f"analysis-mean error {em:.2e} of spread after autotune ({choice})"
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_tile_handles_reproduce_the_single_domain_sweep(cuda, precision):
     """The multi-GPU decomposition on one device: one handle per tile (its
