@@ -5,7 +5,9 @@
 //    transform (T + wbar 1^T, RTPP applied as weight_RTPP does, :959-970),
 //    obsanal(n, m) = ybar(n) + sum_k obshdxf(n, k) trans(k, m), ybar =
 //    obsdat - obsdep, the mean in member order, the q "no update" branch and
-//    the relative-spread clip.
+//    the relative-spread clip.  The k sum runs over the lanes of a warp
+//    (coalesced reads of column m of trans), so it differs from the serial
+//    sum by rounding.
 //  * letkf_efso: observation sensitivity (gfs/letkf/letkf_tools.f90:547-679)
 //    over grid points with their local observation lists.
 #include "letkf_common.cuh"
@@ -32,22 +34,25 @@ __global__ void __launch_bounds__(OSA_NT) obs_analysis_kernel(int ne, int n, con
     const int md = mode ? mode[p] : 0;
     const double yb = ybar[p];
     const double* tp = trans + (size_t)p * ne * ne;
-    for (int m = tid; m < ne; m += OSA_NT) {
+    // one warp per member m, the lanes over k: column m of trans is contiguous
+    const int lane = tid & 31, wid = tid >> 5;
+    for (int m = wid; m < ne; m += OSA_NT / 32) {
       double v;
       if (md == 1) {
         v = yb + h[m];
       } else {
-        v = yb;
-        for (int k = 0; k < ne; k++) {
+        double part = 0.0;
+        for (int k = lane; k < ne; k += 32) {
           double w = tp[(size_t)m * ne + k];
           if (alpha != 0.0) {
             w = (1.0 - alpha) * w;
             if (k == m) w = w + alpha;
           }
-          v = v + h[k] * w;
+          part = fma(h[k], w, part);
         }
+        v = yb + warp_sum(part);
       }
-      a[m] = v;
+      if (lane == 0) a[m] = v;
     }
     __syncthreads();
     if (tid == 0) {
@@ -102,12 +107,12 @@ __global__ void __launch_bounds__(OSA_NT) efso_djdy_kernel(int ne, int npts, int
     __syncthreads();
     for (int64_t l = l0 + tid; l < l1; l += OSA_NT) {
       const int ob = idx[l];
-      const double rd = rdiag[l], rl = rloc[l];
+      const double rinv = 1.0 / rdiag[l], rl = rloc[l];  // one division per observation, not per member
       double acc[EFSO_MAX_TERM];
 #pragma unroll
       for (int t = 0; t < EFSO_MAX_TERM; t++) acc[t] = 0.0;
       for (int m = 0; m < ne; m++) {
-        const double hr = hdxa[(size_t)ob * ne + m] / rd * rl;
+        const double hr = hdxa[(size_t)ob * ne + m] * rinv * rl;
 #pragma unroll
         for (int t = 0; t < EFSO_MAX_TERM; t++)
           if (t < nterm) acc[t] = acc[t] + w1[t * ne + m] * hr;

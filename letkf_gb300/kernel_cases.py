@@ -15,6 +15,14 @@ where the kernel streams the ensemble):
   relax         RTPS update with relax_beta weights of 50,000 points, k = 64
   largek        large-ensemble core of 512 points, k = 512, 100-900 local obs
                 each, and the FP32 update of 6 variables
+  speedy_io     80 SPEEDY T63 member files (192x96, 7 levels, 30 records;
+                177 MB of file bytes) decoded to FP64, ensemble mean and
+                spread, encoded back
+  obsope        SPEEDY observation operator on those 80 members (354 MB in
+                FP64) for 300,000 observations of all seven elements
+  obs_space     obs-space analysis of 20,000 observation locations (k = 64,
+                655 MB of transforms) and EFSO over 50,000 points with 50
+                local observations each
 Used for the ncu summaries under profiles/; prints one line per case.
 """
 from __future__ import annotations
@@ -144,8 +152,89 @@ def case_largek(dev):
     return f"{npts} points (k = {ne}, mean L = {Ls.mean():.0f}), {dt * 1e3:.1f} ms, {npts / dt:.0f} points/s, {ok} ok"
 
 
+def _speedy_members(dev, ne=80, nlon=192, nlat=96, nlev=7):
+    import torch
+
+    from . import synthetic as S
+
+    rng = np.random.default_rng(8)
+    lon, lat = S.speedy_grid(nlon, nlat)
+    v3d, v2d = S.speedy_members(rng, ne, nlon, nlat, nlev)
+    return rng, lon, lat, torch.as_tensor(v3d, device=dev), torch.as_tensor(v2d, device=dev)
+
+
+def case_speedy_io(dev):
+    import torch
+
+    from . import speedy_io as IO
+
+    ne, nlon, nlat, nlev = 80, 192, 96, 7
+    rng = np.random.default_rng(9)
+    raw = torch.as_tensor(rng.standard_normal(ne * IO.grd_nrec(nlev) * nlat * nlon).astype(">f4").view(np.uint8),
+                          device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g3, g2 = IO.decode_members(raw, ne, nlon, nlat, nlev)
+    IO.mean_spread(g3, g2)
+    back = IO.encode_members(g3, g2)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    assert torch.equal(back, raw)
+    return f"{ne} members x {raw.numel() // ne} bytes, {dt * 1e3:.1f} ms"
+
+
+def case_obsope(dev):
+    import torch
+
+    from . import synthetic as S
+    from .core import speedy_obsope
+
+    rng, lon, lat, v3d, v2d = _speedy_members(dev)
+    el, lo, la, lv, od = S.speedy_obs_records(rng, 300_000, lon, lat, 192, with_edges=False)
+    t = lambda a, dt=torch.float64: torch.as_tensor(a, dtype=dt, device=dev)
+    args = (t(lat), t(S.SPEEDY_SIG), v3d, v2d, t(el, torch.int32), t(lo), t(la), t(lv), t(od))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hx, qc = speedy_obsope(*args)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    return f"{el.size} obs x {v3d.shape[0]} members, {dt * 1e3:.1f} ms, qc {float(qc.float().mean()):.2f}"
+
+
+def case_obs_space(dev):
+    import torch
+
+    from .core import efso, obs_analysis
+
+    rng = np.random.default_rng(10)
+    ne, n = 64, 20_000
+    trans = torch.randn((n, ne, ne), dtype=torch.float64, device=dev) * 0.1
+    hdxf = torch.randn((n, ne), dtype=torch.float64, device=dev)
+    ybar = torch.randn(n, dtype=torch.float64, device=dev)
+    mode = torch.as_tensor(rng.integers(0, 3, n), dtype=torch.int32, device=dev)
+    npts, nobs, nv = 50_000, 100_000, 6
+    offs = torch.arange(0, 50 * (npts + 1), 50, dtype=torch.int64, device=dev)
+    idx = torch.as_tensor(rng.integers(0, nobs, 50 * npts), dtype=torch.int32, device=dev)
+    rd = torch.rand(50 * npts, dtype=torch.float64, device=dev) + 0.5
+    rl = torch.rand(50 * npts, dtype=torch.float64, device=dev)
+    hdxa = torch.randn((nobs, ne), dtype=torch.float64, device=dev)
+    fcst = torch.randn((nv, npts, ne), dtype=torch.float64, device=dev)
+    fcer = torch.randn((nv, npts), dtype=torch.float64, device=dev)
+    obsdep = torch.randn(nobs, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    obs_analysis(trans, ybar, hdxf, 0.5, mode, 0.05)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    efso(ne, offs, idx, rd, rl, hdxa, fcst, fcer, [0, 0, 1, 2, -1, -1], obsdep)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    return f"obs_analysis {n} obs {1e3 * (t1 - t0):.1f} ms; efso {npts} points {1e3 * (t2 - t1):.1f} ms"
+
+
 CASES = {"sweep_tc": lambda d: case_sweep(d, True), "sweep_simt": lambda d: case_sweep(d, False),
-         "f64": case_f64, "l96": case_l96, "relax": case_relax, "largek": case_largek}
+         "f64": case_f64, "l96": case_l96, "relax": case_relax, "largek": case_largek,
+         "speedy_io": case_speedy_io, "obsope": case_obsope, "obs_space": case_obs_space}
 
 
 def main():

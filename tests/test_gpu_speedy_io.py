@@ -15,12 +15,13 @@ def _members(rng, ne, nlon, nlat, nlev):
     return rng.standard_normal((ne, IO.grd_nrec(nlev), nlat, nlon)).astype(np.float32) * 100.0
 
 
-@pytest.mark.parametrize("bo", [">", "<"])
-def test_decode_into_analysis_layout(cuda, bo):
+@pytest.mark.parametrize("bo,nlon,nlat", [(">", 96, 48), ("<", 96, 48), (">", 15, 7)])
+def test_decode_into_analysis_layout(cuda, bo, nlon, nlat):
+    """96 x 48 takes the 16-byte path, 15 x 7 (odd rows) the 4-byte one."""
     import torch
 
     rng = np.random.default_rng(1)
-    ne, nlon, nlat, nlev = 5, 96, 48, 7
+    ne, nlev = 5, 7
     x = _members(rng, ne, nlon, nlat, nlev)
     raw = torch.as_tensor(np.frombuffer(x.astype(bo + "f4").tobytes(), dtype=np.uint8).copy(), device=cuda)
     g3, g2 = IO.decode_members(raw, ne, nlon, nlat, nlev, byteorder=bo)
@@ -34,12 +35,12 @@ def test_decode_into_analysis_layout(cuda, bo):
     assert np.array_equal(f2.cpu().numpy(), want2.astype(np.float32))
 
 
-@pytest.mark.parametrize("bo", [">", "<"])
-def test_encode_rounds_to_real4(cuda, bo):
+@pytest.mark.parametrize("bo,nlon,nlat", [(">", 16, 8), ("<", 16, 8), (">", 15, 7)])
+def test_encode_rounds_to_real4(cuda, bo, nlon, nlat):
     import torch
 
     rng = np.random.default_rng(2)
-    ne, nlon, nlat, nlev = 3, 16, 8, 7
+    ne, nlev = 3, 7
     nij = nlon * nlat
     g3 = rng.standard_normal((4, nlev, ne, nij)) * 1e3
     g2 = rng.standard_normal((2, ne, nij)) * 1e5
