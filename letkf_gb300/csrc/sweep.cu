@@ -147,6 +147,7 @@ struct letkf_sweep_s {
   int tc_ns_scaled = 1;
   int tc_ns_tol_exp = 3;
   int polish_tol_exp = 7;
+  int tc_polish = 0;
   // CUDA graph of the mixed-form run: replayed while the kernel arguments,
   // launch choices and stream stay the same, captured again otherwise
   int use_graph = 1;
@@ -448,6 +449,10 @@ int letkf_sweep_set_option(letkf_sweep_t h, int option, int value) {
       if (value < 4 || value > 12) return LETKF_ERR_ARG;
       h->polish_tol_exp = value;
       return LETKF_OK;
+    case LETKF_OPT_TC_POLISH:
+      if (value != 0 && value != 1) return LETKF_ERR_ARG;
+      h->tc_polish = value;
+      return LETKF_OK;
     case LETKF_OPT_GRAPH:
       if (value != 0 && value != 1) return LETKF_ERR_ARG;
       h->use_graph = value;
@@ -582,6 +587,7 @@ static void build_args(letkf_sweep_t h, SweepArgs& a) {
   a.tc_ns_scaled = h->tc_ns_scaled;
   a.tc_ns_tol = (float)std::pow(10.0, -h->tc_ns_tol_exp);
   a.polish_tol = (float)std::pow(10.0, -h->polish_tol_exp);
+  a.tc_polish = h->tc_polish;
   a.defer_list = h->defer_list;  // read by the tensor-core sweep only
   a.defer_count = h->defer_count;
 }

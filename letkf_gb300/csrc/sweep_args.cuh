@@ -42,6 +42,7 @@ struct SweepArgs {
   int tc_ns_scaled;     // spectrum-scaled tensor-core steps (1) or plain ones (0)
   float tc_ns_tol;      // tensor-core phase ends once ||ZY - I||_F^2 < tc_ns_tol
   float polish_tol;     // FP32 polish: last step once ||Z A Z / s - I||_F^2 < polish_tol
+  int tc_polish;        // the anchored polish step on the tensor cores (1) or in FP32 (0)
 };
 
 }  // namespace letkf

@@ -77,6 +77,20 @@ struct TcLayout {
   static constexpr int TOTAL = CTRL + 16;
 };
 
+// sum_j M[j][c] x[j] for a 64 x 64 row-major matrix in shared memory (column
+// c read as consecutive lanes); four partial sums keep the loads in flight
+__device__ __forceinline__ float col_dot64(const float* M, const float* x, int c) {
+  float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll 4
+  for (int j = 0; j < 64; j += 4) {
+    a0 = fmaf(M[j * 64 + c], x[j], a0);
+    a1 = fmaf(M[(j + 1) * 64 + c], x[j + 1], a1);
+    a2 = fmaf(M[(j + 2) * 64 + c], x[j + 2], a2);
+    a3 = fmaf(M[(j + 3) * 64 + c], x[j + 3], a3);
+  }
+  return (a0 + a1) + (a2 + a3);
+}
+
 // Newton-Schulz map of one eigenvalue of ZY, x (3 - x)^2 / 4
 __device__ __forceinline__ float f_ns(float x) {
   const float t = 3.f - x;
@@ -371,7 +385,15 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
         // scaling s: power iteration guarded by the Gershgorin bound (s >= lambda_max / 2)
         float gsum = 0.f;
         if (tid < 64) {
-          for (int j = 0; j < 64; j++) gsum += fabsf(Gt[j * 64 + tid]);
+          float g0 = 0.f, g1 = 0.f, g2 = 0.f, g3 = 0.f;
+#pragma unroll 4
+          for (int j = 0; j < 64; j += 4) {
+            g0 += fabsf(Gt[j * 64 + tid]);
+            g1 += fabsf(Gt[(j + 1) * 64 + tid]);
+            g2 += fabsf(Gt[(j + 2) * 64 + tid]);
+            g3 += fabsf(Gt[(j + 3) * 64 + tid]);
+          }
+          gsum = (g0 + g1) + (g2 + g3);
           vx[tid] = Gt[tid * 64 + tid] * (1.f + 0.25f * __sinf(1.7f * tid));
         }
         gsum = warp_max(gsum);
@@ -384,8 +406,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
         for (int it = 0; it < 8; it++) {
           float part = 0.f, xx = 0.f;
           if (tid < 64) {
-            float acc = 0.f;
-            for (int j = 0; j < 64; j++) acc = fmaf(Gt[j * 64 + tid], vx[j], acc);
+            const float acc = col_dot64(Gt, vx, tid);
             vy[tid] = acc;
             part = acc * acc;
             xx = vx[tid] * vx[tid];
@@ -476,12 +497,14 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
               }
             }
           }
-          tc::fence_before_sync();
-          e2 = block_sum<float, TC_NT>(e2, red);
-          if (e2 < a.tc_ns_tol) done = true;
+          // ||ZY - I||^2 from warps 2 and 3 (rows 64..127), summed across the
+          // barrier that publishes the B operand
+          e2 = warp_sum(e2);
+          if (lane == 0 && wid >= 2) red[wid] = e2;
           tc::fence_smem_async();
           tc::fence_before_sync();
           __syncthreads();
+          if (red[2] + red[3] < a.tc_ns_tol) done = true;
           // [Y;Z] T
           if (tid == 0) {
             tc::fence_after_sync();
@@ -538,60 +561,211 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
           }
         }
         if (tmo) break;
-        // FP32 polish.  The coupled iteration never looks at A again, so the
-        // 16-bit rounding of the tensor-core phase shifts the matrix it is
-        // converging for.  Finish with the uncoupled iteration
-        //   Q = Z (A/s) Z,  Z <- (3 Z - Q Z) / 2,
-        // which references the exact A (kept in TMEM) at every step and so
-        // converges to (A/s)^(-1/2) from the tensor-core estimate.
-        float* Zf = reinterpret_cast<float*>(sm + L::ZF);
-        float* Af = reinterpret_cast<float*>(sm + L::YF);  // A / s
-        float* Pf = reinterpret_cast<float*>(sm + L::TF);  // A Z, then Q
-        {
-          float row[64];
-          if (r >= 64) {
+        if (a.tc_polish) {
+          // Tensor-core polish: the anchored step Q = Z (A/s) Z^T,
+          // Z <- Z - Z (Q - I) / 2, as three stacked 3-term bf16 products
+          // D = S B^T with S = [scratch; Z] (Z stays in rows 64..127):
+          //   B = A/s (exact A from TMEM)      -> rows 64..127: P = Z A/s
+          //   S rows 0..63 = P, B = Z          -> rows 0..63:   Q = P Z^T
+          //   B = R = Q - I                    -> rows 64..127: Z R
+          // R is small, so its 16-bit split is ample; Z's own 16-bit rounding
+          // is what the step measures and corrects.  Ends after the step whose
+          // ||Q - I||_F^2 fell below 1e-6 (the FP32 accumulation in TMEM
+          // leaves about 1e-7), at most TC_POLISH_MAX steps.
+          int pit = 0;
+          for (bool last = false; !last && !tmo;) {
+            // B <- A / s (row r of A from TMEM lanes 0..63)
+            if (wid < 2) {
 #pragma unroll
-            for (int c0 = 0; c0 < 64; c0 += 8) {
-              const uint32_t off = tc::kmajor_off_bf16(r, c0, 64);
-              float sh[8], sl[8];
-              unpack8(*reinterpret_cast<const uint4*>(sm + L::S_HI + off), sh);
-              unpack8(*reinterpret_cast<const uint4*>(sm + L::S_LO + off), sl);
+              for (int c0 = 0; c0 < 64; c0 += 16) {
+                float v[16];
+                tc::tmem_ld16(D1 + lane_off + c0, v);
 #pragma unroll
-              for (int j = 0; j < 8; j++) row[c0 + j] = sh[j] + sl[j];
+                for (int j = 0; j < 16; j++) v[j] *= inv_s;
+#pragma unroll
+                for (int g = 0; g < 2; g++) {
+                  uint4 h, l;
+                  split8(v + 8 * g, h, l);
+                  const uint32_t off = tc::kmajor_off_bf16(r, c0 + 8 * g, 64);
+                  *reinterpret_cast<uint4*>(sm + L::B_HI + off) = h;
+                  *reinterpret_cast<uint4*>(sm + L::B_LO + off) = l;
+                }
+              }
+            }
+            tc::fence_smem_async();
+            tc::fence_before_sync();
+            __syncthreads();
+            if (tid == 0) {
+              tc::fence_after_sync();
+              ns_mma(D0, sbase + L::S_HI, sbase + L::S_LO, sbase + L::B_HI, sbase + L::B_LO, idesc);
+              tc::mma_commit(&mbar[2]);
+            }
+            wait_bar(2);
+            tc::fence_after_sync();
+            // S rows 0..63 <- P (from rows 64..127 of D); B <- Z
+            if (wid >= 2) {
+#pragma unroll
+              for (int c0 = 0; c0 < 64; c0 += 16) {
+                float v[16];
+                tc::tmem_ld16(D0 + lane_off + c0, v);
+#pragma unroll
+                for (int g = 0; g < 2; g++) {
+                  uint4 h, l;
+                  split8(v + 8 * g, h, l);
+                  const uint32_t off = tc::kmajor_off_bf16(r - 64, c0 + 8 * g, 64);
+                  *reinterpret_cast<uint4*>(sm + L::S_HI + off) = h;
+                  *reinterpret_cast<uint4*>(sm + L::S_LO + off) = l;
+                }
+              }
+            }
+            for (int i = tid; i < 8192 / 16; i += TC_NT) {
+              reinterpret_cast<uint4*>(sm + L::B_HI)[i] = reinterpret_cast<const uint4*>(sm + L::S_HI + 8192)[i];
+              reinterpret_cast<uint4*>(sm + L::B_LO)[i] = reinterpret_cast<const uint4*>(sm + L::S_LO + 8192)[i];
+            }
+            tc::fence_smem_async();
+            tc::fence_before_sync();
+            __syncthreads();
+            if (tid == 0) {
+              tc::fence_after_sync();
+              ns_mma(D0, sbase + L::S_HI, sbase + L::S_LO, sbase + L::B_HI, sbase + L::B_LO, idesc);
+              tc::mma_commit(&mbar[2]);
+            }
+            wait_bar(2);
+            tc::fence_after_sync();
+            // B <- R = Q - I (rows 0..63 of D); ||R||_F^2
+            float e2 = 0.f;
+            if (wid < 2) {
+#pragma unroll
+              for (int c0 = 0; c0 < 64; c0 += 16) {
+                float v[16];
+                tc::tmem_ld16(D0 + lane_off + c0, v);
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                  v[j] -= (r == c0 + j) ? 1.f : 0.f;
+                  e2 = fmaf(v[j], v[j], e2);
+                }
+#pragma unroll
+                for (int g = 0; g < 2; g++) {
+                  uint4 h, l;
+                  split8(v + 8 * g, h, l);
+                  const uint32_t off = tc::kmajor_off_bf16(r, c0 + 8 * g, 64);
+                  *reinterpret_cast<uint4*>(sm + L::B_HI + off) = h;
+                  *reinterpret_cast<uint4*>(sm + L::B_LO + off) = l;
+                }
+              }
+            }
+            tc::fence_smem_async();
+            tc::fence_before_sync();
+            e2 = block_sum<float, TC_NT>(e2, red);
+            pit++;
+            last = e2 < 1.0e-6f || pit >= TC_POLISH_MAX;
+            if (tid == 0) {
+              tc::fence_after_sync();
+              ns_mma(D0, sbase + L::S_HI, sbase + L::S_LO, sbase + L::B_HI, sbase + L::B_LO, idesc);
+              tc::mma_commit(&mbar[2]);
+            }
+            wait_bar(2);
+            tc::fence_after_sync();
+            if (__syncthreads_or(tmo)) {
+              tmo = 1;
+              break;
+            }
+            // Z <- Z - Z R / 2 (rows 64..127); the last step writes W = coef Z
+            if (wid >= 2) {
+#pragma unroll
+              for (int c0 = 0; c0 < 64; c0 += 16) {
+                float v[16];
+                tc::tmem_ld16(D0 + lane_off + c0, v);
+#pragma unroll
+                for (int g = 0; g < 2; g++) {
+                  const uint32_t off = tc::kmajor_off_bf16(r, c0 + 8 * g, 64);
+                  float sh[8], sl[8], zn[8];
+                  unpack8(*reinterpret_cast<const uint4*>(sm + L::S_HI + off), sh);
+                  unpack8(*reinterpret_cast<const uint4*>(sm + L::S_LO + off), sl);
+#pragma unroll
+                  for (int j = 0; j < 8; j++) zn[j] = (sh[j] + sl[j]) - 0.5f * v[8 * g + j];
+                  if (last) {
+                    float* dst = Wm + (r - 64) * 64 + c0 + 8 * g;
+#pragma unroll
+                    for (int j = 0; j < 8; j++) dst[j] = coef * zn[j];
+                  } else {
+                    uint4 h, l;
+                    split8(zn, h, l);
+                    *reinterpret_cast<uint4*>(sm + L::S_HI + off) = h;
+                    *reinterpret_cast<uint4*>(sm + L::S_LO + off) = l;
+                  }
+                }
+              }
+            }
+            tc::fence_before_sync();
+            __syncthreads();
+          }
+          if (tmo) break;
+          // W symmetric, as the reference's V diag(.) V^T is
+          for (int idx = tid; idx < 64 * 64; idx += TC_NT) {
+            const int i = idx >> 6, j = idx & 63;
+            if (i < j) {
+              const float v = 0.5f * (Wm[i * 64 + j] + Wm[j * 64 + i]);
+              Wm[i * 64 + j] = v;
+              Wm[j * 64 + i] = v;
             }
           }
           __syncthreads();
-          if (r >= 64) {
-            float* dst = Zf + (r - 64) * 64;
-#pragma unroll
-            for (int j = 0; j < 64; j += 4)
-              *reinterpret_cast<float4*>(dst + j) = make_float4(row[j], row[j + 1], row[j + 2], row[j + 3]);
-          } else {
-#pragma unroll
-            for (int c0 = 0; c0 < 64; c0 += 16) {
-              float v[16];
-              tc::tmem_ld16(D1 + lane_off + c0, v);
-#pragma unroll
-              for (int j = 0; j < 16; j++) Af[r * 64 + c0 + j] = v[j] * inv_s;
+          it += pit;
+        } else {
+          // FP32 polish.  The coupled iteration never looks at A again, so the
+          // 16-bit rounding of the tensor-core phase shifts the matrix it is
+          // converging for.  Finish with the uncoupled iteration
+          //   Q = Z (A/s) Z,  Z <- (3 Z - Q Z) / 2,
+          // which references the exact A (kept in TMEM) at every step and so
+          // converges to (A/s)^(-1/2) from the tensor-core estimate.
+          float* Zf = reinterpret_cast<float*>(sm + L::ZF);
+          float* Af = reinterpret_cast<float*>(sm + L::YF);  // A / s
+          float* Pf = reinterpret_cast<float*>(sm + L::TF);  // A Z, then Q
+          {
+            float row[64];
+            if (r >= 64) {
+  #pragma unroll
+              for (int c0 = 0; c0 < 64; c0 += 8) {
+                const uint32_t off = tc::kmajor_off_bf16(r, c0, 64);
+                float sh[8], sl[8];
+                unpack8(*reinterpret_cast<const uint4*>(sm + L::S_HI + off), sh);
+                unpack8(*reinterpret_cast<const uint4*>(sm + L::S_LO + off), sl);
+  #pragma unroll
+                for (int j = 0; j < 8; j++) row[c0 + j] = sh[j] + sl[j];
+              }
+            }
+            __syncthreads();
+            if (r >= 64) {
+              float* dst = Zf + (r - 64) * 64;
+  #pragma unroll
+              for (int j = 0; j < 64; j += 4)
+                *reinterpret_cast<float4*>(dst + j) = make_float4(row[j], row[j + 1], row[j + 2], row[j + 3]);
+            } else {
+  #pragma unroll
+              for (int c0 = 0; c0 < 64; c0 += 16) {
+                float v[16];
+                tc::tmem_ld16(D1 + lane_off + c0, v);
+  #pragma unroll
+                for (int j = 0; j < 16; j++) Af[r * 64 + c0 + j] = v[j] * inv_s;
+              }
             }
           }
+          tc::fence_before_sync();
+          __syncthreads();
+          it += ns_polish<TC_NP>(Af, Zf, Pf, red, tc_max > 0 ? TC_POLISH_MAX : a.max_ns_iter, a.polish_tol);
+          for (int idx = tid; idx < 64 * 64; idx += TC_NT) Wm[idx] = coef * Zf[idx];
+          __syncthreads();
         }
-        tc::fence_before_sync();
-        __syncthreads();
-        it += ns_polish<TC_NP>(Af, Zf, Pf, red, tc_max > 0 ? TC_POLISH_MAX : a.max_ns_iter, a.polish_tol);
-        for (int idx = tid; idx < 64 * 64; idx += TC_NT) Wm[idx] = coef * Zf[idx];
-        __syncthreads();
         if (tmo) break;
         // wbar = Z (Z b) / s with Z = W / coef (W symmetric: column reads)
         if (tid < 64) {
-          float acc = 0.f;
-          for (int j = 0; j < 64; j++) acc = fmaf(Wm[j * 64 + tid], vb[j], acc);
+          const float acc = col_dot64(Wm, vb, tid);
           vg[tid] = acc / coef;
         }
         __syncthreads();
         if (tid < 64) {
-          float acc = 0.f;
-          for (int j = 0; j < 64; j++) acc = fmaf(Wm[j * 64 + tid], vg[j], acc);
+          const float acc = col_dot64(Wm, vg, tid);
           vwb[tid] = acc / (coef * s);
         }
         if (tid == 0) {
@@ -649,12 +823,25 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
       if (lane == 0) meanv[8 + v] = mean + dlt;
     }
     __syncthreads();
-    for (int t = tid; t < nv * n; t += TC_NT) {
-      const int v = t / n, mm = t - v * n;
-      float acc = 0.f;
-      const float* xp = xs + v * 64;
-      for (int k = 0; k < n; k++) acc = fmaf(xp[k], Wm[k * 64 + mm], acc);
-      a.xa[((size_t)v * a.npts + pt) * n + mm] = (float)(meanv[8 + v] + (double)acc);
+    {
+      // thread: member mm, variables vg, vg + 2, ... (up to four); one W load
+      // feeds every variable and the sums run in k order as before
+      const int mm = tid & 63, vg = tid >> 6;
+      if (mm < n) {
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 2
+        for (int k = 0; k < n; k++) {
+          const float w = Wm[k * 64 + mm];
+#pragma unroll
+          for (int j = 0; j < 4; j++)
+            if (vg + 2 * j < nv) acc[j] = fmaf(xs[(vg + 2 * j) * 64 + k], w, acc[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const int v = vg + 2 * j;
+          if (v < nv) a.xa[((size_t)v * a.npts + pt) * n + mm] = (float)(meanv[8 + v] + (double)acc[j]);
+        }
+      }
     }
   }
   // drain (bounded), report, release tensor memory

@@ -28,6 +28,7 @@ OPT_TC_NS_SCALING = 6
 OPT_TC_NS_TOL = 7
 OPT_POLISH_TOL = 8
 OPT_GRAPH = 9
+OPT_TC_POLISH = 10
 
 
 class SweepDesc(C.Structure):

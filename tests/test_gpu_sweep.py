@@ -33,6 +33,37 @@ def _spread(xb):
     return np.sqrt(((xb - xb.mean(-1, keepdims=True)) ** 2).sum(-1) / (xb.shape[-1] - 1)).mean()
 
 
+@pytest.mark.parametrize("ne", [20, 40, 64])
+def test_tc_polish_against_oracle(cuda, ne):
+    """The anchored polish step on the tensor cores (LETKF_OPT_TC_POLISH)
+    meets the mixed-form bar against the oracle."""
+    from letkf_gb300.sweep import OPT_TC_POLISH, PREC_MIXED, Sweep
+
+    case, prm, perm, grd, so, varloc, hdxf, dep = _setup(ne=ne, f32=True)
+    xb = case["xb"].astype(np.float64)
+    npts = case["pri"].size
+    infl0 = np.full(npts, 1.05)
+    xa_ref, infl_ref, nl_ref = so.sweep(hdxf[perm], dep[perm], xb, case["pri"], case["prj"], case["prlev"], infl0)
+    sw = Sweep(ne, case["nvar"], case["nlon"], case["nlat"], npts, prm, precision=PREC_MIXED)
+    sw.set_points(case["pri"], case["prj"], case["prlev"])
+    sw.set_obs(case["ri"], case["rj"], case["lev"], case["dat"], case["err"], dep, case["cls"],
+               hdxf.astype(np.float32))
+    sw.set_option(OPT_TC_POLISH, 1)
+    sw.set_background(case["xb"])
+    sw.set_inflation(infl0)
+    sw.run()
+    xa = sw.analysis().astype(np.float64)
+    dg = sw.diagnostics()
+    sw.close()
+    assert (dg["status"] == 0).all()
+    spread = _spread(xb)
+    em = np.sqrt(np.mean((xa.mean(-1) - xa_ref.mean(-1)) ** 2)) / spread
+    ep = np.sqrt(np.mean(((xa - xa.mean(-1, keepdims=True)) - (xa_ref - xa_ref.mean(-1, keepdims=True))) ** 2))
+    ep /= spread
+    assert em < 1e-4 and ep < 1e-4, (em, ep)
+    np.testing.assert_allclose(dg["infl"], infl_ref, rtol=1e-4)
+
+
 @pytest.mark.parametrize("ne,var_local,eig,tc,scaled", [(40, None, 0, 1, 1), (64, [1.0, 0.5, 0.0], 0, 1, 1),
                                                       (20, None, 0, 1, 1), (50, None, 0, 1, 1), (64, None, 0, 1, 0),
                                                       (64, None, 0, 0, 1),
