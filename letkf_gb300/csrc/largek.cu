@@ -10,8 +10,12 @@
 //      power-iteration estimate of lambda_max (tight: fewer iterations); a
 //      point whose residual grows restarts once from the Gershgorin bound,
 //      which always converges; Y0 = A/s, Z0 = I
-//   3. coupled Newton-Schulz  T = Z Y, Y <- 1.5 Y - 0.5 Y T,
-//      Z <- 1.5 Z - 0.5 T Z  until ||T - I||² < tol (per-point active flags)
+//   3. coupled Newton-Schulz  T = Z Y, Y <- b Y + a Y T, Z <- b Z + a T Z
+//      until ||T - I||² < tol (per-point active flags); the first step is
+//      plain (a = -0.5, b = 1.5), later ones spectrum-scaled per point
+//      (a = -0.5 g sqrt(g), b = 1.5 sqrt(g) with the step scale g from the
+//      tracked lower spectral bound, as in the tensor-core sweep); a
+//      residual above what a spectrum in [lo, 1] allows restarts the point
 //   4. two uncoupled steps anchored to A:  Z <- 1.5 Z - 0.5 (Z (A/s) Z) Z,
 //      symmetrised
 //   5. W = sqrt((k-1)/s) Z, wbar = Z (Z Ywᵀdep) / s, inflation update.
@@ -36,6 +40,8 @@ struct LkPoint {  // per-point scalars of a batch
   float e2_prev;  // residual of the previous iteration
   int kind;       // 0 transform, 1 no observations, 2 unsupported spectrum, 3 no convergence
   int restarted;  // 1 after the restart from the Gershgorin scale
+  float lo;       // lower bound of the spectrum of ZY (0.9 c / s at the start)
+  int steps;      // Newton-Schulz steps since the (re)start
 };
 
 __global__ void lk_weights_kernel(int64_t n, const float* __restrict__ rdiag, const float* __restrict__ rloc,
@@ -109,6 +115,8 @@ __global__ void __launch_bounds__(LKP_NT) lk_prep_kernel(int ne, int kp, const i
     q.e2_prev = INFINITY;
     q.kind = kind;
     q.restarted = 0;
+    q.lo = 0.f;
+    q.steps = 0;
     pt[b] = q;
     active[b] = kind == 0;
   }
@@ -154,6 +162,8 @@ __global__ void __launch_bounds__(LKP_NT) lk_prep_kernel(int ne, int kp, const i
   if (tid == 0) {
     pt[b].s = (double)s;
     pt[b].gmax = gmax;
+    pt[b].lo = 0.9f * (float)(c / (double)s);
+    pt[b].steps = 0;
     inv_s[b] = is;
   }
   float* Yb = Y + mo;
@@ -165,37 +175,61 @@ __global__ void __launch_bounds__(LKP_NT) lk_prep_kernel(int ne, int kp, const i
   }
 }
 
-// Converged points leave the coupled phase.  A residual that is not finite or
-// grows (after the first steps) restarts the point once from the Gershgorin
-// scale (counts[1]); a second failure, or a point still iterating at the cap
-// (last != 0), fails the point.  counts[0] = points still iterating.
-__global__ void lk_check_kernel(int nb, int it, const float* __restrict__ e2, int* active, int* counts, LkPoint* pt,
-                                int* restart, int last) {
+// Converged points leave the coupled phase.  With the spectrum of ZY in
+// [lo, u] (u = gmax / s before the first step, 1 + d after it) the residual
+// is at most kp max((1 - lo)^2, (u - 1)^2); a residual above that, or not
+// finite, restarts the point once from the Gershgorin scale (counts[1]); a
+// second failure, or a point still iterating at the cap (last != 0), fails
+// the point.  Points that go on get this step's coefficients (alpha_b,
+// beta_b) and their bound follows f.  counts[0] = points still iterating.
+__global__ void lk_check_kernel(int nb, int kp, int it, const float* __restrict__ e2, int* active, int* counts,
+                                LkPoint* pt, int* restart, int last, float* alpha_b, float* beta_b) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nb || !active[b]) return;
+  (void)it;
   const float r = e2[b];
-  const float prev = pt[b].e2_prev;
-  const bool grows = !isfinite(r) || (it >= 2 && r > prev) || r > 4.f * prev;
-  if (grows && !pt[b].restarted) {
-    pt[b].restarted = 1;
-    pt[b].e2_prev = INFINITY;
+  LkPoint q = pt[b];
+  const float u = q.steps == 0 ? q.gmax * (float)(1.0 / q.s) : 1.02f;
+  const float d0 = 1.f - q.lo, d1 = u - 1.f;
+  const float bound = (float)kp * fmaxf(d0 * d0, d1 * d1) * 1.05f + 1.0e-3f;
+  const bool bad = !isfinite(r) || r > bound;
+  if (bad && !q.restarted) {
+    q.restarted = 1;
+    q.e2_prev = INFINITY;
     restart[b] = 1;
+    active[b] = 0;  // left alone by this iteration's updates, reset and reactivated after them
     atomicAdd(&counts[0], 1);
     atomicAdd(&counts[1], 1);
-  } else if (grows || (last && !(r < LK_NS_TOL))) {
-    pt[b].kind = 3;
+  } else if (bad || (last && !(r < LK_NS_TOL))) {
+    q.kind = 3;
     active[b] = 0;
   } else if (r < LK_NS_TOL) {
     active[b] = 0;
   } else {
-    pt[b].e2_prev = r;
+    float g = 1.f;
+    if (q.steps == 0) {
+      // plain first step: with s = 1.05 x the power estimate the top of the
+      // spectrum is near 1 (f(1) = 1), so the bound follows the bottom; a
+      // power estimate far below lambda_max shows as a residual above the
+      // bound and restarts the point from the Gershgorin scale (top <= 1)
+      q.lo = f_ns(q.lo);
+    } else {
+      g = ns_scale(q.lo);
+      q.lo = f_ns(g * q.lo);
+    }
+    const float sg = sqrtf(g);
+    alpha_b[b] = -0.5f * g * sg;
+    beta_b[b] = 1.5f * sg;
+    q.steps++;
+    q.e2_prev = r;
     atomicAdd(&counts[0], 1);
   }
+  pt[b] = q;
 }
 
-// restart flagged points from s = Gershgorin bound: Y = A/s, Z = I
+// restart flagged points from s = Gershgorin bound: Y = A/s, Z = I, active again
 __global__ void lk_restart_kernel(int kp, const float* __restrict__ G, float* Y, float* Z, float* inv_s, LkPoint* pt,
-                                  int* restart) {
+                                  int* restart, int* active) {
   const int b = blockIdx.y;
   if (!restart[b]) return;
   const size_t mo = (size_t)b * kp * kp;
@@ -208,7 +242,10 @@ __global__ void lk_restart_kernel(int kp, const float* __restrict__ G, float* Y,
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     pt[b].s = (double)s;
+    pt[b].lo = 0.9f * (float)(pt[b].c / (double)s);
+    pt[b].steps = 0;
     inv_s[b] = is;
+    active[b] = 1;
   }
 }
 
@@ -406,7 +443,7 @@ extern "C" int letkf_core_batch_largek(int ne, int npts, const int64_t* offs, co
       cudaStreamSynchronize(s) != cudaSuccess)
     return LETKF_ERR_CUDA;
   float *w = nullptr, *G = nullptr, *Y = nullptr, *Z = nullptr, *Yn = nullptr, *Zn = nullptr, *T = nullptr;
-  float *bvec = nullptr, *e2 = nullptr, *inv_s = nullptr;
+  float *bvec = nullptr, *e2 = nullptr, *inv_s = nullptr, *alphas = nullptr, *betas = nullptr;
   int *active = nullptr, *count = nullptr, *err = nullptr, *restart = nullptr;
   LkPoint* pt = nullptr;
   bool ok = true;
@@ -421,6 +458,8 @@ extern "C" int letkf_core_batch_largek(int ne, int npts, const int64_t* offs, co
   A(&bvec, sizeof(float) * (size_t)kp * B);
   A(&e2, sizeof(float) * B);
   A(&inv_s, sizeof(float) * B);
+  A(&alphas, sizeof(float) * B);
+  A(&betas, sizeof(float) * B);
   A(&active, sizeof(int) * B);
   A(&count, 2 * sizeof(int));
   A(&restart, sizeof(int) * B);
@@ -467,35 +506,39 @@ extern "C" int letkf_core_batch_largek(int ne, int npts, const int64_t* offs, co
       g.e2 = e2;
       st = lk_gemm<LK_T>(g, nb, s);
       if (st) break;
-      lk_check_kernel<<<(nb + 127) / 128, 128, 0, s>>>(nb, it, e2, active, count, pt, restart, it == LK_NS_MAX - 1);
+      lk_check_kernel<<<(nb + 127) / 128, 128, 0, s>>>(nb, kp, it, e2, active, count, pt, restart,
+                                                       it == LK_NS_MAX - 1, alphas, betas);
       note_launch();
       int h_count[2] = {0, 0};
       cudaMemcpyAsync(h_count, count, 2 * sizeof(int), cudaMemcpyDeviceToHost, s);
       st = cuda_status(cudaStreamSynchronize(s));
       if (st || h_count[0] == 0) break;
-      if (h_count[1] > 0) {  // restart, then iterate again from Y0, Z0
-        dim3 rg(64, nb);
-        lk_restart_kernel<<<rg, 256, 0, s>>>(kp, G, Y, Z, inv_s, pt, restart);
-        note_launch();
-        cudaMemsetAsync(restart, 0, sizeof(int) * nb, s);
-        continue;
-      }
-      g.alpha = -0.5f;
-      g.beta = 1.5f;
-      g.X = Y;  // Y <- 1.5 Y - 0.5 Y T
+      g.alpha_b = alphas;  // per-point step coefficients
+      g.beta_b = betas;
+      g.X = Y;  // Y <- b Y + a Y T
       g.Y = T;
       g.D = Y;
       g.out = Yn;
       st = lk_gemm<LK_AXPBY>(g, nb, s);
       if (st) break;
-      g.X = T;  // Z <- 1.5 Z - 0.5 T Z
+      g.X = T;  // Z <- b Z + a T Z
       g.Y = Z;
       g.D = Z;
       g.out = Zn;
       st = lk_gemm<LK_AXPBY>(g, nb, s);
+      g.alpha_b = nullptr;
+      g.beta_b = nullptr;
       std::swap(Y, Yn);
       std::swap(Z, Zn);
+      if (st == LETKF_OK && h_count[1] > 0) {  // restarted points: Y0, Z0 from the Gershgorin scale
+        dim3 rg(64, nb);
+        lk_restart_kernel<<<rg, 256, 0, s>>>(kp, G, Y, Z, inv_s, pt, restart, active);
+        note_launch();
+        cudaMemsetAsync(restart, 0, sizeof(int) * nb, s);
+      }
     }
+    g.alpha_b = nullptr;
+    g.beta_b = nullptr;
     // 4. uncoupled steps anchored to A (G holds A)
     lk_reactivate_kernel<<<(nb + 127) / 128, 128, 0, s>>>(nb, pt, active);
     note_launch();
@@ -538,7 +581,7 @@ extern "C" int letkf_core_batch_largek(int ne, int npts, const int64_t* offs, co
     st = cuda_status(cudaStreamSynchronize(s));
     if (st == LETKF_OK && h_err) st = LETKF_ERR_TIMEOUT;
   }
-  void* fr[] = {w, G, Y, Z, Yn, Zn, T, bvec, e2, inv_s, active, count, err, pt, restart};
+  void* fr[] = {w, G, Y, Z, Yn, Zn, T, bvec, e2, inv_s, alphas, betas, active, count, err, pt, restart};
   for (void* p : fr)
     if (p) cudaFreeAsync(p, s);
   return st;

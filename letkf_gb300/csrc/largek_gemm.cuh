@@ -14,7 +14,8 @@
 //   LK_GRAM   out = Ywᵀ Y over the point's local rows (K = its L, rows of the
 //             packed [nrows][ne] array, Yw = w_l y_l)
 //   LK_T      out = X Y and e2[b] += ||out - I||²_F   (Newton-Schulz residual)
-//   LK_AXPBY  out = alpha X Y + beta D   (alpha per point when alpha_b is set;
+//   LK_AXPBY  out = alpha X Y + beta D   (alpha, beta per point when alpha_b,
+//             beta_b are set;
 //             D may be NULL: out = alpha X Y)
 // X, Y, D, out are [batch][kp][kp] row-major; B(n, k) = Y[k][n], so no operand
 // needs to be symmetric.  Points with active[b] == 0 copy D to out (AXPBY) or
@@ -44,6 +45,7 @@ struct LkGemmArgs {
   const float* D;
   float alpha, beta;
   const float* alpha_b;   // [batch] or NULL
+  const float* beta_b;    // [batch] or NULL
   float* out;
   float* e2;              // [batch] (LK_T)
   const int* active;      // [batch] or NULL
@@ -121,8 +123,53 @@ __global__ void __launch_bounds__(LK_NT, 3) largek_gemm_kernel(LkGemmArgs a) {
   int tmo = 0;
   const int r = tid & 127, h = tid >> 7;  // staging: row r, K half h (8 values)
 
+  // stage values of this thread: rows r of A and B, K half h (8 values each);
+  // the next stage's loads are issued before this stage is split and stored,
+  // so their latency overlaps the staging, the barrier and the MMA issue
+  float va[8], vb[8];
+  auto load_stage = [&](int c, float (&xa)[8], float (&xb)[8]) {
+    const int k0 = c * LK_KC + h * 8;
+    if (MODE == LK_GRAM) {
+      // A(m, l) = w_l y_l[m], B(n, l) = y_l[n]; rows beyond L or members beyond ne are 0
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const int l = k0 + j;
+        float ya = 0.f, yb = 0.f;
+        if (l < L) {
+          const float* row = a.rows + (size_t)(r0 + l) * a.ne;
+          const float w = a.wts[r0 + l];
+          if (m0 + r < a.ne) ya = w * row[m0 + r];
+          if (n0 + r < a.ne) yb = row[n0 + r];
+        }
+        xa[j] = ya;
+        xb[j] = yb;
+      }
+    } else {
+      const float4 x0 = *reinterpret_cast<const float4*>(a.X + mo + (size_t)(m0 + r) * kp + k0);
+      const float4 x1 = *reinterpret_cast<const float4*>(a.X + mo + (size_t)(m0 + r) * kp + k0 + 4);
+      xa[0] = x0.x;
+      xa[1] = x0.y;
+      xa[2] = x0.z;
+      xa[3] = x0.w;
+      xa[4] = x1.x;
+      xa[5] = x1.y;
+      xa[6] = x1.z;
+      xa[7] = x1.w;
+#pragma unroll
+      for (int j = 0; j < 8; j++) xb[j] = a.Y[mo + (size_t)(k0 + j) * kp + n0 + r];
+    }
+  };
+  if (nk > 0) load_stage(0, va, vb);
+
   for (int c = 0; c < nk; c++) {
     const int buf = c & 1;
+    float ca[8], cb[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      ca[j] = va[j];
+      cb[j] = vb[j];
+    }
+    if (c + 1 < nk) load_stage(c + 1, va, vb);
     if (outst[buf]) {
       if (!tc::mbar_wait(&mbar[buf], par[buf], LK_WAIT)) tmo = 1;
       par[buf] ^= 1u;
@@ -130,37 +177,13 @@ __global__ void __launch_bounds__(LK_NT, 3) largek_gemm_kernel(LkGemmArgs a) {
     }
     tc::fence_after_sync();
     unsigned char* st = sm + buf * LK_STAGE;
-    const int k0 = c * LK_KC;
 #pragma unroll
     for (int g = 0; g < 2; g++) {
       const int kk = h * 8 + g * 4;
-      float va[4], vb[4];
-      if (MODE == LK_GRAM) {
-        // A(m, l) = w_l y_l[m], B(n, l) = y_l[n]; rows beyond L or members beyond ne are 0
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-          const int l = k0 + kk + j;
-          float ya = 0.f, yb = 0.f;
-          if (l < L) {
-            const float* row = a.rows + (size_t)(r0 + l) * a.ne;
-            const float w = a.wts[r0 + l];
-            if (m0 + r < a.ne) ya = w * row[m0 + r];
-            if (n0 + r < a.ne) yb = row[n0 + r];
-          }
-          va[j] = ya;
-          vb[j] = yb;
-        }
-      } else {
-        const float4 x = *reinterpret_cast<const float4*>(a.X + mo + (size_t)(m0 + r) * kp + k0 + kk);
-        va[0] = x.x;
-        va[1] = x.y;
-        va[2] = x.z;
-        va[3] = x.w;
-#pragma unroll
-        for (int j = 0; j < 4; j++) vb[j] = a.Y[mo + (size_t)(k0 + kk + j) * kp + n0 + r];
-      }
-      lk_store(st, st + LK_OPER, r, kk, va);
-      lk_store(st + 2 * LK_OPER, st + 3 * LK_OPER, r, kk, vb);
+      const float qa[4] = {ca[4 * g], ca[4 * g + 1], ca[4 * g + 2], ca[4 * g + 3]};
+      const float qb[4] = {cb[4 * g], cb[4 * g + 1], cb[4 * g + 2], cb[4 * g + 3]};
+      lk_store(st, st + LK_OPER, r, kk, qa);
+      lk_store(st + 2 * LK_OPER, st + 3 * LK_OPER, r, kk, qb);
     }
     tc::fence_smem_async();
     tc::fence_before_sync();
@@ -213,14 +236,15 @@ __global__ void __launch_bounds__(LK_NT, 3) largek_gemm_kernel(LkGemmArgs a) {
       float* dst = a.out + orow + c0;
       if (MODE == LK_AXPBY) {
         const float al = a.alpha_b ? a.alpha_b[b] : a.alpha;
+        const float be = a.beta_b ? a.beta_b[b] : a.beta;
         if (a.D) {
           const float* dd = a.D + orow + c0;
 #pragma unroll
           for (int j = 0; j < 16; j += 4) {
             const float4 d4 = *reinterpret_cast<const float4*>(dd + j);
             *reinterpret_cast<float4*>(dst + j) =
-                make_float4(al * v[j] + a.beta * d4.x, al * v[j + 1] + a.beta * d4.y, al * v[j + 2] + a.beta * d4.z,
-                            al * v[j + 3] + a.beta * d4.w);
+                make_float4(al * v[j] + be * d4.x, al * v[j + 1] + be * d4.y, al * v[j + 2] + be * d4.z,
+                            al * v[j + 3] + be * d4.w);
           }
         } else {
 #pragma unroll

@@ -28,6 +28,23 @@ inline cudaError_t set_smem_once(K kern, size_t bytes, std::atomic<uint32_t>& do
 
 constexpr double kSigmaB = 0.04;  // common/common_letkf.f90:75 error stdev of parm_infl
 
+// Newton-Schulz map of one eigenvalue of ZY, x (3 - x)^2 / 4
+__device__ __forceinline__ float f_ns(float x) {
+  const float t = 3.f - x;
+  return 0.25f * x * t * t;
+}
+
+// Newton-Schulz step scale a >= 1 for a spectrum of ZY in [lo, 1 + d], d = 0.02:
+// the a with f(a lo) = f(a (1 + d)), a = 3 (1 - sqrt(l)) / (1 - l^1.5) / (1 + d),
+// l = lo / (1 + d); S <- sqrt(a) S (3I - aZY) / 2 maps eigenvalue x to f(a x)
+__device__ __forceinline__ float ns_scale(float lo) {
+  const float d1 = 1.02f;
+  const float l = fminf(fmaxf(lo / d1, 0.f), 0.999f);
+  const float r = sqrtf(l);
+  const float al = 3.f * (1.f - r) / ((1.f - l * r) * d1);
+  return fmaxf(al, 1.f);
+}
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll

@@ -91,21 +91,6 @@ __device__ __forceinline__ float col_dot64(const float* M, const float* x, int c
   return (a0 + a1) + (a2 + a3);
 }
 
-// Newton-Schulz map of one eigenvalue of ZY, x (3 - x)^2 / 4
-__device__ __forceinline__ float f_ns(float x) {
-  const float t = 3.f - x;
-  return 0.25f * x * t * t;
-}
-
-// step scale a >= 1 for a spectrum in [lo, 1 + d], d = 0.02: f(a lo) = f(a (1 + d))
-__device__ __forceinline__ float ns_scale(float lo) {
-  const float d1 = 1.02f;
-  const float l = fminf(fmaxf(lo / d1, 0.f), 0.999f);
-  const float r = sqrtf(l);
-  const float al = 3.f * (1.f - r) / ((1.f - l * r) * d1);
-  return fmaxf(al, 1.f);
-}
-
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
   const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
   return *reinterpret_cast<const uint32_t*>(&v);
