@@ -59,8 +59,8 @@ __global__ void __launch_bounds__(LKP_NT) lk_prep_kernel(int ne, int kp, const i
                                                           double minfl, float* G, float* Y, float* Z,
                                                           float* bvec, float* inv_s, LkPoint* pt, int* active) {
   __shared__ double red[LKP_NT / 32];
-  __shared__ float xv[1024];
-  __shared__ float yv[1024];
+  __shared__ __align__(16) float xv[1024];
+  __shared__ __align__(16) float yv[1024];
   __shared__ float redf[LKP_NT / 32];
   const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int64_t r0 = offs[b];
@@ -124,30 +124,42 @@ __global__ void __launch_bounds__(LKP_NT) lk_prep_kernel(int ne, int kp, const i
   const float cf = (float)c;
   for (int m = tid; m < kp; m += LKP_NT) A[(size_t)m * kp + m] = (m < ne ? A[(size_t)m * kp + m] : 0.f) + cf;
   __syncthreads();
-  // Gershgorin bound and power iteration (s >= lambda_max / 2 keeps Newton-Schulz convergent)
+  // Gershgorin bound and power iteration (s >= lambda_max / 2 keeps Newton-Schulz convergent);
+  // one warp per row, the lanes over 16-byte column groups (coalesced row reads)
+  const int kp4 = kp / 4;
   float gmax = 0.f;
-  for (int m = tid; m < kp; m += LKP_NT) {
+  for (int m = wid; m < kp; m += LKP_NT / 32) {
+    const float4* row4 = reinterpret_cast<const float4*>(A + (size_t)m * kp);
     float g = 0.f;
-    const float* row = A + (size_t)m * kp;
-    for (int j = 0; j < kp; j++) g += fabsf(row[j]);
-    gmax = fmaxf(gmax, g);
-    xv[m] = row[m] * (1.f + 0.25f * __sinf(1.7f * m));
+    for (int j4 = lane; j4 < kp4; j4 += 32) {
+      const float4 x = row4[j4];
+      g += (fabsf(x.x) + fabsf(x.y)) + (fabsf(x.z) + fabsf(x.w));
+    }
+    gmax = fmaxf(gmax, warp_sum(g));
   }
-  gmax = warp_max(gmax);
+  for (int m = tid; m < kp; m += LKP_NT) xv[m] = A[(size_t)m * kp + m] * (1.f + 0.25f * __sinf(1.7f * m));
   __syncthreads();
   if (lane == 0) redf[wid] = gmax;
   __syncthreads();
   gmax = 0.f;
   for (int i = 0; i < LKP_NT / 32; i++) gmax = fmaxf(gmax, redf[i]);
   float lam = 0.f;
+  const float4* xv4 = reinterpret_cast<const float4*>(xv);
   for (int it = 0; it < 8; it++) {
+    for (int m = wid; m < kp; m += LKP_NT / 32) {
+      const float4* row4 = reinterpret_cast<const float4*>(A + (size_t)m * kp);
+      float acc = 0.f;
+      for (int j4 = lane; j4 < kp4; j4 += 32) {
+        const float4 x = row4[j4], v = xv4[j4];
+        acc = fmaf(x.x, v.x, fmaf(x.y, v.y, fmaf(x.z, v.z, fmaf(x.w, v.w, acc))));
+      }
+      acc = warp_sum(acc);
+      if (lane == 0) yv[m] = acc;
+    }
+    __syncthreads();
     double nrm2 = 0.0, x2 = 0.0;
     for (int m = tid; m < kp; m += LKP_NT) {
-      const float* row = A + (size_t)m * kp;
-      float acc = 0.f;
-      for (int j = 0; j < kp; j++) acc = fmaf(row[j], xv[j], acc);
-      yv[m] = acc;
-      nrm2 += (double)acc * acc;
+      nrm2 += (double)yv[m] * yv[m];
       x2 += (double)xv[m] * xv[m];
     }
     nrm2 = bsum(nrm2);

@@ -5,9 +5,7 @@
 //    transform (T + wbar 1^T, RTPP applied as weight_RTPP does, :959-970),
 //    obsanal(n, m) = ybar(n) + sum_k obshdxf(n, k) trans(k, m), ybar =
 //    obsdat - obsdep, the mean in member order, the q "no update" branch and
-//    the relative-spread clip.  The k sum runs over the lanes of a warp
-//    (coalesced reads of column m of trans), so it differs from the serial
-//    sum by rounding.
+//    the relative-spread clip.
 //  * letkf_efso: observation sensitivity (gfs/letkf/letkf_tools.f90:547-679)
 //    over grid points with their local observation lists.
 #include "letkf_common.cuh"
@@ -34,25 +32,23 @@ __global__ void __launch_bounds__(OSA_NT) obs_analysis_kernel(int ne, int n, con
     const int md = mode ? mode[p] : 0;
     const double yb = ybar[p];
     const double* tp = trans + (size_t)p * ne * ne;
-    // one warp per member m, the lanes over k: column m of trans is contiguous
-    const int lane = tid & 31, wid = tid >> 5;
-    for (int m = wid; m < ne; m += OSA_NT / 32) {
+    // thread per member m: it walks column m of trans (contiguous, stays in L1)
+    for (int m = tid; m < ne; m += OSA_NT) {
       double v;
       if (md == 1) {
         v = yb + h[m];
       } else {
-        double part = 0.0;
-        for (int k = lane; k < ne; k += 32) {
+        v = yb;
+        for (int k = 0; k < ne; k++) {
           double w = tp[(size_t)m * ne + k];
           if (alpha != 0.0) {
             w = (1.0 - alpha) * w;
             if (k == m) w = w + alpha;
           }
-          part = fma(h[k], w, part);
+          v = v + h[k] * w;
         }
-        v = yb + warp_sum(part);
       }
-      if (lane == 0) a[m] = v;
+      a[m] = v;
     }
     __syncthreads();
     if (tid == 0) {
