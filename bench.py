@@ -71,6 +71,7 @@ def parse():
                     help="run the autotuner on this many points before timing (0: the options given)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
     ap.add_argument("--no-largek", action="store_true", help="skip the large-ensemble measurement")
+    ap.add_argument("--no-configs", action="store_true", help="skip the Lorenz-96 and SPEEDY-grid parity lines")
     ap.add_argument("--largek-points", type=int, default=4096, help="sampled points of the large-ensemble sweep")
     ap.add_argument("--serve-requests", type=int, default=48, help="requests of the serving measurement")
     ap.add_argument("--serve-slots", type=int, default=3, help="jobs on the device at once")
@@ -306,6 +307,101 @@ def run_serving(args, dev):
 
 
 # --------------------------------------------------------------- large k
+def run_configs(args, dev):
+    """The two small configurations beside the headline: Lorenz-96 (N = 40, k = 20,
+    40 identity obs, xlocal = 3, inflation 1.05) in the FP64 plain and mixed forms,
+    and the SPEEDY grid (96x48x7, k = 40, radiosonde-like obs) in the FP64 plain
+    form, each against the oracle (L96: every point; SPEEDY: every 61st point of
+    u, v, t, q) with throughput from CUDA events."""
+    import torch
+
+    from letkf_gb300 import synthetic as S
+    from letkf_gb300.core import l96_obs_cell
+    from letkf_gb300.drivers import l96_letkf, speedy_letkf, speedy_sort_obs
+    from oracle import oracle as O
+
+    out = {}
+    t = lambda a, dt=torch.float64: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
+    ev = lambda: (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+    # ---- Lorenz-96 ----
+    c = S.l96_case(11)
+    xf = c["xf"].T.copy()
+    nx, ne = xf.shape
+    xm = xf.sum(1) / ne
+    ref = np.zeros_like(xf)
+    for ix in range(1, nx + 1):
+        idx, rl = O.l96_select(c["h"], ix, 3.0)
+        r = O.letkf_core(c["hdxf"][idx], np.full(idx.size, c["obserr"] ** 2), rl, c["dep"][idx], 1.05)
+        ref[ix - 1] = xm[ix - 1] + (xf[ix - 1] - xm[ix - 1]) @ r["trans"]
+    spread = np.sqrt(((xf - xm[:, None]) ** 2).sum(1) / (ne - 1)).mean()
+    h = t(c["h"])
+    cell = l96_obs_cell(h)
+    l96 = {"workload": "Lorenz-96 N=40, k=20, 40 obs, xlocal=3, inflation 1.05"}
+    for prec in ("f64", "mixed"):
+        xft = t(xf)
+        hxf = h @ xft
+        y = t(c["y"])
+        l96_letkf(xft, hxf, y, cell, obserr=float(c["obserr"]), precision=prec)
+        torch.cuda.synchronize()
+        e0, e1 = ev()
+        e0.record()
+        reps = 20
+        for _ in range(reps):
+            xa, _ = l96_letkf(xft, hxf, y, cell, obserr=float(c["obserr"]), precision=prec)
+        e1.record()
+        torch.cuda.synchronize()
+        dt = e0.elapsed_time(e1) / 1e3 / reps
+        err = float(np.abs(xa.cpu().numpy() - ref).max() / spread)
+        l96[prec] = {"max_abs_error_over_spread": err, "ms_per_analysis": 1e3 * dt, "points_per_s": nx / dt}
+    out["lorenz96"] = l96
+    # ---- SPEEDY grid, FP64 plain form ----
+    c = S.speedy_case(4)
+    perm, grd = speedy_sort_obs(c["lon"], c["lat"], c["olon"], c["olat"])
+    srt = {k: c[k][perm] for k in ("elm", "olon", "olat", "olev", "odat", "oerr")}
+    hdxf, dep = c["hdxf"][perm], c["dep"][perm]
+    grid = {"lon": t(c["lon"]), "lat": t(c["lat"]), "nobsgrd": t(grd, torch.int32)}
+    obs = {"elm": t(srt["elm"]), "lon": t(srt["olon"]), "lat": t(srt["olat"]), "lev": t(srt["olev"]),
+           "dat": t(srt["odat"]), "err": t(srt["oerr"])}
+    params = (c["dist_zero"], c["dist_zerov"], c["dlat_zero"], c["sigma_obs"], c["sigma_obsv"])
+    nv3d, nlev, ne, nij = c["gues3d"].shape
+    var_local = np.ones((nv3d, 7))
+    args_ = (grid, obs, t(hdxf), t(dep), t(c["gues3d"]), t(c["logpfm"]), t(c["dlon_zero"]), params, var_local)
+    infl = torch.full((nv3d, nlev, nij), 1.1, dtype=torch.float64, device=dev)
+    speedy_letkf(*args_, infl.clone())
+    torch.cuda.synchronize()
+    e0, e1 = ev()
+    e0.record()
+    anal3d, _ = speedy_letkf(*args_, infl)
+    e1.record()
+    torch.cuda.synchronize()
+    dt = e0.elapsed_time(e1) / 1e3
+    anal3d = anal3d.cpu().numpy()
+    so = O.SpeedyObs(c["lon"], c["lat"], grd, srt["elm"], srt["olon"], srt["olat"], srt["olev"], srt["odat"],
+                     srt["oerr"], c["dist_zero"], c["dist_zerov"], c["dlat_zero"], c["sigma_obs"], c["sigma_obsv"],
+                     var_local[0])
+    g3 = c["gues3d"]
+    worst, npts = 0.0, 0
+    sp = np.sqrt(((g3 - g3.mean(2, keepdims=True)) ** 2).sum(2) / (ne - 1)).mean()
+    for p in range(0, nlev * nij, 61):
+        ilev, ij = divmod(p, nij)
+        ri, rl, rd = so.obs_local(c["glon"][ij], c["glat"][ij], c["dlon_zero"][ij], ilev + 1, c["logpfm"][ilev, ij])
+        r = O.letkf_core(hdxf[ri] if ri.size else np.zeros((1, ne)), rd if ri.size else np.ones(1),
+                         rl if ri.size else np.ones(1), dep[ri] if ri.size else np.zeros(1), 1.1, nobsl=ri.size)
+        for n in range(nv3d):
+            xb = g3[n, ilev, :, ij]
+            m = xb[0]
+            for k in range(1, ne):
+                m = m + xb[k]
+            m = m / ne
+            w = np.eye(ne) if (n == 3 and ilev + 1 >= 5) else r["trans"]
+            worst = max(worst, float(np.abs(anal3d[n, ilev, :, ij] - (m + (xb - m) @ w)).max() / sp))
+        npts += 1
+    out["speedy"] = {"workload": f"SPEEDY grid 96x48x7, k=40, {srt['elm'].size} radiosonde-like obs, u/v/t/q, FP64 plain form",
+                     "points_per_s": nlev * nij / dt, "ms_per_analysis": 1e3 * dt,
+                     "max_abs_error_over_spread": worst, "checked_points": npts, "target": 1e-10}
+    return out
+
+
 def run_largek(args, dev):
     """Large-ensemble configuration on a sample of its points: 360x181x32
     global grid, 6 variables, k = 512, 3e6 observations, SPEEDY lat/lon
@@ -561,6 +657,8 @@ def run_gpu(args, rank, world, dist):
         out["serving"] = run_serving(args, dev)
     if not args.no_largek:
         out["large_k"] = run_largek(args, dev)
+    if not args.no_configs:
+        out["configs"] = run_configs(args, dev)
     return out, sw
 
 
