@@ -194,11 +194,10 @@ __global__ void __launch_bounds__(LKP_NT) lk_prep_kernel(int ne, int kp, const i
 // second failure, or a point still iterating at the cap (last != 0), fails
 // the point.  Points that go on get this step's coefficients (alpha_b,
 // beta_b) and their bound follows f.  counts[0] = points still iterating.
-__global__ void lk_check_kernel(int nb, int kp, int it, const float* __restrict__ e2, int* active, int* counts,
-                                LkPoint* pt, int* restart, int last, float* alpha_b, float* beta_b) {
+__global__ void lk_check_kernel(int nb, int kp, const float* __restrict__ e2, int* active, int* counts, LkPoint* pt,
+                                int* restart, int last, float* alpha_b, float* beta_b) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nb || !active[b]) return;
-  (void)it;
   const float r = e2[b];
   LkPoint q = pt[b];
   const float u = q.steps == 0 ? q.gmax * (float)(1.0 / q.s) : 1.02f;
@@ -518,8 +517,8 @@ extern "C" int letkf_core_batch_largek(int ne, int npts, const int64_t* offs, co
       g.e2 = e2;
       st = lk_gemm<LK_T>(g, nb, s);
       if (st) break;
-      lk_check_kernel<<<(nb + 127) / 128, 128, 0, s>>>(nb, kp, it, e2, active, count, pt, restart,
-                                                       it == LK_NS_MAX - 1, alphas, betas);
+      lk_check_kernel<<<(nb + 127) / 128, 128, 0, s>>>(nb, kp, e2, active, count, pt, restart, it == LK_NS_MAX - 1,
+                                                       alphas, betas);
       note_launch();
       int h_count[2] = {0, 0};
       cudaMemcpyAsync(h_count, count, 2 * sizeof(int), cudaMemcpyDeviceToHost, s);
