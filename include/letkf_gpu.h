@@ -302,6 +302,7 @@ int letkf_l96_obs_cell(int nx, int ny, const double* h, int* cell, void* stream)
 #define LETKF_OPT_POLISH_TOL 8    /* v: the FP32 polish takes its last step once ||Z A Z / s - I||_F^2 < 10^-v (4..12, default 7) */
 #define LETKF_OPT_GRAPH 9         /* 1 (default): the mixed-form run is a CUDA graph, replayed while arguments stay the same */
 #define LETKF_OPT_TC_POLISH 10    /* 1: the anchored polish step of the tensor-core sweep on the tensor cores; 0 (default): FP32 */
+#define LETKF_OPT_TC_SCALE_BOUND 11 /* 1 (default): tensor-core scale s = min(||A||_F, Gershgorin), every step scaled; 0: power iteration */
 
 typedef struct letkf_sweep_desc {
   int ne;           /* ensemble size (MEMBER) */

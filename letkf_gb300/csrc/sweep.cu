@@ -148,6 +148,7 @@ struct letkf_sweep_s {
   int tc_ns_tol_exp = 3;
   int polish_tol_exp = 7;
   int tc_polish = 0;
+  int tc_scale_bound = 1;
   // CUDA graph of the mixed-form run: replayed while the kernel arguments,
   // launch choices and stream stay the same, captured again otherwise
   int use_graph = 1;
@@ -453,6 +454,10 @@ int letkf_sweep_set_option(letkf_sweep_t h, int option, int value) {
       if (value != 0 && value != 1) return LETKF_ERR_ARG;
       h->tc_polish = value;
       return LETKF_OK;
+    case LETKF_OPT_TC_SCALE_BOUND:
+      if (value != 0 && value != 1) return LETKF_ERR_ARG;
+      h->tc_scale_bound = value;
+      return LETKF_OK;
     case LETKF_OPT_GRAPH:
       if (value != 0 && value != 1) return LETKF_ERR_ARG;
       h->use_graph = value;
@@ -588,6 +593,7 @@ static void build_args(letkf_sweep_t h, SweepArgs& a) {
   a.tc_ns_tol = (float)std::pow(10.0, -h->tc_ns_tol_exp);
   a.polish_tol = (float)std::pow(10.0, -h->polish_tol_exp);
   a.tc_polish = h->tc_polish;
+  a.tc_scale_bound = h->tc_scale_bound;
   a.defer_list = h->defer_list;  // read by the tensor-core sweep only
   a.defer_count = h->defer_count;
 }

@@ -43,6 +43,7 @@ struct SweepArgs {
   float tc_ns_tol;      // tensor-core phase ends once ||ZY - I||_F^2 < tc_ns_tol
   float polish_tol;     // FP32 polish: last step once ||Z A Z / s - I||_F^2 < polish_tol
   int tc_polish;        // the anchored polish step on the tensor cores (1) or in FP32 (0)
+  int tc_scale_bound;   // scale s from min(||A||_F, Gershgorin), every step scaled (1); power iteration (0)
 };
 
 }  // namespace letkf

@@ -387,8 +387,26 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
         __syncthreads();
         const float gmax = fmaxf(fmaxf(red[0], red[1]), fmaxf(red[2], red[3]));
         __syncthreads();
-        float lam = 0.f;
-        for (int it = 0; it < 8; it++) {
+        float lam = 0.f, fro = 0.f;
+        if (a.tc_scale_bound) {
+          // s = min(||A||_F, Gershgorin) >= lambda_max: every eigenvalue of A/s is <= 1
+          float f2 = 0.f;
+          if (tid < 64) {
+            float q0 = 0.f, q1 = 0.f, q2 = 0.f, q3 = 0.f;
+#pragma unroll 4
+            for (int j = 0; j < 64; j += 4) {
+              const float x0 = Gt[j * 64 + tid], x1 = Gt[(j + 1) * 64 + tid];
+              const float x2 = Gt[(j + 2) * 64 + tid], x3 = Gt[(j + 3) * 64 + tid];
+              q0 = fmaf(x0, x0, q0);
+              q1 = fmaf(x1, x1, q1);
+              q2 = fmaf(x2, x2, q2);
+              q3 = fmaf(x3, x3, q3);
+            }
+            f2 = (q0 + q1) + (q2 + q3);
+          }
+          fro = sqrtf(block_sum<float, TC_NT>(f2, red));
+        }
+        for (int it = 0; it < (a.tc_scale_bound ? 0 : 8); it++) {
           float part = 0.f, xx = 0.f;
           if (tid < 64) {
             const float acc = col_dot64(Gt, vx, tid);
@@ -404,7 +422,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
           if (tid < 64) vx[tid] = vy[tid] * inv;
           __syncthreads();
         }
-        const float s = fmaxf(1.05f * lam, 0.5f * gmax);
+        const float s = a.tc_scale_bound ? fminf(fro, gmax) : fmaxf(1.05f * lam, 0.5f * gmax);
         const float inv_s = 1.f / s;
         // S = [A/s ; I] split into bf16 hi / lo (row r per thread)
 #pragma unroll
@@ -439,8 +457,10 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
         // ZY towards 1; stop once ||ZY - I||_F^2 < tc_ns_tol (or after TC_NS_MAX).
         // Spectrum scaling: with X = ZY = (A/s) Z^2 and f(x) = x (3 - x)^2 / 4,
         // the step S <- sqrt(a) S (3I - aX) / 2 maps every eigenvalue x of X to
-        // f(a x).  The first step is plain (a = 1; x <= gmax / s <= 2), which
-        // leaves the spectrum in [lo, 1]; later steps take the a that balances
+        // f(a x).  With s = min(||A||_F, Gershgorin) >= lambda_max the spectrum
+        // starts in [lo, 1] and every step is scaled; with the power-iteration
+        // scale the first step is plain (a = 1; x <= gmax / s <= 2), which
+        // leaves the spectrum in [lo, 1].  A scaled step takes the a that balances
         // f(a lo) = f(a (1 + d)), a = 3 (1 - sqrt(l)) / (1 - l^1.5) / (1 + d)
         // with l = lo / (1 + d), which multiplies the small eigenvalues by about
         // 6.75 per step instead of 2.25.  lo starts from the diagonal shift
@@ -504,7 +524,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
           }
           // S <- sqrt(a) (1.5 S - 0.5 a S X) (each thread rewrites only its own row)
           float ka = 1.5f, kb = 0.5f;
-          if (it == 0) {
+          if (it == 0 && !a.tc_scale_bound) {
             lo = fminf(f_ns(lo), lo_top);
           } else if (a.tc_ns_scaled) {
             const float al = ns_scale(lo);

@@ -88,12 +88,10 @@ __device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count) {
 
 // arrive on the barrier and add `bytes` to the transaction count of its phase
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* mbar, uint32_t bytes) {
-  uint64_t state;
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;"
-               : "=l"(state)
-               : "r"(smem_u32(mbar)), "r"(bytes)
-               : "memory");
-  (void)state;
+  asm volatile(
+      "{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}\n" ::"r"(smem_u32(mbar)),
+      "r"(bytes)
+      : "memory");
 }
 
 // TMA bulk copy global -> shared (untiled): both addresses 16-byte aligned,

@@ -29,6 +29,7 @@ OPT_TC_NS_TOL = 7
 OPT_POLISH_TOL = 8
 OPT_GRAPH = 9
 OPT_TC_POLISH = 10
+OPT_TC_SCALE_BOUND = 11
 
 
 class SweepDesc(C.Structure):
