@@ -325,7 +325,10 @@ __device__ __forceinline__ void sym_gemm_tile(const float* X, const float* Yb, i
 // quadratic convergence then reaches the FP32 floor) or max_iter.  Returns the
 // iterations done; Y, Z hold the last iterate.
 template <int NP>
-__device__ int ns_iterate(float* Y, float* Z, float* T, float* redf, int max_iter) {
+__device__ int ns_iterate(float* Y, float* Z, float* T, float* redf, int max_iter, float lo = -1.f) {
+  // lo >= 0: the spectrum of ZY starts in [lo, 1] and every step is
+  // spectrum-scaled (Y' = sqrt(a) Y (3I - aT) / 2, likewise Z; see ns_scale);
+  // lo < 0: plain steps
   using C = MixedCfg<NP>;
   constexpr int NTI = NP / C::TR;
   const int tid = threadIdx.x;
@@ -347,18 +350,26 @@ __device__ int ns_iterate(float* Y, float* Z, float* T, float* redf, int max_ite
       }
     e2 = block_sum<float, C::NT>(e2, redf);  // also publishes T
     if (e2 < 1.0e-8f) last = true;
-    // Y' = 1.5 Y - 0.5 Y T ; Z' = 1.5 Z - 0.5 T Z
+    float ka = 1.5f, kb = 0.5f;
+    if (lo >= 0.f) {
+      const float al = ns_scale(lo);
+      const float sa = sqrtf(al);
+      ka = 1.5f * sa;
+      kb = 0.5f * al * sa;
+      lo = f_ns(al * lo);
+    }
+    // Y' = ka Y - kb Y T ; Z' = ka Z - kb T Z
     float ynew[C::TR][C::TC];
     sym_gemm_tile<NP>(Y, T, i0, j0, acc);
 #pragma unroll
     for (int a = 0; a < C::TR; a++)
 #pragma unroll
-      for (int b = 0; b < C::TC; b++) ynew[a][b] = 1.5f * Y[(i0 + a) * NP + j0 + b] - 0.5f * acc[a][b];
+      for (int b = 0; b < C::TC; b++) ynew[a][b] = ka * Y[(i0 + a) * NP + j0 + b] - kb * acc[a][b];
     sym_gemm_tile<NP>(T, Z, i0, j0, acc);
 #pragma unroll
     for (int a = 0; a < C::TR; a++)
 #pragma unroll
-      for (int b = 0; b < C::TC; b++) acc[a][b] = 1.5f * Z[(i0 + a) * NP + j0 + b] - 0.5f * acc[a][b];
+      for (int b = 0; b < C::TC; b++) acc[a][b] = ka * Z[(i0 + a) * NP + j0 + b] - kb * acc[a][b];
     __syncthreads();
 #pragma unroll
     for (int a = 0; a < C::TR; a++)
@@ -463,17 +474,20 @@ __device__ float ns_invsqrt(float* sm, float cdiag, int max_iter, int* iters) {
   float* A = sm + S::A;
   float* Z = sm + S::V;
   float* T = sm + N::T;
-  float* xv = sm + S::G;   // power-iteration vector
-  float* yv = sm + S::LAM;
   float* redf = sm + S::RED;
-  // Gershgorin bound (>= lambda_max) and a power-iteration estimate.  A is
+  // s = min(Gershgorin, ||A||_F) >= lambda_max, so the spectrum of A/s lies in
+  // [c/s, 1] and every Newton-Schulz step can be spectrum-scaled.  A is
   // symmetric: row i is read as column i (consecutive lanes, no bank conflicts).
-  float g = 0.f;
+  float g = 0.f, f2 = 0.f;
   if (tid < NP) {
-    float s = 0.f;
-    for (int j = 0; j < NP; j++) s += fabsf(A[j * NP + tid]);
+    float s = 0.f, q = 0.f;
+    for (int j = 0; j < NP; j++) {
+      const float x = A[j * NP + tid];
+      s += fabsf(x);
+      q = fmaf(x, x, q);
+    }
     g = s;
-    xv[tid] = A[tid * NP + tid] * (1.f + 0.25f * __sinf(1.7f * tid));
+    f2 = q;
   }
   g = warp_max(g);
   __syncthreads();
@@ -482,24 +496,8 @@ __device__ float ns_invsqrt(float* sm, float cdiag, int max_iter, int* iters) {
   float gmax = redf[0];
   for (int w = 1; w < C::NT / 32; w++) gmax = fmaxf(gmax, redf[w]);
   __syncthreads();
-  float lam = 0.f;
-  for (int it = 0; it < 8; it++) {
-    float part = 0.f, xx = 0.f;
-    if (tid < NP) {
-      float s = 0.f;
-      for (int j = 0; j < NP; j++) s = fmaf(A[j * NP + tid], xv[j], s);
-      yv[tid] = s;
-      part = s * s;
-      xx = xv[tid] * xv[tid];
-    }
-    const float nrm2 = block_sum<float, C::NT>(part, redf);
-    const float x2 = block_sum<float, C::NT>(xx, redf);
-    lam = sqrtf(nrm2 / fmaxf(x2, 1e-30f));
-    const float inv = rsqrtf(fmaxf(nrm2, 1e-30f));
-    if (tid < NP) xv[tid] = yv[tid] * inv;
-    __syncthreads();
-  }
-  const float s = fmaxf(1.05f * lam, 0.5f * gmax);
+  const float fro = sqrtf(block_sum<float, C::NT>(f2, redf));
+  const float s = fminf(gmax, fro);
   const float inv_s = 1.f / s;
   // Y0 = A/s (in place), Z0 = I
   for (int idx = tid; idx < NP * NP; idx += C::NT) {
@@ -507,7 +505,7 @@ __device__ float ns_invsqrt(float* sm, float cdiag, int max_iter, int* iters) {
     Z[idx] = (idx / NP == idx % NP) ? 1.f : 0.f;
   }
   __syncthreads();
-  const int it = ns_iterate<NP>(A, Z, T, redf, max_iter);
+  const int it = ns_iterate<NP>(A, Z, T, redf, max_iter, 0.9f * cdiag * inv_s);
   if (iters) *iters = it;
   return s;
 }
