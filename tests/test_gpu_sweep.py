@@ -235,6 +235,19 @@ def test_graph_replay_equals_eager_runs(cuda, tc):
     sw.set_option(OPT_TC_NS_SCALING, 0)                        # new kernel arguments: a new capture
     g, _ = run(sw, case["xb"], st.cuda_stream)
     assert np.abs(g.astype(np.float64) - e1).max() < 1e-3 * _spread(case["xb"].astype(np.float64))
+    sw.set_option(OPT_TC_NS_SCALING, 1)
+    # fewer observations reuse the resident buffers; same bits as a fresh handle
+    sub = slice(0, len(case["ri"]) // 2)
+    obs_sub = (case["ri"][sub], case["rj"][sub], case["lev"][sub], case["dat"][sub], case["err"][sub], dep[sub],
+               case["cls"][sub], hdxf[sub].astype(np.float32))
+    sw.set_obs(*obs_sub)
+    g, gi = run(sw, case["xb"], st.cuda_stream)
+    fresh = make(0)
+    fresh.set_obs(*obs_sub)
+    f, fi = run(fresh, case["xb"])
+    fresh.close()
+    np.testing.assert_array_equal(g, f)
+    np.testing.assert_array_equal(gi, fi)
     sw.close()
 
 
