@@ -46,18 +46,23 @@ __device__ __forceinline__ double scale_ndist_exact(const SweepArgs& a, int ob, 
 }
 
 struct SearchSmem {
-  int* pidx;    // [CH + NT]
+  int* pidx;    // [CH + CPT*NT]
   float* pw;    // weight rloc / err^2
   float* pd;    // departure
   float* pr;    // rloc
   int* rowib;   // [SW_MAXROWS]
   int* rowpre;  // [SW_MAXROWS + 1]
-  int* wcnt;    // [NT/32 + 1]
+  int* wcnt;    // [CPT*NT/32 + 1]
 };
 
-template <int NT, int CH, typename Flush>
+// One pass over the candidates of a grid point.  Each batch tests CPT*NT
+// candidates (CPT per thread, candidate base + g*NT + tid in group g), so the
+// batches and their barriers are CPT times fewer; accepted observations are
+// compacted group by group, which keeps the reference's candidate order.
+template <int NT, int CH, int CPT = 1, typename Flush>
 __device__ int sweep_search(const SweepArgs& a, double ri, double rj, double logr, double rz, const SearchSmem& s,
                             Flush&& flush) {
+  constexpr int NW = NT / 32;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int ld = a.nlon + 1;
   const float dzf2 = 13.33333333f;  // scale/letkf/letkf_obs.f90:30 (default-real literal)
@@ -89,84 +94,105 @@ __device__ int sweep_search(const SweepArgs& a, double ri, double rj, double log
     }
     __syncthreads();
     const int ncand = s.rowpre[nrow];
-    for (int base = 0; base < ncand; base += NT) {
-      const int c = base + tid;
-      int ob = -1;
-      bool ok_acc = false;
-      float w = 0.f, dv = 0.f, rl = 0.f;
-      if (c < ncand) {
-        int lo = 0, hi = nrow - 1;  // rowpre[lo] <= c < rowpre[lo+1]
-        while (lo < hi) {
-          const int mid = (lo + hi + 1) >> 1;
-          if (s.rowpre[mid] <= c) lo = mid;
-          else hi = mid - 1;
-        }
-        ob = s.rowib[lo] + (c - s.rowpre[lo]);
-        const int meta = a.obsMeta[ob];
-        if (!(meta & 2)) {
-          const float4 f = a.obsF[ob];
-          const float di = rif - f.x, dj = rjf - f.y;
-          const float h2 = (di * di * dx2 + dj * dj * dy2) * f.w;
-          const float4 g = a.obsA[ob];
-          const float vv = ((meta & 1) ? rzf : logrf) - f.z;
-          float nd = h2 + vv * vv * g.x;
-          bool ok = nd <= band_lo;
-          if (!ok && nd <= band_hi) {
-            const double ndd = scale_ndist_exact(a, ob, ri, rj, logr, rz);
-            ok = !(ndd > dzf2d);
-            nd = (float)ndd;
+    for (int base = 0; base < ncand; base += CPT * NT) {
+      int obg[CPT], before[CPT];
+      bool okg[CPT];
+      float wg[CPT], dg[CPT], rg[CPT];
+#pragma unroll
+      for (int g = 0; g < CPT; g++) {
+        const int c = base + g * NT + tid;
+        int ob = -1;
+        bool ok_acc = false;
+        float w = 0.f, dv = 0.f, rl = 0.f;
+        if (c < ncand) {
+          int lo = 0, hi = nrow - 1;  // rowpre[lo] <= c < rowpre[lo+1]
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s.rowpre[mid] <= c) lo = mid;
+            else hi = mid - 1;
           }
-          if (ok) {
-            ok_acc = true;
-            rl = __expf(-0.5f * nd) * g.w;
-            w = rl * g.y;
-            dv = g.z;
+          ob = s.rowib[lo] + (c - s.rowpre[lo]);
+          const int meta = a.obsMeta[ob];
+          if (!(meta & 2)) {
+            const float4 f = a.obsF[ob];
+            const float di = rif - f.x, dj = rjf - f.y;
+            const float h2 = (di * di * dx2 + dj * dj * dy2) * f.w;
+            const float4 q = a.obsA[ob];
+            const float vv = ((meta & 1) ? rzf : logrf) - f.z;
+            float nd = h2 + vv * vv * q.x;
+            bool ok = nd <= band_lo;
+            if (!ok && nd <= band_hi) {
+              const double ndd = scale_ndist_exact(a, ob, ri, rj, logr, rz);
+              ok = !(ndd > dzf2d);
+              nd = (float)ndd;
+            }
+            if (ok) {
+              ok_acc = true;
+              rl = __expf(-0.5f * nd) * q.w;
+              w = rl * q.y;
+              dv = q.z;
+            }
           }
         }
+        const unsigned bal = __ballot_sync(0xffffffffu, ok_acc);
+        before[g] = __popc(bal & ((1u << lane) - 1u));
+        if (lane == 0) s.wcnt[g * NW + wid] = __popc(bal);
+        obg[g] = ob;
+        okg[g] = ok_acc;
+        wg[g] = w;
+        dg[g] = dv;
+        rg[g] = rl;
       }
-      const unsigned bal = __ballot_sync(0xffffffffu, ok_acc);
-      const int before = __popc(bal & ((1u << lane) - 1u));
-      if (lane == 0) s.wcnt[wid] = __popc(bal);
       __syncthreads();
       if (tid == 0) {
         int t = 0;
-        for (int k = 0; k < NT / 32; k++) {
+        for (int k = 0; k < CPT * NW; k++) {
           const int v = s.wcnt[k];
           s.wcnt[k] = t;
           t += v;
         }
-        s.wcnt[NT / 32] = t;
+        s.wcnt[CPT * NW] = t;
       }
       __syncthreads();
-      if (ok_acc) {
-        const int slot = pend + s.wcnt[wid] + before;
-        s.pidx[slot] = ob;
-        s.pw[slot] = w;
-        s.pd[slot] = dv;
-        s.pr[slot] = rl;
-      }
-      pend += s.wcnt[NT / 32];
-      L += s.wcnt[NT / 32];
+#pragma unroll
+      for (int g = 0; g < CPT; g++)
+        if (okg[g]) {
+          const int slot = pend + s.wcnt[g * NW + wid] + before[g];
+          s.pidx[slot] = obg[g];
+          s.pw[slot] = wg[g];
+          s.pd[slot] = dg[g];
+          s.pr[slot] = rg[g];
+        }
+      pend += s.wcnt[CPT * NW];
+      L += s.wcnt[CPT * NW];
       __syncthreads();
       while (pend >= CH) {
         flush(CH);
         __syncthreads();
-        // move the tail (fewer than NT entries) to the front
+        // move the tail (fewer than CPT*NT entries) to the front
         const int rest = pend - CH;
-        int i0 = 0;
-        float w0 = 0.f, d0 = 0.f, r0 = 0.f;
-        if (tid < rest) {
-          i0 = s.pidx[CH + tid];
-          w0 = s.pw[CH + tid];
-          d0 = s.pd[CH + tid];
-          r0 = s.pr[CH + tid];
+        int i0[CPT];
+        float w0[CPT], d0[CPT], r0[CPT];
+#pragma unroll
+        for (int g = 0; g < CPT; g++) {
+          const int t = g * NT + tid;
+          if (t < rest) {
+            i0[g] = s.pidx[CH + t];
+            w0[g] = s.pw[CH + t];
+            d0[g] = s.pd[CH + t];
+            r0[g] = s.pr[CH + t];
+          }
         }
         __syncthreads();
-        if (tid < rest) {
-          s.pidx[tid] = i0;
-          s.pw[tid] = w0;
-          s.pd[tid] = d0;
-          s.pr[tid] = r0;
+#pragma unroll
+        for (int g = 0; g < CPT; g++) {
+          const int t = g * NT + tid;
+          if (t < rest) {
+            s.pidx[t] = i0[g];
+            s.pw[t] = w0[g];
+            s.pd[t] = d0[g];
+            s.pr[t] = r0[g];
+          }
         }
         pend = rest;
         __syncthreads();
