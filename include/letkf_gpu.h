@@ -271,6 +271,19 @@ int letkf_search_l96(int nx, int ny, const int* obs_cell, int npts, const int* p
                      double tdif, double tlocal, double obserr, const int64_t* offs, int* nobsl,
                      int* idx, double* rloc, double* rdiag, void* stream);
 
+/* 4D-LETKF selection of the Lorenz-96 driver (lorenz96/letkf/letkf.f90:
+ * 217-254, nwindow > 1): for analysis slot `slot` (0-based nn - 1) the
+ * observations of every slot n = 0..nslot-1 in slot order, each slot's in
+ * observation order, with tdif = |slot - n| (0 when tlocal < 0) in
+ * rloc = exp(-0.5 (d/xlocal)^2) exp(-0.5 (tdif/tlocal)^2) and the 1e-4 drop.
+ * obs_cell[nslot][ny] (1-based grid index per slot); idx is the row n*ny + i
+ * of the slot-stacked observation arrays.  Count pass (idx NULL) then fill
+ * pass as letkf_search_l96.  nslot = 1, slot = 0 equals letkf_search_l96 with
+ * tdif = 0. */
+int letkf_search_l96_4d(int nx, int nslot, int ny, const int* obs_cell, int npts, const int* pix, int slot,
+                        double xlocal, double tlocal, double obserr, const int64_t* offs, int* nobsl, int* idx,
+                        double* rloc, double* rdiag, void* stream);
+
 /* Grid index of each observation of the Lorenz-96 driver: the first maximum
  * of row i of h (ny x nx, column-major, on the device), 1-based
  * (lorenz96/letkf/letkf.f90:226-228). */

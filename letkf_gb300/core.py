@@ -401,6 +401,31 @@ def search_l96(nx, obs_cell, pix, xlocal=3.0, obserr=1.0, tdif=0.0, tlocal=-1.0,
     return offs, idx[:total], rloc[:total], rdiag[:total]
 
 
+def search_l96_4d(nx, obs_cell, pix, slot, xlocal=3.0, obserr=1.0, tlocal=2.0, stream=None):
+    """4D-LETKF selection of the Lorenz-96 driver (lorenz96/letkf/letkf.f90:
+    217-254) for analysis slot `slot` (0-based): obs_cell int32 [nslot, ny]
+    (1-based grid index per observation and slot), pix int32 [npts].  Returns
+    (offs, idx, rloc, rdiag) with idx the row n*ny + i of the slot-stacked
+    observations."""
+    import torch
+
+    dev = obs_cell.device
+    nslot, ny = obs_cell.shape
+    npts = pix.numel()
+    nobsl = torch.empty(npts, dtype=torch.int32, device=dev)
+    cell = obs_cell.contiguous()
+    args = (nx, nslot, ny, _dptr(cell), npts, _dptr(pix), int(slot), float(xlocal), float(tlocal), float(obserr))
+    check(lib().letkf_search_l96_4d(*args, None, _dptr(nobsl), None, None, None, _stream(stream)), "search_l96_4d")
+    offs = exclusive_scan(nobsl, stream)
+    total = int(offs[-1].item())
+    idx = torch.empty(max(total, 1), dtype=torch.int32, device=dev)
+    rloc = torch.empty(max(total, 1), dtype=torch.float64, device=dev)
+    rdiag = torch.empty(max(total, 1), dtype=torch.float64, device=dev)
+    check(lib().letkf_search_l96_4d(*args, _dptr(offs), None, _dptr(idx), _dptr(rloc), _dptr(rdiag),
+                                    _stream(stream)), "search_l96_4d")
+    return offs, idx[:total], rloc[:total], rdiag[:total]
+
+
 __all__ = ["letkf_core", "core_batch_f64", "core_batch_mixed", "update_f64", "exclusive_scan", "gather_rows",
            "search_scale", "search_speedy", "search_l96", "l96_obs_cell", "obs_departure", "update_relax_f64", "relax_beta", "core_batch_largek", "update_mixed", "obs_analysis", "efso", "RELAX_NONE", "RELAX_RTPP",
            "RELAX_RTPS", "LETKF_OK"]

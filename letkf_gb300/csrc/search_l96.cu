@@ -124,6 +124,66 @@ __global__ void l96_search_kernel(L96Ctx c, int npts, const int* __restrict__ pi
     for (int t = 0; t < n; t++) rdiag[base + t] = rdiag_value;
 }
 
+// 4D-LETKF selection (lorenz96/letkf/letkf.f90:217-254): for analysis slot
+// `slot` every observation slot n in order, tdif = |slot - n| (0 when tlocal <
+// 0), the observation's row in the slot-stacked arrays being n*ny + i.  Buckets
+// of slot n: boff + n*(nx+1), bobs + n*ny.
+struct L96Ctx4d {
+  int nx, ny, nslot, slot;
+  const int64_t* boff;
+  const int* bobs;
+  double xlocal, xmaxloc, tlocal;
+};
+
+__global__ void l96_search4d_kernel(L96Ctx4d c, int npts, const int* __restrict__ pix,
+                                    const int64_t* __restrict__ offs, int* __restrict__ nobsl, int* __restrict__ idx,
+                                    double* __restrict__ rloc, double* __restrict__ rdiag, double rdiag_value) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npts) return;
+  const int ix = pix[p];
+  const int64_t base = idx ? offs[p] : 0;
+  int n = 0;
+  for (int sl = 0; sl < c.nslot; sl++) {
+    L96Ctx s1;
+    s1.nx = c.nx;
+    s1.ny = c.ny;
+    s1.boff = c.boff + (size_t)sl * (c.nx + 1);
+    s1.bobs = c.bobs + (size_t)sl * c.ny;
+    s1.xlocal = c.xlocal;
+    s1.xmaxloc = c.xmaxloc;
+    const double tdif = c.tlocal < 0.0 ? 0.0 : (double)abs(c.slot - sl);
+    const double tq = tdif / c.tlocal;
+    s1.tfac = exp(-0.5 * (tq * tq));
+    const int n0 = n;  // this slot's entries start here, sorted by observation index
+    l96_visit(s1, ix, [&](int j, int dist) {
+      const double r = l96_rloc(s1, dist);
+      if (r < 0.0) return;
+      if (!idx) {
+        n += (int)(s1.boff[j] - s1.boff[j - 1]);
+        return;
+      }
+      for (int64_t q = s1.boff[j - 1]; q < s1.boff[j]; q++) {
+        const int ob = sl * c.ny + s1.bobs[q];
+        int t = n;
+        while (t > n0 && idx[base + t - 1] > ob) {
+          idx[base + t] = idx[base + t - 1];
+          rloc[base + t] = rloc[base + t - 1];
+          t--;
+        }
+        idx[base + t] = ob;
+        rloc[base + t] = r;
+        n++;
+      }
+    });
+  }
+  if (!idx) {
+    nobsl[p] = n;
+    return;
+  }
+  if (rdiag)
+    for (int t = 0; t < n; t++) rdiag[base + t] = rdiag_value;
+}
+
 }  // namespace letkf
 
 using namespace letkf;
@@ -189,6 +249,66 @@ int letkf_search_l96(int nx, int ny, const int* obs_cell, int npts, const int* p
     c.tfac = tlocal < 0.0 ? 1.0 : exp(-0.5 * (tq * tq));
     l96_search_kernel<<<(npts + 127) / 128, 128, 0, s>>>(c, npts, pix, offs, nobsl, idx, rloc, rdiag,
                                                          obserr * obserr);
+    note_launch();
+    st = cuda_status(cudaGetLastError());
+  }
+  cudaFreeAsync(buf, s);
+  return st;
+}
+
+int letkf_search_l96_4d(int nx, int nslot, int ny, const int* obs_cell, int npts, const int* pix, int slot,
+                        double xlocal, double tlocal, double obserr, const int64_t* offs, int* nobsl, int* idx,
+                        double* rloc, double* rdiag, void* stream) {
+  if (nx < 1 || nslot < 1 || ny < 0 || npts < 0 || slot < 0 || slot >= nslot || !(xlocal > 0.0) ||
+      (ny > 0 && !obs_cell) || (npts > 0 && !pix))
+    return LETKF_ERR_ARG;
+  if (!idx && !nobsl) return LETKF_ERR_ARG;
+  if (idx && (!offs || !rloc)) return LETKF_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return LETKF_ERR_NOGPU;
+  }
+  if (npts == 0) return LETKF_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  // per slot: bucket offsets [nx+1], counts and cursor [nx], observations [ny]; shared scan scratch
+  const int nb = (nx + 1023) / 1024 + 1;
+  const size_t ns = (size_t)nslot;
+  const size_t bytes = sizeof(int64_t) * (ns * ((size_t)nx + 1) + nb) + sizeof(int) * (ns * (2 * (size_t)nx + ny) + 1);
+  unsigned char* buf = nullptr;
+  if (cudaMallocAsync((void**)&buf, bytes, s) != cudaSuccess) return LETKF_ERR_CUDA;
+  int64_t* boff = reinterpret_cast<int64_t*>(buf);
+  int64_t* scr = boff + ns * (nx + 1);
+  int* cnt = reinterpret_cast<int*>(scr + nb);
+  int* cur = cnt + ns * nx;
+  int* bobs = cur + ns * nx;
+  int st = cuda_status(cudaMemsetAsync(cnt, 0, sizeof(int) * 2 * ns * (size_t)nx, s));
+  for (int sl = 0; sl < nslot && st == LETKF_OK; sl++) {
+    const int* cell = obs_cell + (size_t)sl * ny;
+    if (ny > 0) {
+      l96_bucket_count<<<(ny + 255) / 256, 256, 0, s>>>(nx, ny, cell, cnt + (size_t)sl * nx);
+      note_launch();
+    }
+    st = launch_exclusive_scan(nx, cnt + (size_t)sl * nx, boff + (size_t)sl * (nx + 1), scr, s);
+    if (st == LETKF_OK && ny > 0) {
+      l96_bucket_fill<<<(ny + 255) / 256, 256, 0, s>>>(nx, ny, cell, boff + (size_t)sl * (nx + 1),
+                                                       cur + (size_t)sl * nx, bobs + (size_t)sl * ny);
+      note_launch();
+    }
+  }
+  if (st == LETKF_OK) {
+    L96Ctx4d c;
+    c.nx = nx;
+    c.ny = ny;
+    c.nslot = nslot;
+    c.slot = slot;
+    c.boff = boff;
+    c.bobs = bobs;
+    c.xlocal = xlocal;
+    c.xmaxloc = xlocal * 2.0 * sqrt(10.0 / 3.0);
+    c.tlocal = tlocal;
+    l96_search4d_kernel<<<(npts + 127) / 128, 128, 0, s>>>(c, npts, pix, offs, nobsl, idx, rloc, rdiag,
+                                                           obserr * obserr);
     note_launch();
     st = cuda_status(cudaGetLastError());
   }

@@ -2,6 +2,7 @@
 the device path of this library (search -> gather -> batched core -> update).
 
 * ``l96_letkf``   -- lorenz96/letkf/letkf.f90:180-265 (one time slot)
+* ``l96_letkf_4d`` -- the same with nwindow > 1 time slots (4D-LETKF)
 * ``speedy_letkf`` -- speedy/letkf/letkf_tools.f90:44-203 (das_letkf)
 * ``speedy_sort_obs`` -- speedy/letkf/letkf_obs.f90:243-313 (bucket sort)
 * ``speedy_obs_setup`` -- set_letkf_obs (speedy/letkf/letkf_obs.f90:48-313) with
@@ -294,4 +295,53 @@ def l96_letkf(xf, hxf, y, obs_cell, obserr=1.0, xlocal=3.0, parm_infl=None, msw_
     return xa, parm_infl
 
 
-__all__ = ["speedy_sort_obs", "var_local_n2n", "speedy_letkf", "l96_letkf"]
+def l96_letkf_4d(xf, hxf, y, obs_cell, obserr=1.0, xlocal=3.0, tlocal=2.0, parm_infl=None, msw_infl=1.05,
+                 precision="f64", stream=None):
+    """4D-LETKF of the Lorenz-96 driver (lorenz96/letkf/letkf.f90:183-288,
+    nwindow > 1, fixed localisation): xf float64 [nslot, nx, ne] first guesses
+    of the slots; hxf [nslot, ny, ne] = H_n xf_n; y [nslot, ny]; obs_cell int32
+    [nslot, ny] (l96_obs_cell of each slot's H).  Departures and perturbations
+    per slot (:197-213), then for every analysis slot nn and point the
+    observations of all slots with tdif = |nn - n| (:217-254), the core, the
+    fixed-inflation reset and the update of slot nn.  parm_infl float64
+    [nslot, nx] (in/out).  Returns (xa [nslot, nx, ne], parm_infl)."""
+    import torch
+
+    nslot, nx, ne = xf.shape
+    ny = hxf.shape[1]
+    dev = xf.device
+    if parm_infl is None:
+        parm_infl = torch.full((nslot, nx), float(abs(msw_infl)), dtype=torch.float64, device=dev)
+    hd, dp = [], []
+    for n in range(nslot):
+        h_n, d_n, _ = K.obs_departure(hxf[n].contiguous(), y[n].contiguous(), stream=stream)
+        hd.append(h_n)
+        dp.append(d_n)
+    hdxf = torch.cat(hd).contiguous()          # rows n*ny + i
+    dep = torch.cat(dp).contiguous()
+    pix = torch.arange(1, nx + 1, dtype=torch.int32, device=dev)
+    xa = torch.empty_like(xf)
+    for nn in range(nslot):
+        offs, idx, rloc, rdiag = K.search_l96_4d(nx, obs_cell, pix, nn, xlocal, obserr, tlocal, stream)
+        rows, dl = K.gather_rows(idx, hdxf, dep, stream)
+        pinf = parm_infl[nn].contiguous()
+        if precision == "f64":
+            out = K.core_batch_f64(ne, offs, rows, rdiag, rloc, dl, pinf, stream=stream)
+            trans = out["trans"]
+        elif precision == "mixed":
+            f = lambda t: t.to(torch.float32).contiguous()
+            out = K.core_batch_mixed(ne, offs, f(rows), f(rdiag), f(rloc), f(dl), pinf, stream=stream)
+            trans = out["trans"].to(torch.float64)
+        else:
+            raise ValueError(f"precision {precision!r}")
+        if bool((out["status"] != K.LETKF_OK).any()):
+            raise K.LetkfError(int(out["status"].max()), "l96_letkf_4d: eigensolver")
+        if msw_infl > 0.0:
+            pinf.fill_(float(msw_infl))
+        parm_infl[nn] = pinf
+        xa[nn] = K.update_f64(xf[nn].reshape(1, nx, ne).contiguous(), trans.contiguous(), None, stream)[0]
+    return xa, parm_infl
+
+
+__all__ = ["speedy_sort_obs", "var_local_n2n", "speedy_letkf", "l96_letkf", "l96_letkf_4d", "speedy_obs_setup",
+           "speedy_cycle"]

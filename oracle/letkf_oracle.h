@@ -130,6 +130,8 @@ double oracle_scale_dist_zero_fac_square(void);
 /* ---- Lorenz-96 selection (lorenz96/letkf/letkf.f90:220-254), nwindow=1 ---- */
 int oracle_l96_select(int nx, int ny, const double* h /* ny x nx col-major */, int ix, double xlocal,
                       double tlocal, int* idx, double* rloc);
+int oracle_l96_select_4d(int nx, int ny, int nslot, const double* h, int slot, int ix, double xlocal, double tlocal,
+                         int* idx, double* rloc);
 
 /* ---- sweeps (das_letkf loops) ---- */
 /* Ensemble mean and perturbation, sequential member sum

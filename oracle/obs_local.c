@@ -453,6 +453,42 @@ int oracle_l96_select(int nx, int ny, const double* h, int ix, double xlocal, do
   return ny_loc;
 }
 
+/* 4D selection of the Lorenz-96 driver (lorenz96/letkf/letkf.f90:217-254):
+ * for analysis slot `slot` (1-based nn) the observations of every slot n in
+ * slot order, tdif = |nn - n| (0 when tlocal < 0), rloc = exp(-0.5 (dist /
+ * xlocal)^2) exp(-0.5 (tdif / tlocal)^2), dropped below 1e-4.  h holds nslot
+ * blocks of ny x nx (column-major); idx is the row n*ny + i (0-based) of the
+ * slot-stacked observation arrays. */
+int oracle_l96_select_4d(int nx, int ny, int nslot, const double* h, int slot, int ix, double xlocal, double tlocal,
+                         int* idx, double* rloc) {
+  const double xmaxloc = xlocal * 2.0 * sqrt(10.0 / 3.0);
+  int n, i, j, ny_loc = 0;
+  for (n = 1; n <= nslot; n++) {
+    const double* hn = h + (size_t)(n - 1) * nx * ny;
+    double tdif = (double)abs(slot - n);
+    if (tlocal < 0.0) tdif = 0.0;
+    for (i = 1; i <= ny; i++) {
+      double mx = hn[(size_t)0 * ny + (i - 1)];
+      for (j = 2; j <= nx; j++)
+        if (hn[(size_t)(j - 1) * ny + (i - 1)] > mx) mx = hn[(size_t)(j - 1) * ny + (i - 1)];
+      for (j = 1; j <= nx; j++)
+        if (mx == hn[(size_t)(j - 1) * ny + (i - 1)]) break;
+      {
+        int a = abs(j - ix), b = nx - abs(j - ix);
+        double dist = (double)(a < b ? a : b);
+        if (dist < xmaxloc) {
+          double r = exp(-0.5 * (dist / xlocal) * (dist / xlocal)) * exp(-0.5 * (tdif / tlocal) * (tdif / tlocal));
+          ny_loc++;
+          idx[ny_loc - 1] = (n - 1) * ny + (i - 1);
+          rloc[ny_loc - 1] = r;
+          if (r < 0.0001) ny_loc--;
+        }
+      }
+    }
+  }
+  return ny_loc;
+}
+
 /* speedy/common/common_speedy.f90:335-370 and letkf_tools.f90:96-112 */
 void oracle_ensmean(int npts, int ne, const double* x, double* mean, double* pert) {
   int p, m;

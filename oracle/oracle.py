@@ -44,6 +44,8 @@ def lib():
         _lib.oracle_scale_obs_local.argtypes = [C.c_void_p, d, d, d, d, pi, pd, pd]
         _lib.oracle_scale_dist_zero_fac.restype = d
         _lib.oracle_scale_dist_zero_fac_square.restype = d
+        _lib.oracle_l96_select_4d.restype = C.c_int
+        _lib.oracle_l96_select_4d.argtypes = [C.c_int, C.c_int, C.c_int, pd, C.c_int, C.c_int, d, d, pi, pd]
         _lib.oracle_l96_select.restype = C.c_int
         _lib.oracle_l96_select.argtypes = [C.c_int, C.c_int, pd, C.c_int, d, d, pi, pd]
         _lib.oracle_ensmean.argtypes = [C.c_int, C.c_int, pd, pd, pd]
@@ -280,6 +282,19 @@ def l96_select(h, ix, xlocal=3.0, tlocal=2.0):
     idx = np.zeros(ny, dtype=np.int32)
     rloc = np.zeros(ny)
     n = lib().oracle_l96_select(nx, ny, _pd(h), ix, xlocal, tlocal, _pi(idx), _pd(rloc))
+    return idx[:n].copy(), rloc[:n].copy()
+
+
+def l96_select_4d(h4d, slot, ix, xlocal=3.0, tlocal=2.0):
+    """h4d is (nslot, ny, nx); slot and ix are 1-based as in the reference.
+    Indices are rows n*ny + i of the slot-stacked observations."""
+    h4d = np.asarray(h4d, dtype=np.float64)
+    nslot, ny, nx = h4d.shape
+    hf = np.ascontiguousarray(np.stack([np.asfortranarray(h4d[n]).ravel(order="F") for n in range(nslot)]))
+    idx = np.zeros(max(nslot * ny, 1), dtype=np.int32)
+    rloc = np.zeros(max(nslot * ny, 1))
+    n = lib().oracle_l96_select_4d(nx, ny, nslot, _pd(hf), int(slot), int(ix), float(xlocal), float(tlocal),
+                                   _pi(idx), _pd(rloc))
     return idx[:n].copy(), rloc[:n].copy()
 
 

@@ -202,3 +202,99 @@ def test_speedy_das_letkf_matches_oracle(cuda):
             _close(anal3d[n, ilev, :, ij], ref, 1e-10)
         checked += 1
     assert checked > 40
+
+
+# ---------------------------------------------------------------- 4D Lorenz-96
+@pytest.mark.gpu
+@pytest.mark.parametrize("tlocal", [2.0, -1.0, 0.7])
+def test_l96_search_4d_matches_oracle(cuda, tlocal):
+    """4D selection (lorenz96/letkf/letkf.f90:217-254): three slots with their
+    own H (scattered cells, ties), every analysis slot, lists in slot and
+    observation order with tdif = |nn - n|."""
+    import torch
+
+    from letkf_gb300.core import l96_obs_cell, search_l96_4d
+
+    rng = np.random.default_rng(17)
+    nslot, nx, ny = 3, 120, 150
+    h4d = np.zeros((nslot, ny, nx))
+    for n in range(nslot):
+        cells = rng.integers(1, nx + 1, ny)
+        h4d[n, np.arange(ny), cells - 1] = 1.0
+        ties = rng.choice(ny, 10, replace=False)
+        h4d[n, ties, (cells[ties] + 5) % nx] = 1.0
+    cell = torch.stack([l96_obs_cell(_t(h4d[n], torch.float64, cuda)) for n in range(nslot)])
+    pix = torch.arange(1, nx + 1, dtype=torch.int32, device=cuda)
+    for slot in range(nslot):
+        offs, idx, rloc, rdiag = search_l96_4d(nx, cell, pix, slot, 3.0, 0.5, tlocal)
+        offs, idx, rloc = offs.cpu().numpy(), idx.cpu().numpy(), rloc.cpu().numpy()
+        assert np.all(rdiag.cpu().numpy() == 0.25)
+        for ix in range(1, nx + 1):
+            ri, rl = O.l96_select_4d(h4d, slot + 1, ix, 3.0, tlocal)
+            s = slice(offs[ix - 1], offs[ix])
+            np.testing.assert_array_equal(idx[s], ri, err_msg=f"slot {slot} ix {ix}")
+            np.testing.assert_allclose(rloc[s], rl, rtol=1e-14, atol=0)
+
+
+@pytest.mark.gpu
+def test_l96_letkf_4d_matches_oracle(cuda):
+    """Two-slot 4D-LETKF analysis (nwindow = 2, fixed localisation and
+    inflation) on the Lorenz-96 ring against the oracle's selection + core +
+    update of each analysis slot."""
+    import torch
+
+    from letkf_gb300.core import l96_obs_cell
+    from letkf_gb300.drivers import l96_letkf_4d
+
+    rng = np.random.default_rng(23)
+    nslot, nx, ne = 2, 40, 20
+    xf = 8.0 + 2.0 * rng.standard_normal((nslot, nx, ne))
+    h = np.eye(nx)
+    hxf = np.stack([h @ xf[n] for n in range(nslot)])
+    y = 8.0 + rng.standard_normal((nslot, nx))
+    h4d = np.stack([h, h])
+    cell = torch.stack([l96_obs_cell(_t(h, torch.float64, cuda))] * nslot)
+    xa, infl = l96_letkf_4d(_t(xf, torch.float64, cuda), _t(hxf, torch.float64, cuda), _t(y, torch.float64, cuda),
+                            cell, obserr=1.0, xlocal=3.0, tlocal=2.0)
+    xa = xa.cpu().numpy()
+    assert np.all(infl.cpu().numpy() == 1.05)
+    # oracle: per-slot departures, then every analysis slot over both slots' observations
+    hdxf, dep = [], []
+    for n in range(nslot):
+        m = hxf[n][:, 0].copy()
+        for k in range(1, ne):
+            m = m + hxf[n][:, k]
+        m = m / ne
+        hdxf.append(hxf[n] - m[:, None])
+        dep.append(y[n] - m)
+    hdxf, dep = np.concatenate(hdxf), np.concatenate(dep)
+    for nn in range(nslot):
+        xm = xf[nn][:, 0].copy()
+        for k in range(1, ne):
+            xm = xm + xf[nn][:, k]
+        xm = xm / ne
+        for ix in range(1, nx + 1):
+            ri, rl = O.l96_select_4d(h4d, nn + 1, ix, 3.0, 2.0)
+            r = O.letkf_core(hdxf[ri], np.ones(ri.size), rl, dep[ri], 1.05)
+            ref = xm[ix - 1] + (xf[nn][ix - 1] - xm[ix - 1]) @ r["trans"]
+            _close(xa[nn, ix - 1], ref, 1e-10)
+
+
+def test_oracle_l96_select_4d_reduces_to_one_slot_and_weights_time():
+    """One slot equals the single-slot selection; further slots repeat the
+    spatial weights times exp(-0.5 (tdif/tlocal)^2) in slot order."""
+    nx = 40
+    h = np.eye(nx)
+    i1, r1 = O.l96_select(h, 7, 3.0, 2.0)
+    i4, r4 = O.l96_select_4d(h[None], 1, 7, 3.0, 2.0)
+    np.testing.assert_array_equal(i1, i4)
+    np.testing.assert_array_equal(r1, r4)
+    i3, r3 = O.l96_select_4d(np.stack([h, h, h]), 2, 7, 3.0, 2.0)
+    n = i1.size
+    assert i3.size == 3 * n
+    np.testing.assert_array_equal(i3[:n], i1)
+    np.testing.assert_array_equal(i3[n:2 * n], i1 + nx)
+    np.testing.assert_allclose(r3[n:2 * n], r1, rtol=1e-15)                       # tdif = 0
+    np.testing.assert_allclose(r3[:n], r1 * np.exp(-0.5 * 0.25), rtol=1e-15)       # tdif = 1
+    _, rneg = O.l96_select_4d(np.stack([h, h, h]), 2, 7, 3.0, -1.0)
+    np.testing.assert_allclose(rneg[:n], r1, rtol=1e-15)                          # no time localisation
