@@ -68,9 +68,12 @@ int letkf_core_batch_f64(int ne, int npts, const int64_t* offs, const double* ro
                          double* parm_infl, double* trans, double* transm, double* pao,
                          int rdiag_wloc, double minfl, int* status, void* stream);
 
-/* Mixed-precision batched core: FP32 rows/weights, FP32 Gram and eigensolver
- * with an FP64 refinement of the transform; outputs FP32 trans/transm and
- * FP64 inflation.  Same layout and semantics as letkf_core_batch_f64. */
+/* Mixed-precision batched core: FP32 rows/weights and Gram; the transform by
+ * spectrum-scaled Newton-Schulz (W = sqrt((k-1)/s) (A/s)^(-1/2)) where
+ * mtx_eigen's truncation cannot act (c > 0, tr(G) < 1e6 c), else by the
+ * parallel Jacobi eigensolver with the reference's truncation; outputs FP32
+ * trans/transm and FP64 inflation.  Same layout and semantics as
+ * letkf_core_batch_f64. */
 int letkf_core_batch_mixed(int ne, int npts, const int64_t* offs, const float* rows,
                            const float* rdiag, const float* rloc, const float* dep,
                            double* parm_infl, float* trans, float* transm, int rdiag_wloc,

@@ -1,8 +1,11 @@
 // core_mixed.cu -- batched mixed-precision letkf_core on packed local rows.
 //
-// One CTA per point (persistent grid).  FP32 Gram and Jacobi eigensolver on
-// chip; FP64 for the inflation sums.  Outputs FP32 trans / transm with the
-// semantics of common/common_letkf.f90:50-243 (transm present: trans = T,
+// One CTA per point (persistent grid).  FP32 Gram on chip; the transform by
+// spectrum-scaled Newton-Schulz (W = sqrt((k-1)/s) (A/s)^(-1/2),
+// wbar = Z (Z b) / s) where mtx_eigen's truncation cannot act (c > 0 and
+// tr(G) < 1e6 c), else the parallel Jacobi eigensolver with the reference's
+// truncation; FP64 for the inflation sums.  Outputs FP32 trans / transm with
+// the semantics of common/common_letkf.f90:50-243 (transm present: trans = T,
 // transm = wbar; absent: trans = T + wbar 1^T).
 #include "mixed_core.cuh"
 
@@ -12,7 +15,8 @@ template <int NP>
 __global__ void __launch_bounds__(MixedCfg<NP>::NT) core_mixed_kernel(
     int n, int npts, const int64_t* __restrict__ offs, const float* __restrict__ rows,
     const float* __restrict__ rdiag, const float* __restrict__ rloc, const float* __restrict__ dep,
-    double* parm_infl, float* trans, float* transm, int rdiag_wloc, double minfl, int* status, int max_sweeps) {
+    double* parm_infl, float* trans, float* transm, int rdiag_wloc, double minfl, int* status, int max_sweeps,
+    int use_ns) {
   using C = MixedCfg<NP>;
   using S = MixedSmem<NP>;
   extern __shared__ __align__(16) float sm[];
@@ -55,6 +59,39 @@ __global__ void __launch_bounds__(MixedCfg<NP>::NT) core_mixed_kernel(
     const float c = (float)((double)(n - 1) / infl);
     for (int i = tid; i < NP; i += C::NT) sm[S::A + i * NP + i] += c;
     __syncthreads();
+    if (use_ns && c > 0.f && trace < 1.0e6 * (double)c) {
+      int its = 0;
+      const float s = ns_invsqrt<NP>(sm, c, 24, &its);
+      const float* Z = sm + S::V;
+      if (tid < NP) {
+        float g = 0.f;
+        for (int j = 0; j < NP; j++) g = fmaf(Z[j * NP + tid], sm[S::B + j], g);
+        sm[S::G + tid] = g;
+      }
+      __syncthreads();
+      if (tid < NP) {
+        float w = 0.f;
+        for (int j = 0; j < NP; j++) w = fmaf(Z[j * NP + tid], sm[S::G + j], w);
+        sm[S::WB + tid] = w / s;
+      }
+      __syncthreads();
+      const float coef = sqrtf((float)(n - 1) / s);
+      const float* wb = sm + S::WB;
+      const bool sep = transm != nullptr;
+      for (int idx = tid; idx < n * n; idx += C::NT) {
+        const int j = idx / n, i = idx - j * n;  // trans(i, j): background member i, analysis member j
+        const float w = coef * Z[i * NP + j];
+        T[idx] = sep ? w : w + wb[i];
+      }
+      if (sep)
+        for (int i = tid; i < n; i += C::NT) transm[(size_t)p * n + i] = wb[i];
+      if (tid == 0) {
+        parm_infl[p] = infl_update(n, infl, acc.p1, trace, acc.p3);
+        status[p] = LETKF_OK;
+      }
+      __syncthreads();
+      continue;
+    }
     jacobi_eig<NP>(sm, max_sweeps);
     const int st = eig_postprocess<NP>(sm, n);
     if (st != LETKF_OK) {
@@ -82,19 +119,20 @@ template <int NP>
 static int launch_mixed_np(int ne, int npts, const int64_t* offs, const float* rows, const float* rdiag,
                            const float* rloc, const float* dep, double* parm_infl, float* trans, float* transm,
                            int rdiag_wloc, double minfl, int* status, cudaStream_t stream) {
-  using S = MixedSmem<NP>;
+  // the Newton-Schulz product T sits after the Jacobi layout
+  const size_t bytes = sizeof(float) * (size_t)NSSmem<NP>::TOTAL;
   auto kern = core_mixed_kernel<NP>;
-  cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::BYTES);
+  cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (err != cudaSuccess) return cuda_status(err);
   int dev = 0, nsm = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, MixedCfg<NP>::NT, S::BYTES);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, MixedCfg<NP>::NT, bytes);
   if (per_sm < 1) per_sm = 1;
   int grid = nsm * per_sm;
   if (grid > npts) grid = npts;
-  kern<<<grid, MixedCfg<NP>::NT, S::BYTES, stream>>>(ne, npts, offs, rows, rdiag, rloc, dep, parm_infl, trans,
-                                                      transm, rdiag_wloc, minfl, status, 12);
+  kern<<<grid, MixedCfg<NP>::NT, bytes, stream>>>(ne, npts, offs, rows, rdiag, rloc, dep, parm_infl, trans, transm,
+                                                   rdiag_wloc, minfl, status, 12, 1);
   note_launch();
   return cuda_status(cudaGetLastError());
 }
