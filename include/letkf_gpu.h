@@ -162,6 +162,27 @@ int letkf_search_scale(int nlon, int nlat, const int* nobsgrd /* [(nlon+1)*nlat]
                        const double* var_local_row, const double* params, const int64_t* offs,
                        int* nobsl, int* idx, double* rloc, double* rdiag, void* stream);
 
+/* GFS lat/lon search (gfs/letkf/letkf_tools.f90:686-955): the SPEEDY box walk
+ * over the same bucket-sorted observations with the GFS tests:
+ * dlat_zero = max(dist_zero, dist_zero_rain) / pi / re * 180 and
+ * dlon_zero = dlat_zero / cos(lat pi / 180) per point; vertical distance
+ * |ln obsdat - ln p| for ps, |ln base_obsv_rain - ln p| against dist_zerov_rain
+ * for rain (19999), 0 for TC obs (>= 99991), |ln obslev - ln p| otherwise;
+ * horizontal cut-off dist_zero_rain for rain; rloc = exp(-0.5 ((d/sigma_h)^2 +
+ * (dlev/sigma_obsv)^2)) (sigma_h = sigma_obs_rain for rain) times the
+ * variable localisation; rdiag = err^2.  prlev[npts] is the point's pressure
+ * (pfull; the reference's rlev).  var_local_row[6] (u/v, t/tv, q/rh, ps, rain,
+ * tc) or NULL for nvar = 0 (no variable localisation, as the EFSO and
+ * obs-space calls use); with it, element codes outside the GFS list are not
+ * selected.  params[8]: dist_zero, dist_zerov, dist_zero_rain,
+ * dist_zerov_rain, sigma_obs, sigma_obsv, sigma_obs_rain, base_obsv_rain.
+ * idx is the sorted observation index (the reference's oindex). */
+int letkf_search_gfs(int nlon, int nlat, const double* lon, const double* lat, const int* nobsgrd, int nobs,
+                     const double* obselm, const double* obslon, const double* obslat, const double* obslev,
+                     const double* obsdat, const double* obserr, int npts, const double* plon, const double* plat,
+                     const double* prlev, const double* var_local_row, const double* params, const int64_t* offs,
+                     int* nobsl, int* idx, double* rloc, double* rdiag, void* stream);
+
 /* SPEEDY lat/lon search (speedy/letkf/letkf_tools.f90:272-603).  nobsgrd is
  * [nlon*nlat] (i fastest); obselm holds the SPEEDY element ids.
  * params[5]: dist_zero, dist_zerov, dlat_zero, sigma_obs, sigma_obsv.

@@ -352,6 +352,41 @@ def search_speedy(grid, obs, pts, params, var_local_row, stream=None):
     return offs, idx[:total], rloc[:total], rdiag[:total]
 
 
+GFS_PARAM_ORDER = ("dist_zero", "dist_zerov", "dist_zero_rain", "dist_zerov_rain", "sigma_obs", "sigma_obsv",
+                   "sigma_obs_rain", "base_obsv_rain")
+
+
+def search_gfs(grid, obs, pts, params, var_local_row=None, stream=None):
+    """GFS lat/lon search (gfs/letkf/letkf_tools.f90:686-955) on device tensors.
+    grid: dict lon, lat (float64), nobsgrd (int32 [nlat, nlon]); obs: dict elm,
+    lon, lat, lev, dat, err (float64, bucket-sorted); pts: dict lon, lat, rlev
+    (float64, rlev = the point's pressure); params: dict with GFS_PARAM_ORDER
+    keys; var_local_row: 6 weights or None (nvar = 0).  Returns (offs, idx,
+    rloc, rdiag)."""
+    import torch
+
+    dev = obs["lon"].device
+    npts = pts["lon"].numel()
+    nlat, nlon = grid["nobsgrd"].shape
+    nobs = obs["lon"].numel()
+    P = torch.tensor([float(params[k]) for k in GFS_PARAM_ORDER], dtype=torch.float64)
+    vl = None if var_local_row is None else torch.as_tensor(var_local_row, dtype=torch.float64, device=dev)
+    nobsl = torch.empty(npts, dtype=torch.int32, device=dev)
+    args = (nlon, nlat, _dptr(grid["lon"]), _dptr(grid["lat"]), _dptr(grid["nobsgrd"]), nobs, _dptr(obs["elm"]),
+            _dptr(obs["lon"]), _dptr(obs["lat"]), _dptr(obs["lev"]), _dptr(obs["dat"]), _dptr(obs["err"]), npts,
+            _dptr(pts["lon"]), _dptr(pts["lat"]), _dptr(pts["rlev"]), _dptr(vl),
+            C.c_void_p(P.data_ptr()))
+    check(lib().letkf_search_gfs(*args, None, _dptr(nobsl), None, None, None, _stream(stream)), "search_gfs")
+    offs = exclusive_scan(nobsl, stream)
+    total = int(offs[-1].item())
+    idx = torch.empty(max(total, 1), dtype=torch.int32, device=dev)
+    rloc = torch.empty(max(total, 1), dtype=torch.float64, device=dev)
+    rdiag = torch.empty(max(total, 1), dtype=torch.float64, device=dev)
+    check(lib().letkf_search_gfs(*args, _dptr(offs), None, _dptr(idx), _dptr(rloc), _dptr(rdiag), _stream(stream)),
+          "search_gfs")
+    return offs, idx[:total], rloc[:total], rdiag[:total]
+
+
 def l96_obs_cell(h, stream=None):
     """Grid index (1-based) of each Lorenz-96 observation: the first maximum of
     its row of h (ny, nx) (lorenz96/letkf/letkf.f90:226-228).  h: device tensor."""

@@ -24,6 +24,11 @@ int launch_search_speedy(int, int, const double*, const double*, const int*, int
                          const double*, const double*, const double*, const double*, int, const double*,
                          const double*, const double*, const int*, const double*, const double*, const double*,
                          const int64_t*, int*, int*, double*, double*, cudaStream_t);
+int launch_search_gfs(int nlon, int nlat, const double* lon, const double* lat, const int* G, const double* elm,
+                      const double* olon, const double* olat, const double* olev, const double* odat,
+                      const double* oerr, int npts, const double* plon, const double* plat, const double* prlev,
+                      const double* var_local, const double* params, const int64_t* offs, int* nobsl, int* idx,
+                      double* rloc, double* rdiag, cudaStream_t stream);
 int launch_exclusive_scan(int, const int*, int64_t*, int64_t*, cudaStream_t);
 int launch_gather_rows(int, int64_t, const int*, const void*, const void*, int, void*, void*, cudaStream_t);
 
@@ -179,6 +184,25 @@ int letkf_search_speedy(int nlon, int nlat, const double* lon, const double* lat
   return launch_search_speedy(nlon, nlat, lon, lat, nobsgrd, nobs, obselm, obslon, obslat, obslev, obsdat, obserr,
                               npts, plon, plat, pdlon_zero, pilev, plogpfm, var_local_row, hp, offs, nobsl, idx, rloc,
                               rdiag, (cudaStream_t)stream);
+}
+
+int letkf_search_gfs(int nlon, int nlat, const double* lon, const double* lat, const int* nobsgrd, int nobs,
+                     const double* obselm, const double* obslon, const double* obslat, const double* obslev,
+                     const double* obsdat, const double* obserr, int npts, const double* plon, const double* plat,
+                     const double* prlev, const double* var_local_row, const double* params, const int64_t* offs,
+                     int* nobsl, int* idx, double* rloc, double* rdiag, void* stream) {
+  if (nlon < 2 || nlat < 3 || nobs < 0 || npts < 0 || !nobsgrd || !params) return LETKF_ERR_ARG;
+  if (npts > 0 && (!plon || !plat || !prlev)) return LETKF_ERR_ARG;
+  if (!idx && !nobsl) return LETKF_ERR_ARG;
+  if (idx && (!offs || !rloc || !rdiag)) return LETKF_ERR_ARG;
+  if (!have_gpu()) return LETKF_ERR_NOGPU;
+  double hp[8];
+  if (cudaMemcpy(hp, params, sizeof(double) * 8, cudaMemcpyDefault) != cudaSuccess) {
+    memcpy(hp, params, sizeof(double) * 8);
+    cudaGetLastError();
+  }
+  return launch_search_gfs(nlon, nlat, lon, lat, nobsgrd, obselm, obslon, obslat, obslev, obsdat, obserr, npts, plon,
+                           plat, prlev, var_local_row, hp, offs, nobsl, idx, rloc, rdiag, (cudaStream_t)stream);
 }
 
 int letkf_exclusive_scan(int n, const int* counts, int64_t* offs, void* stream) {

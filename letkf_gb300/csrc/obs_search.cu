@@ -113,7 +113,61 @@ struct SpeedyCtx {
   const int* G;
   const double *elm, *olon, *olat, *olev, *odat, *oerr, *var_local;
   double dist_zero, dist_zerov, sigma_obs, sigma_obsv;
+  // GFS variant (gfs/letkf/letkf_tools.f90:686-925)
+  int gfs;
+  double dist_zero_rain, dist_zerov_rain, sigma_obs_rain, base_obsv_rain;
 };
+
+// GFS candidate test (gfs/letkf/letkf_tools.f90:833-915); logrlev = ln p of
+// the point; var_local (6 classes) may be NULL (nvar = 0)
+__device__ __forceinline__ void gfs_range(const SpeedyCtx& c, int ib, int ie, double lon1, double lat1,
+                                          double logrlev, int* idx, double* rloc, double* rdiag, int64_t base,
+                                          int& cnt) {
+  for (int ip = ib; ip <= ie; ip++) {
+    const int ob = ip - 1;
+    const int elm = (int)llround(c.elm[ob]);
+    double dlev;
+    if (elm == 14593) {
+      dlev = fabs(log(c.odat[ob]) - logrlev);
+      if (dlev > c.dist_zerov) continue;
+    } else if (elm == 19999) {
+      dlev = fabs(log(c.base_obsv_rain) - logrlev);
+      if (dlev > c.dist_zerov_rain) continue;
+    } else if (elm >= 99991) {
+      dlev = 0.0;
+    } else {
+      dlev = fabs(log(c.olev[ob]) - logrlev);
+      if (dlev > c.dist_zerov) continue;
+    }
+    const double dist = distll(c.olon[ob], c.olat[ob], lon1, lat1);
+    if (dist > (elm == 19999 ? c.dist_zero_rain : c.dist_zero)) continue;
+    double vl = 1.0;
+    if (c.var_local) {
+      int iobs;
+      switch (elm) {
+        case 2819: case 2820: iobs = 1; break;
+        case 3073: case 3074: iobs = 2; break;
+        case 3330: case 3331: iobs = 3; break;
+        case 14593: iobs = 4; break;
+        case 19999: iobs = 5; break;
+        case 99991: case 99992: case 99993: iobs = 6; break;
+        default: iobs = 0; break;  // class undefined in the reference: not selected
+      }
+      if (iobs == 0) continue;
+      vl = c.var_local[iobs - 1];
+      if (vl < 2.2250738585072014e-308) continue;
+    }
+    if (idx) {
+      const double a = dist / (elm == 19999 ? c.sigma_obs_rain : c.sigma_obs), b = dlev / c.sigma_obsv;
+      double r = exp(-0.5 * (a * a + b * b));
+      if (c.var_local) r = r * vl;
+      idx[base + cnt] = ob;
+      rdiag[base + cnt] = c.oerr[ob] * c.oerr[ob];
+      rloc[base + cnt] = r;
+    }
+    cnt++;
+  }
+}
 
 // Test candidates [ib, ie] (1-based, inclusive) for one point; appends.
 __device__ __forceinline__ void speedy_range(const SpeedyCtx& c, int ib, int ie, double lon1, double lat1, int ilev,
@@ -163,7 +217,8 @@ __device__ __forceinline__ void speedy_sub(const SpeedyCtx& c, int imin, int ima
     else ib = 1;
     const int ie = c.G[(size_t)(j - 1) * nlon + imax - 1];
     if (ie - ib + 1 == 0) continue;
-    speedy_range(c, ib, ie, lon1, lat1, ilev, logpfm, idx, rloc, rdiag, base, cnt);
+    if (c.gfs) gfs_range(c, ib, ie, lon1, lat1, logpfm, idx, rloc, rdiag, base, cnt);
+    else speedy_range(c, ib, ie, lon1, lat1, ilev, logpfm, idx, rloc, rdiag, base, cnt);
   }
 }
 
@@ -175,9 +230,12 @@ __global__ void search_speedy_kernel(SpeedyCtx c, int npts, const double* __rest
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= npts) return;
   const int nlon = c.nlon, nlat = c.nlat;
-  const double lon1 = plon[p], lat1 = plat[p], logpfm = plogp[p];
-  const int ilev = pilev[p];
-  double minlon = lon1 - pdlon[p], maxlon = lon1 + pdlon[p];
+  const double lon1 = plon[p], lat1 = plat[p];
+  // SPEEDY: ln p_full of the point and its level; GFS: ln of the point's pressure
+  const double logpfm = c.gfs ? log(plogp[p]) : plogp[p];
+  const int ilev = c.gfs ? 0 : pilev[p];
+  const double dlon = c.gfs ? dlat_zero / cos(lat1 * 3.1415926535 / 180.0) : pdlon[p];
+  double minlon = lon1 - dlon, maxlon = lon1 + dlon;
   const double minlat = lat1 - dlat_zero, maxlat = lat1 + dlat_zero;
   if (maxlon - minlon >= 360.0) {
     minlon = 0.0;
@@ -289,10 +347,49 @@ int launch_search_speedy(int nlon, int nlat, const double* lon, const double* la
   c.dist_zerov = params[1];
   c.sigma_obs = params[3];
   c.sigma_obsv = params[4];
+  c.gfs = 0;
+  c.dist_zero_rain = c.dist_zerov_rain = c.sigma_obs_rain = c.base_obsv_rain = 0.0;
   (void)nobs;
   const int bs = search_block(npts);
   search_speedy_kernel<<<(npts + bs - 1) / bs, bs, 0, stream>>>(c, npts, plon, plat, pdlon, pilev, plogp, params[2],
                                                                   offs, nobsl, idx, rloc, rdiag);
+  note_launch();
+  return cuda_status(cudaGetLastError());
+}
+
+int launch_search_gfs(int nlon, int nlat, const double* lon, const double* lat, const int* G, const double* elm,
+                      const double* olon, const double* olat, const double* olev, const double* odat,
+                      const double* oerr, int npts, const double* plon, const double* plat, const double* prlev,
+                      const double* var_local, const double* params, const int64_t* offs, int* nobsl, int* idx,
+                      double* rloc, double* rdiag, cudaStream_t stream) {
+  if (npts <= 0) return npts == 0 ? LETKF_OK : LETKF_ERR_ARG;
+  SpeedyCtx c;
+  c.nlon = nlon;
+  c.nlat = nlat;
+  c.lon = lon;
+  c.lat = lat;
+  c.G = G;
+  c.elm = elm;
+  c.olon = olon;
+  c.olat = olat;
+  c.olev = olev;
+  c.odat = odat;
+  c.oerr = oerr;
+  c.var_local = var_local;
+  c.gfs = 1;
+  c.dist_zero = params[0];
+  c.dist_zerov = params[1];
+  c.dist_zero_rain = params[2];
+  c.dist_zerov_rain = params[3];
+  c.sigma_obs = params[4];
+  c.sigma_obsv = params[5];
+  c.sigma_obs_rain = params[6];
+  c.base_obsv_rain = params[7];
+  const double dz = c.dist_zero > c.dist_zero_rain ? c.dist_zero : c.dist_zero_rain;
+  const double dlat_zero = dz / 3.1415926535 / 6371.3e3 * 180.0;  // gfs/letkf/letkf_tools.f90:712
+  const int bs = search_block(npts);
+  search_speedy_kernel<<<(npts + bs - 1) / bs, bs, 0, stream>>>(c, npts, plon, plat, nullptr, nullptr, prlev,
+                                                                  dlat_zero, offs, nobsl, idx, rloc, rdiag);
   note_launch();
   return cuda_status(cudaGetLastError());
 }

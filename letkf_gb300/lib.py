@@ -49,6 +49,8 @@ _SIGS = {
     "letkf_update_f64": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
     "letkf_search_scale": (_i, [_i, _i, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp,
                                 _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "letkf_search_gfs": (_i, [_i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp,
+                              _vp, _vp, _vp, _vp, _vp, _vp]),
     "letkf_search_speedy": (_i, [_i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp,
                                  _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "letkf_exclusive_scan": (_i, [_i, _vp, _vp, _vp]),

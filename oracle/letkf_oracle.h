@@ -86,6 +86,15 @@ typedef struct {
 int oracle_speedy_obs_local(const oracle_speedy_obs* o, double lon1, double lat1, double dlon_zero,
                             int ilev, double logpfm, int* idx, double* rloc, double* rdiag);
 
+/* GFS obs_local (gfs/letkf/letkf_tools.f90:686-925) on the SPEEDY bucket layout */
+typedef struct {
+  double dist_zero, dist_zerov, dist_zero_rain, dist_zerov_rain;
+  double sigma_obs, sigma_obsv, sigma_obs_rain, base_obsv_rain;
+  const double* var_local; /* [6] (u/v, t/tv, q/rh, ps, rain, tc) or NULL */
+} oracle_gfs_params;
+int oracle_gfs_obs_local(const oracle_speedy_obs* o, const oracle_gfs_params* g, double rlon, double rlat,
+                         double rlev, int* idx, double* rloc, double* rdiag);
+
 /* ---- SCALE Cartesian search (scale/letkf/letkf_obs.f90, letkf_tools.f90) ---- */
 /* obs classes used for the vertical / horizontal scale switch */
 enum { ORC_CLS_DEFAULT = 0, ORC_CLS_PS = 1, ORC_CLS_RAIN = 2, ORC_CLS_RADAR_REF = 3,

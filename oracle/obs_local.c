@@ -121,20 +121,20 @@ static int first_below(double x, const double* axis, int lim) {
 #define ID_RAIN 9999
 
 /* speedy/letkf/letkf_tools.f90:272-573 */
-int oracle_speedy_obs_local(const oracle_speedy_obs* o, double lon1, double lat1, double dlon_zero,
-                            int ilev, double logpfm, int* idx, double* rloc, double* rdiag) {
+/* the candidate box of a point (speedy/letkf/letkf_tools.f90:297-452, the
+ * same steps as gfs/letkf/letkf_tools.f90:709-825): sorted-observation
+ * indices (1-based) into nobs_use, returns their number */
+static int collect_box(const oracle_speedy_obs* o, double lon1, double lat1, double dlon_zero, double dlat_zero,
+                       int* nobs_use) {
   const int nlon = o->nlon, nlat = o->nlat;
   const double* lon = o->lon;
   const double* lat = o->lat;
-  double minlon, maxlon, minlat, maxlat, dist, dlev;
-  int imin, imax, jmin, jmax, n, nn, iobs, nobsl;
-  int* nobs_use;
-  if (o->nobs <= 0) return 0;
-  nobs_use = (int*)malloc(sizeof(int) * (size_t)o->nobs);
+  double minlon, maxlon, minlat, maxlat;
+  int imin, imax, jmin, jmax, nn;
   minlon = lon1 - dlon_zero;
   maxlon = lon1 + dlon_zero;
-  minlat = lat1 - o->dlat_zero;
-  maxlat = lat1 + o->dlat_zero;
+  minlat = lat1 - dlat_zero;
+  maxlat = lat1 + dlat_zero;
   if (maxlon - minlon >= 360.0) {
     minlon = 0.0;
     maxlon = 360.0;
@@ -207,7 +207,17 @@ int oracle_speedy_obs_local(const oracle_speedy_obs* o, double lon1, double lat1
       }
     }
   }
-  nn = nn - 1;
+  return nn - 1;
+}
+
+int oracle_speedy_obs_local(const oracle_speedy_obs* o, double lon1, double lat1, double dlon_zero,
+                            int ilev, double logpfm, int* idx, double* rloc, double* rdiag) {
+  double dist, dlev;
+  int n, nn, iobs, nobsl;
+  int* nobs_use;
+  if (o->nobs <= 0) return 0;
+  nobs_use = (int*)malloc(sizeof(int) * (size_t)o->nobs);
+  nn = collect_box(o, lon1, lat1, dlon_zero, o->dlat_zero, nobs_use);
   nobsl = 0;
   for (n = 1; n <= nn; n++) {
     int ob = nobs_use[n - 1] - 1; /* 0-based sorted index */
@@ -451,6 +461,86 @@ int oracle_l96_select(int nx, int ny, const double* h, int ix, double xlocal, do
     }
   }
   return ny_loc;
+}
+
+/* GFS element ids (gfs/common/common_obs_gfs.f90:48-61) */
+#define GFS_U 2819
+#define GFS_V 2820
+#define GFS_T 3073
+#define GFS_TV 3074
+#define GFS_Q 3330
+#define GFS_RH 3331
+#define GFS_PS 14593
+#define GFS_RAIN 19999
+#define GFS_TCLON 99991
+#define GFS_TCLAT 99992
+#define GFS_TCMIP 99993
+
+/* obs_local of the GFS driver (gfs/letkf/letkf_tools.f90:686-925) at a point
+ * (rlon, rlat, pressure rlev): the SPEEDY box with dlat_zero = max(dist_zero,
+ * dist_zero_rain) / pi / re * 180 and dlon_zero = dlat_zero / cos(rlat pi /
+ * 180); vertical distance from ln(obsdat) for ps, ln(base_obsv_rain) (against
+ * dist_zerov_rain) for rain, 0 for TC obs, ln(obslev) otherwise; horizontal
+ * cut-off dist_zero_rain for rain; variable localisation over six classes when
+ * var_local != NULL (element codes outside the GFS list are then not
+ * selected: the reference leaves their class undefined). */
+int oracle_gfs_obs_local(const oracle_speedy_obs* o, const oracle_gfs_params* g, double rlon, double rlat,
+                         double rlev, int* idx, double* rloc, double* rdiag) {
+  const double pi = 3.1415926535, re = 6371.3e3;
+  double dlat_zero, dlon_zero, dist, dlev, logrlev;
+  int n, nn, iobs = 0, nobsl;
+  int* nobs_use;
+  if (o->nobs <= 0) return 0;
+  nobs_use = (int*)malloc(sizeof(int) * (size_t)o->nobs);
+  dlat_zero = (g->dist_zero > g->dist_zero_rain ? g->dist_zero : g->dist_zero_rain) / pi / re * 180.0;
+  dlon_zero = dlat_zero / cos(rlat * pi / 180.0);
+  nn = collect_box(o, rlon, rlat, dlon_zero, dlat_zero, nobs_use);
+  logrlev = log(rlev);
+  nobsl = 0;
+  for (n = 1; n <= nn; n++) {
+    const int ob = nobs_use[n - 1] - 1;
+    const int elm = (int)lround(o->obselm[ob]);
+    if (elm == GFS_PS) {
+      dlev = fabs(log(o->obsdat[ob]) - logrlev);
+      if (dlev > g->dist_zerov) continue;
+    } else if (elm == GFS_RAIN) {
+      dlev = fabs(log(g->base_obsv_rain) - logrlev);
+      if (dlev > g->dist_zerov_rain) continue;
+    } else if (elm >= GFS_TCLON) {
+      dlev = 0.0;
+    } else {
+      dlev = fabs(log(o->obslev[ob]) - logrlev);
+      if (dlev > g->dist_zerov) continue;
+    }
+    oracle_com_distll_1(o->obslon[ob], o->obslat[ob], rlon, rlat, &dist);
+    if (elm == GFS_RAIN) {
+      if (dist > g->dist_zero_rain) continue;
+    } else {
+      if (dist > g->dist_zero) continue;
+    }
+    if (g->var_local) {
+      switch (elm) {
+        case GFS_U: case GFS_V: iobs = 1; break;
+        case GFS_T: case GFS_TV: iobs = 2; break;
+        case GFS_Q: case GFS_RH: iobs = 3; break;
+        case GFS_PS: iobs = 4; break;
+        case GFS_RAIN: iobs = 5; break;
+        case GFS_TCLON: case GFS_TCLAT: case GFS_TCMIP: iobs = 6; break;
+        default: iobs = 0; break;
+      }
+      if (iobs == 0 || g->var_local[iobs - 1] < 2.2250738585072014e-308) continue;
+    }
+    idx[nobsl] = ob;
+    rdiag[nobsl] = o->obserr[ob] * o->obserr[ob];
+    {
+      const double a = dist / (elm == GFS_RAIN ? g->sigma_obs_rain : g->sigma_obs), b = dlev / g->sigma_obsv;
+      rloc[nobsl] = exp(-0.5 * (a * a + b * b));
+    }
+    if (g->var_local) rloc[nobsl] = rloc[nobsl] * g->var_local[iobs - 1];
+    nobsl++;
+  }
+  free(nobs_use);
+  return nobsl;
 }
 
 /* 4D selection of the Lorenz-96 driver (lorenz96/letkf/letkf.f90:217-254):

@@ -37,6 +37,8 @@ def lib():
         _lib.oracle_com_distll_1.argtypes = [d, d, d, d, pd]
         _lib.oracle_speedy_sort_obs.restype = C.c_int
         _lib.oracle_speedy_sort_obs.argtypes = [C.c_int, C.c_int, pd, pd, C.c_int, pd, pd, pi, pi]
+        _lib.oracle_gfs_obs_local.restype = C.c_int
+        _lib.oracle_gfs_obs_local.argtypes = [C.c_void_p, C.c_void_p, d, d, d, pi, pd, pd]
         _lib.oracle_speedy_obs_local.restype = C.c_int
         _lib.oracle_speedy_obs_local.argtypes = [C.c_void_p, d, d, d, C.c_int, d, pi, pd, pd]
         _lib.oracle_scale_sort_obs.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, pd, pd, pi, pi]
@@ -187,6 +189,28 @@ class SpeedyObs:
         if nl < 0:
             raise ValueError("unknown observation element id")
         return idx[:nl].copy(), rloc[:nl].copy(), rdiag[:nl].copy()
+
+
+class _GfsParams(C.Structure):
+    _fields_ = [("dist_zero", C.c_double), ("dist_zerov", C.c_double), ("dist_zero_rain", C.c_double),
+                ("dist_zerov_rain", C.c_double), ("sigma_obs", C.c_double), ("sigma_obsv", C.c_double),
+                ("sigma_obs_rain", C.c_double), ("base_obsv_rain", C.c_double), ("var_local", C.c_void_p)]
+
+
+def gfs_obs_local(so, params, rlon, rlat, rlev, var_local=None):
+    """obs_local of the GFS driver (gfs/letkf/letkf_tools.f90:686-925) on the
+    sorted observations of a SpeedyObs `so`.  params: dist_zero, dist_zerov,
+    dist_zero_rain, dist_zerov_rain, sigma_obs, sigma_obsv, sigma_obs_rain,
+    base_obsv_rain; var_local: 6 weights or None.  Returns (idx, rloc, rdiag)."""
+    vl = None if var_local is None else _f64(var_local)
+    g = _GfsParams(*[float(x) for x in params], None if vl is None else vl.ctypes.data)
+    n = max(so.s.nobs, 1)
+    idx = np.zeros(n, dtype=np.int32)
+    rloc = np.zeros(n)
+    rdiag = np.zeros(n)
+    nl = lib().oracle_gfs_obs_local(C.byref(so.s), C.byref(g), float(rlon), float(rlat), float(rlev), _pi(idx),
+                                    _pd(rloc), _pd(rdiag))
+    return idx[:nl].copy(), rloc[:nl].copy(), rdiag[:nl].copy()
 
 
 def scale_sort_obs(nlon, nlat, obs_ri, obs_rj, ihalo=0, jhalo=0):

@@ -127,3 +127,61 @@ def test_speedy_search_bit_exact(cuda, sigma_obs):
         np.testing.assert_array_equal(rdiag[s], rd)
         total += ri.size
     assert total > 1000
+
+
+# ------------------------------------------------------------------------- GFS
+@pytest.mark.parametrize("var_local", [None, [1.0, 0.5, 0.0, 1.0, 0.8, 1.0]])
+def test_gfs_search_matches_oracle(cuda, var_local):
+    """GFS obs_local (gfs/letkf/letkf_tools.f90:686-925) on the SPEEDY bucket
+    layout: lists and order bit-exact, rloc/rdiag to 1e-13, including tv, rain
+    (own cut-offs), TC track obs (no vertical distance), ps and points near
+    the poles and the date line; with and without variable localisation."""
+    import math
+
+    import torch
+
+    from letkf_gb300.core import search_gfs
+    from letkf_gb300.drivers import speedy_sort_obs
+
+    c = S.speedy_case(9, nstations=400)
+    rng = np.random.default_rng(9)
+    elm = c["elm"].copy()
+    n = elm.size
+    pick = rng.choice(n, n // 5, replace=False)
+    elm[pick[: n // 20]] = 3074                 # Tv
+    elm[pick[n // 20: n // 10]] = 19999         # rain
+    elm[pick[n // 10: n // 10 + 30]] = 99991    # TC track
+    lev = c["olev"].copy()
+    perm, grd = speedy_sort_obs(c["lon"], c["lat"], c["olon"], c["olat"])
+    srt = {"elm": elm[perm], "olon": c["olon"][perm], "olat": c["olat"][perm], "olev": lev[perm],
+           "odat": c["odat"][perm], "oerr": c["oerr"][perm]}
+    so = O.SpeedyObs(c["lon"], c["lat"], grd, srt["elm"], srt["olon"], srt["olat"], srt["olev"], srt["odat"],
+                     srt["oerr"], c["dist_zero"], c["dist_zerov"], c["dlat_zero"], c["sigma_obs"], c["sigma_obsv"],
+                     np.ones(7))
+    f = math.sqrt(10.0 / 3.0) * 2.0
+    prm = {"dist_zero": 500e3 * f, "dist_zerov": 0.4 * f, "dist_zero_rain": 350e3 * f, "dist_zerov_rain": 0.4 * f,
+           "sigma_obs": 500e3, "sigma_obsv": 0.4, "sigma_obs_rain": 350e3, "base_obsv_rain": 85000.0}
+    plon = np.concatenate([rng.uniform(0, 360, 300), [0.0, 359.9, 180.0, 3.75]])
+    plat = np.concatenate([rng.uniform(-88, 88, 300), [87.0, -87.0, 0.0, 89.5]])
+    prlev = np.exp(rng.uniform(np.log(2e4), np.log(1.0e5), plon.size))
+    dv = lambda a, dt=torch.float64: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=cuda)
+    grid = {"lon": dv(c["lon"]), "lat": dv(c["lat"]), "nobsgrd": dv(grd, torch.int32)}
+    obs = {"elm": dv(srt["elm"]), "lon": dv(srt["olon"]), "lat": dv(srt["olat"]), "lev": dv(srt["olev"]),
+           "dat": dv(srt["odat"]), "err": dv(srt["oerr"])}
+    offs, idx, rloc, rdiag = search_gfs(grid, obs, {"lon": dv(plon), "lat": dv(plat), "rlev": dv(prlev)}, prm,
+                                        var_local)
+    offs, idx, rloc, rdiag = (x.cpu().numpy() for x in (offs, idx, rloc, rdiag))
+    params = [prm[k] for k in ("dist_zero", "dist_zerov", "dist_zero_rain", "dist_zerov_rain", "sigma_obs",
+                               "sigma_obsv", "sigma_obs_rain", "base_obsv_rain")]
+    total = 0
+    kinds = set()
+    for p in range(plon.size):
+        ri, rl, rd = O.gfs_obs_local(so, params, plon[p], plat[p], prlev[p], var_local)
+        s = slice(offs[p], offs[p + 1])
+        np.testing.assert_array_equal(idx[s], ri, err_msg=f"point {p}")
+        np.testing.assert_allclose(rloc[s], rl, rtol=1e-13, atol=0)
+        np.testing.assert_array_equal(rdiag[s], rd)
+        total += ri.size
+        kinds.update(int(round(e)) for e in srt["elm"][ri])
+    assert total > 1000
+    assert {3074, 19999, 14593}.issubset(kinds)
