@@ -308,6 +308,23 @@ int letkf_search_l96_4d(int nx, int nslot, int ny, const int* obs_cell, int npts
                         double xlocal, double tlocal, double obserr, const int64_t* offs, int* nobsl, int* idx,
                         double* rloc, double* rdiag, void* stream);
 
+/* Lorenz-96 selection with the driver's localisation mode switch msw_local
+ * (lorenz96/letkf/letkf.f90:18-27,217-254), replacing its selection loop for
+ * every mode: 0 = fixed (as letkf_search_l96_4d); 1 = adaptive, rloc =
+ * wa^sa * wb^sb from com_correl (common/common.f90:111-128) between the
+ * observation's perturbations hdxf[row][ne] and the point's first-guess
+ * perturbations (xf[ix-1][ne] minus the sequential member mean): wb = |cor over
+ * all members|, wa = 1 - |cor(members 1..ceil(ne/2)) - cor(the rest)| / 2;
+ * 2 = the adaptive weight times both fixed factors.  Every candidate within
+ * xmaxloc is weighted and dropped below 1e-4.  hdxf holds the slot-stacked
+ * rows n*ny + i; xf is the analysis slot's first guess [nx][ne] (row-major).
+ * Means, variances and covariances are sequential FP64 sums, each operation
+ * rounded on its own.  Other msw_local values: LETKF_ERR_ARG. */
+int letkf_search_l96_adaptive(int nx, int nslot, int ny, const int* obs_cell, int npts, const int* pix, int slot,
+                              double xlocal, double tlocal, double obserr, int msw_local, double sa, double sb,
+                              int ne, const double* hdxf, const double* xf, const int64_t* offs, int* nobsl,
+                              int* idx, double* rloc, double* rdiag, void* stream);
+
 /* Grid index of each observation of the Lorenz-96 driver: the first maximum
  * of row i of h (ny x nx, column-major, on the device), 1-based
  * (lorenz96/letkf/letkf.f90:226-228). */

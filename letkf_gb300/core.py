@@ -461,6 +461,41 @@ def search_l96_4d(nx, obs_cell, pix, slot, xlocal=3.0, obserr=1.0, tlocal=2.0, s
     return offs, idx[:total], rloc[:total], rdiag[:total]
 
 
+def search_l96_adaptive(nx, obs_cell, pix, slot, hdxf, xf, msw_local=1, sa=1.0, sb=1.0, xlocal=3.0, obserr=1.0,
+                        tlocal=2.0, stream=None):
+    """Lorenz-96 selection with the localisation mode switch msw_local
+    (lorenz96/letkf/letkf.f90:18-27,217-254): 0 fixed, 1 adaptive (ensemble
+    correlation weights wa**sa * wb**sb), 2 both.  obs_cell int32 [nslot, ny]
+    (or [ny] for one slot), pix int32 [npts] (1-based), slot 0-based analysis
+    slot; hdxf float64 [nslot*ny, ne] slot-stacked obs-space perturbations, xf
+    float64 [nx, ne] the analysis slot's first guess.  Returns (offs, idx, rloc,
+    rdiag) with idx the row n*ny + i."""
+    import torch
+
+    dev = obs_cell.device
+    cell = obs_cell.reshape(-1, obs_cell.shape[-1]).contiguous()
+    nslot, ny = cell.shape
+    npts = pix.numel()
+    ne = xf.shape[1]
+    if hdxf.shape != (nslot * ny, ne) or xf.shape[0] != nx:
+        raise ValueError("search_l96_adaptive: hdxf must be [nslot*ny, ne] and xf [nx, ne]")
+    hd = hdxf.to(torch.float64).contiguous()
+    xr = xf.to(torch.float64).contiguous()
+    nobsl = torch.empty(npts, dtype=torch.int32, device=dev)
+    args = (nx, nslot, ny, _dptr(cell), npts, _dptr(pix), int(slot), float(xlocal), float(tlocal), float(obserr),
+            int(msw_local), float(sa), float(sb), ne, _dptr(hd), _dptr(xr))
+    check(lib().letkf_search_l96_adaptive(*args, None, _dptr(nobsl), None, None, None, _stream(stream)),
+          "search_l96_adaptive")
+    offs = exclusive_scan(nobsl, stream)
+    total = int(offs[-1].item())
+    idx = torch.empty(max(total, 1), dtype=torch.int32, device=dev)
+    rloc = torch.empty(max(total, 1), dtype=torch.float64, device=dev)
+    rdiag = torch.empty(max(total, 1), dtype=torch.float64, device=dev)
+    check(lib().letkf_search_l96_adaptive(*args, _dptr(offs), None, _dptr(idx), _dptr(rloc), _dptr(rdiag),
+                                          _stream(stream)), "search_l96_adaptive")
+    return offs, idx[:total], rloc[:total], rdiag[:total]
+
+
 __all__ = ["letkf_core", "core_batch_f64", "core_batch_mixed", "update_f64", "exclusive_scan", "gather_rows",
-           "search_scale", "search_speedy", "search_l96", "l96_obs_cell", "obs_departure", "update_relax_f64", "relax_beta", "core_batch_largek", "update_mixed", "obs_analysis", "efso", "RELAX_NONE", "RELAX_RTPP",
+           "search_scale", "search_speedy", "search_l96", "search_l96_4d", "search_l96_adaptive", "l96_obs_cell", "obs_departure", "update_relax_f64", "relax_beta", "core_batch_largek", "update_mixed", "obs_analysis", "efso", "RELAX_NONE", "RELAX_RTPP",
            "RELAX_RTPS", "LETKF_OK"]

@@ -6,6 +6,11 @@
 // (xmaxloc = xlocal * 2 * sqrt(10/3), :75) and drops it again when
 // rloc = exp(-0.5 (dist/xlocal)^2) * exp(-0.5 (tdif/tlocal)^2) < 1e-4.
 //
+// The adaptive modes (msw_local 1, 2; :237-249) weight each candidate by the
+// ensemble correlations between the observation's perturbations and the
+// point's: wa^sa * wb^sb with wb = |cor(all members)| and wa = 1 - |cor(first
+// ceil(k/2)) - cor(rest)| / 2, times the fixed weights in mode 2.
+//
 // Here the observations are bucketed by grid cell once per call, each point
 // visits only the cells within the cut-off, and its list is then sorted by
 // observation index, which is the reference's emission order.  Cost per point
@@ -124,10 +129,70 @@ __global__ void l96_search_kernel(L96Ctx c, int npts, const int* __restrict__ pi
     for (int t = 0; t < n; t++) rdiag[base + t] = rdiag_value;
 }
 
+// com_mean, com_stdev, com_covar, com_correl (common/common.f90:46-128) over
+// n values read through v1(i), v2(i): sequential sums, every operation rounded
+// on its own (no contraction), so a point's weights equal a CPU evaluation.
+template <typename A, typename B>
+__device__ double l96_correl(int n, A v1, B v2) {
+  double m1 = 0.0, m2 = 0.0;
+  for (int i = 0; i < n; i++) {
+    m1 = __dadd_rn(m1, v1(i));
+    m2 = __dadd_rn(m2, v2(i));
+  }
+  m1 = __ddiv_rn(m1, (double)n);
+  m2 = __ddiv_rn(m2, (double)n);
+  double s1 = 0.0, s2 = 0.0, cv = 0.0;
+  for (int i = 0; i < n; i++) {
+    const double d1 = __dsub_rn(v1(i), m1), d2 = __dsub_rn(v2(i), m2);
+    s1 = __dadd_rn(s1, __dmul_rn(d1, d1));
+    s2 = __dadd_rn(s2, __dmul_rn(d2, d2));
+    cv = __dadd_rn(cv, __dmul_rn(d1, d2));
+  }
+  const double nm1 = (double)(n - 1);
+  const double sd1 = __dsqrt_rn(__ddiv_rn(s1, nm1)), sd2 = __dsqrt_rn(__ddiv_rn(s2, nm1));
+  return __ddiv_rn(__ddiv_rn(__ddiv_rn(cv, nm1), sd1), sd2);
+}
+
+// x^e; e == 1 returns x itself, as the exact power does
+__device__ __forceinline__ double l96_pow(double x, double e) { return e == 1.0 ? x : pow(x, e); }
+
+// Adaptive localisation inputs: msw_local (0 fixed, 1 adaptive, 2 both), the
+// members split ne2 = ceil(ne/2), the exponents, the slot-stacked obs-space
+// perturbations [nslot*ny][ne] and the analysis slot's first guess [nx][ne].
+struct L96Adapt {
+  int mode, ne, ne2;
+  double sa, sb;
+  const double* hdxf;
+  const double* xf;
+};
+
+// rloc of observation row `ob` for the point whose first-guess row is xr with
+// member mean xm (lorenz96/letkf/letkf.f90:237-249)
+__device__ double l96_adapt_rloc(const L96Adapt& a, const double* __restrict__ xr, double xm, int ob, int dist,
+                                 double xlocal, double tdif, double tlocal) {
+  const double* hr = a.hdxf + (size_t)ob * a.ne;
+  const int n2 = a.ne - a.ne2;
+  const double c1 = l96_correl(a.ne2, [&](int i) { return hr[i]; }, [&](int i) { return __dsub_rn(xr[i], xm); });
+  const double c2 = l96_correl(n2, [&](int i) { return hr[a.ne2 + i]; },
+                               [&](int i) { return __dsub_rn(xr[a.ne2 + i], xm); });
+  const double c3 = l96_correl(a.ne, [&](int i) { return hr[i]; }, [&](int i) { return __dsub_rn(xr[i], xm); });
+  const double wb = fabs(c3);
+  const double wa = __dsub_rn(1.0, __dmul_rn(0.5, fabs(__dsub_rn(c1, c2))));
+  double r = __dmul_rn(l96_pow(wa, a.sa), l96_pow(wb, a.sb));
+  if (a.mode == 2) {
+    const double q = __ddiv_rn((double)dist, xlocal), tq = __ddiv_rn(tdif, tlocal);
+    r = __dmul_rn(r, exp(-0.5 * __dmul_rn(q, q)));
+    r = __dmul_rn(r, exp(-0.5 * __dmul_rn(tq, tq)));
+  }
+  return r;
+}
+
 // 4D-LETKF selection (lorenz96/letkf/letkf.f90:217-254): for analysis slot
 // `slot` every observation slot n in order, tdif = |slot - n| (0 when tlocal <
 // 0), the observation's row in the slot-stacked arrays being n*ny + i.  Buckets
-// of slot n: boff + n*(nx+1), bobs + n*ny.
+// of slot n: boff + n*(nx+1), bobs + n*ny.  ADAPT selects the correlation
+// weights; every candidate within xmaxloc is then weighted one by one and
+// dropped below 1e-4, as the reference does.
 struct L96Ctx4d {
   int nx, ny, nslot, slot;
   const int64_t* boff;
@@ -135,13 +200,21 @@ struct L96Ctx4d {
   double xlocal, xmaxloc, tlocal;
 };
 
-__global__ void l96_search4d_kernel(L96Ctx4d c, int npts, const int* __restrict__ pix,
+template <bool ADAPT>
+__global__ void l96_search4d_kernel(L96Ctx4d c, L96Adapt a, int npts, const int* __restrict__ pix,
                                     const int64_t* __restrict__ offs, int* __restrict__ nobsl, int* __restrict__ idx,
                                     double* __restrict__ rloc, double* __restrict__ rdiag, double rdiag_value) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= npts) return;
   const int ix = pix[p];
   const int64_t base = idx ? offs[p] : 0;
+  const double* xr = nullptr;
+  double xm = 0.0;
+  if (ADAPT) {
+    xr = a.xf + (size_t)(ix - 1) * a.ne;
+    for (int m = 0; m < a.ne; m++) xm = __dadd_rn(xm, xr[m]);
+    xm = __ddiv_rn(xm, (double)a.ne);
+  }
   int n = 0;
   for (int sl = 0; sl < c.nslot; sl++) {
     L96Ctx s1;
@@ -156,14 +229,28 @@ __global__ void l96_search4d_kernel(L96Ctx4d c, int npts, const int* __restrict_
     s1.tfac = exp(-0.5 * (tq * tq));
     const int n0 = n;  // this slot's entries start here, sorted by observation index
     l96_visit(s1, ix, [&](int j, int dist) {
-      const double r = l96_rloc(s1, dist);
-      if (r < 0.0) return;
-      if (!idx) {
-        n += (int)(s1.boff[j] - s1.boff[j - 1]);
-        return;
+      double r0 = 0.0;
+      if (ADAPT) {
+        if (!((double)dist < c.xmaxloc)) return;
+      } else {
+        r0 = l96_rloc(s1, dist);
+        if (r0 < 0.0) return;
+        if (!idx) {
+          n += (int)(s1.boff[j] - s1.boff[j - 1]);
+          return;
+        }
       }
       for (int64_t q = s1.boff[j - 1]; q < s1.boff[j]; q++) {
         const int ob = sl * c.ny + s1.bobs[q];
+        double r = r0;
+        if (ADAPT) {
+          r = l96_adapt_rloc(a, xr, xm, ob, dist, c.xlocal, tdif, c.tlocal);
+          if (r < 0.0001) continue;
+          if (!idx) {
+            n++;
+            continue;
+          }
+        }
         int t = n;
         while (t > n0 && idx[base + t - 1] > ob) {
           idx[base + t] = idx[base + t - 1];
@@ -256,9 +343,14 @@ int letkf_search_l96(int nx, int ny, const int* obs_cell, int npts, const int* p
   return st;
 }
 
-int letkf_search_l96_4d(int nx, int nslot, int ny, const int* obs_cell, int npts, const int* pix, int slot,
-                        double xlocal, double tlocal, double obserr, const int64_t* offs, int* nobsl, int* idx,
-                        double* rloc, double* rdiag, void* stream) {
+}  // extern "C"
+
+namespace {
+
+// bucket every slot's observations by cell, then one selection launch
+int search_l96_slots(int nx, int nslot, int ny, const int* obs_cell, int npts, const int* pix, int slot,
+                     double xlocal, double tlocal, double obserr, const L96Adapt& a, const int64_t* offs,
+                     int* nobsl, int* idx, double* rloc, double* rdiag, void* stream) {
   if (nx < 1 || nslot < 1 || ny < 0 || npts < 0 || slot < 0 || slot >= nslot || !(xlocal > 0.0) ||
       (ny > 0 && !obs_cell) || (npts > 0 && !pix))
     return LETKF_ERR_ARG;
@@ -307,13 +399,48 @@ int letkf_search_l96_4d(int nx, int nslot, int ny, const int* obs_cell, int npts
     c.xlocal = xlocal;
     c.xmaxloc = xlocal * 2.0 * sqrt(10.0 / 3.0);
     c.tlocal = tlocal;
-    l96_search4d_kernel<<<(npts + 127) / 128, 128, 0, s>>>(c, npts, pix, offs, nobsl, idx, rloc, rdiag,
-                                                           obserr * obserr);
+    const int grid = (npts + 127) / 128;
+    if (a.mode == 0)
+      l96_search4d_kernel<false><<<grid, 128, 0, s>>>(c, a, npts, pix, offs, nobsl, idx, rloc, rdiag, obserr * obserr);
+    else
+      l96_search4d_kernel<true><<<grid, 128, 0, s>>>(c, a, npts, pix, offs, nobsl, idx, rloc, rdiag, obserr * obserr);
     note_launch();
     st = cuda_status(cudaGetLastError());
   }
   cudaFreeAsync(buf, s);
   return st;
+}
+
+}  // namespace
+
+extern "C" {
+
+int letkf_search_l96_4d(int nx, int nslot, int ny, const int* obs_cell, int npts, const int* pix, int slot,
+                        double xlocal, double tlocal, double obserr, const int64_t* offs, int* nobsl, int* idx,
+                        double* rloc, double* rdiag, void* stream) {
+  L96Adapt a = {};
+  return search_l96_slots(nx, nslot, ny, obs_cell, npts, pix, slot, xlocal, tlocal, obserr, a, offs, nobsl, idx, rloc,
+                          rdiag, stream);
+}
+
+int letkf_search_l96_adaptive(int nx, int nslot, int ny, const int* obs_cell, int npts, const int* pix, int slot,
+                              double xlocal, double tlocal, double obserr, int msw_local, double sa, double sb,
+                              int ne, const double* hdxf, const double* xf, const int64_t* offs, int* nobsl,
+                              int* idx, double* rloc, double* rdiag, void* stream) {
+  if (msw_local < 0 || msw_local > 2) return LETKF_ERR_ARG;
+  L96Adapt a = {};
+  a.mode = msw_local;
+  if (msw_local != 0) {
+    if (ne < 1 || (nslot > 0 && ny > 0 && !hdxf) || (npts > 0 && !xf)) return LETKF_ERR_ARG;
+    a.ne = ne;
+    a.ne2 = (ne + 1) / 2;  // CEILING(REAL(nbv)/2.0)
+    a.sa = sa;
+    a.sb = sb;
+    a.hdxf = hdxf;
+    a.xf = xf;
+  }
+  return search_l96_slots(nx, nslot, ny, obs_cell, npts, pix, slot, xlocal, tlocal, obserr, a, offs, nobsl, idx, rloc,
+                          rdiag, stream);
 }
 
 }  // extern "C"

@@ -258,9 +258,10 @@ def speedy_cycle(gues_paths, obs_path, anal_paths, lon, lat, sig, infl_path=None
 
 # -------------------------------------------------------------------- Lorenz-96
 def l96_letkf(xf, hxf, y, obs_cell, obserr=1.0, xlocal=3.0, parm_infl=None, msw_infl=1.05, precision="f64",
-              stream=None):
+              stream=None, msw_local=0, sa=1.0, sb=1.0):
     """One LETKF analysis of the Lorenz-96 driver (lorenz96/letkf/letkf.f90:
-    180-265, one time slot, fixed localisation).
+    180-265, one time slot).  msw_local 0 is the fixed localisation, 1 the
+    adaptive one (correlation weights wa**sa * wb**sb, :237-243), 2 both.
 
     xf: float64 [nx, ne] background members; hxf: float64 [ny, ne] = H xf;
     y: float64 [ny]; obs_cell: int32 [ny] 1-based grid index of each
@@ -276,7 +277,11 @@ def l96_letkf(xf, hxf, y, obs_cell, obserr=1.0, xlocal=3.0, parm_infl=None, msw_
         parm_infl = torch.full((nx,), float(msw_infl), dtype=torch.float64, device=dev)
     hdxf, dep, _ = K.obs_departure(hxf, y, stream=stream)
     pix = torch.arange(1, nx + 1, dtype=torch.int32, device=dev)
-    offs, idx, rloc, rdiag = K.search_l96(nx, obs_cell, pix, xlocal, obserr, stream=stream)
+    if msw_local == 0:
+        offs, idx, rloc, rdiag = K.search_l96(nx, obs_cell, pix, xlocal, obserr, stream=stream)
+    else:
+        offs, idx, rloc, rdiag = K.search_l96_adaptive(nx, obs_cell, pix, 0, hdxf, xf, msw_local, sa, sb, xlocal,
+                                                       obserr, stream=stream)
     rows, dl = K.gather_rows(idx, hdxf, dep, stream)
     if precision == "f64":
         out = K.core_batch_f64(ne, offs, rows, rdiag, rloc, dl, parm_infl, stream=stream)
@@ -296,9 +301,9 @@ def l96_letkf(xf, hxf, y, obs_cell, obserr=1.0, xlocal=3.0, parm_infl=None, msw_
 
 
 def l96_letkf_4d(xf, hxf, y, obs_cell, obserr=1.0, xlocal=3.0, tlocal=2.0, parm_infl=None, msw_infl=1.05,
-                 precision="f64", stream=None):
+                 precision="f64", stream=None, msw_local=0, sa=1.0, sb=1.0):
     """4D-LETKF of the Lorenz-96 driver (lorenz96/letkf/letkf.f90:183-288,
-    nwindow > 1, fixed localisation): xf float64 [nslot, nx, ne] first guesses
+    nwindow > 1; msw_local as in l96_letkf): xf float64 [nslot, nx, ne] first guesses
     of the slots; hxf [nslot, ny, ne] = H_n xf_n; y [nslot, ny]; obs_cell int32
     [nslot, ny] (l96_obs_cell of each slot's H).  Departures and perturbations
     per slot (:197-213), then for every analysis slot nn and point the
@@ -322,7 +327,11 @@ def l96_letkf_4d(xf, hxf, y, obs_cell, obserr=1.0, xlocal=3.0, tlocal=2.0, parm_
     pix = torch.arange(1, nx + 1, dtype=torch.int32, device=dev)
     xa = torch.empty_like(xf)
     for nn in range(nslot):
-        offs, idx, rloc, rdiag = K.search_l96_4d(nx, obs_cell, pix, nn, xlocal, obserr, tlocal, stream)
+        if msw_local == 0:
+            offs, idx, rloc, rdiag = K.search_l96_4d(nx, obs_cell, pix, nn, xlocal, obserr, tlocal, stream)
+        else:
+            offs, idx, rloc, rdiag = K.search_l96_adaptive(nx, obs_cell, pix, nn, hdxf, xf[nn], msw_local, sa, sb,
+                                                           xlocal, obserr, tlocal, stream)
         rows, dl = K.gather_rows(idx, hdxf, dep, stream)
         pinf = parm_infl[nn].contiguous()
         if precision == "f64":

@@ -58,6 +58,8 @@ _SIGS = {
     "letkf_gather_rows": (_i, [_i, _i64, _vp, _vp, _vp, _i, _vp, _vp, _vp]),
     "letkf_search_l96": (_i, [_i, _i, _vp, _i, _vp, _d, _d, _d, _d, _vp, _vp, _vp, _vp, _vp, _vp]),
     "letkf_search_l96_4d": (_i, [_i, _i, _i, _vp, _i, _vp, _i, _d, _d, _d, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "letkf_search_l96_adaptive": (_i, [_i, _i, _i, _vp, _i, _vp, _i, _d, _d, _d, _i, _d, _d, _i, _vp, _vp, _vp, _vp,
+                                       _vp, _vp, _vp, _vp]),
     "letkf_l96_obs_cell": (_i, [_i, _i, _vp, _vp, _vp]),
     "letkf_obs_departure": (_i, [_i, _i, _vp, _vp, _vp, _d, _vp, _vp, _vp, _vp, _vp]),
     "letkf_core_batch_largek": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _d, _vp, _vp]),

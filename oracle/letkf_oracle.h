@@ -141,6 +141,10 @@ int oracle_l96_select(int nx, int ny, const double* h /* ny x nx col-major */, i
                       double tlocal, int* idx, double* rloc);
 int oracle_l96_select_4d(int nx, int ny, int nslot, const double* h, int slot, int ix, double xlocal, double tlocal,
                          int* idx, double* rloc);
+double oracle_com_correl(int n, const double* v1, const double* v2);
+int oracle_l96_select_adaptive(int nx, int ny, int nslot, const double* h, const double* hdxf, const double* dxf,
+                               int ne, int slot, int ix, double xlocal, double tlocal, int msw_local, double sa,
+                               double sb, int* idx, double* rloc);
 
 /* ---- sweeps (das_letkf loops) ---- */
 /* Ensemble mean and perturbation, sequential member sum

@@ -579,6 +579,92 @@ int oracle_l96_select_4d(int nx, int ny, int nslot, const double* h, int slot, i
   return ny_loc;
 }
 
+/* com_mean, com_stdev, com_covar, com_correl (common/common.f90:46-128):
+ * sequential sums over n values. */
+static double com_mean(int n, const double* v) {
+  double s = 0.0;
+  int i;
+  for (i = 0; i < n; i++) s = s + v[i];
+  return s / (double)n;
+}
+
+static double com_stdev(int n, const double* v) {
+  const double m = com_mean(n, v);
+  double s = 0.0;
+  int i;
+  for (i = 0; i < n; i++) {
+    const double d = v[i] - m;
+    s = s + d * d;
+  }
+  return sqrt(s / (double)(n - 1));
+}
+
+static double com_covar(int n, const double* v1, const double* v2) {
+  const double m1 = com_mean(n, v1), m2 = com_mean(n, v2);
+  double s = 0.0;
+  int i;
+  for (i = 0; i < n; i++) s = s + (v1[i] - m1) * (v2[i] - m2);
+  return s / (double)(n - 1);
+}
+
+double oracle_com_correl(int n, const double* v1, const double* v2) {
+  const double sd1 = com_stdev(n, v1), sd2 = com_stdev(n, v2);
+  const double cov = com_covar(n, v1, v2);
+  return cov / sd1 / sd2;
+}
+
+/* lorenz96/letkf/letkf.f90:217-254 with the localisation switch msw_local
+ * (0 fixed, 1 adaptive, 2 both; :18-27).  hdxf holds the slot-stacked
+ * obs-space perturbations [nslot*ny][ne] (row n*ny + i); dxf the first-guess
+ * perturbations of point ix at the analysis slot [ne]; slot and ix 1-based.
+ * nbv2 = CEILING(REAL(nbv)/2.0) (:76). */
+int oracle_l96_select_adaptive(int nx, int ny, int nslot, const double* h, const double* hdxf, const double* dxf,
+                               int ne, int slot, int ix, double xlocal, double tlocal, int msw_local, double sa,
+                               double sb, int* idx, double* rloc) {
+  const double xmaxloc = xlocal * 2.0 * sqrt(10.0 / 3.0);
+  const int nbv2 = (int)ceil((double)(float)ne / 2.0);
+  int n, i, j, ny_loc = 0;
+  for (n = 1; n <= nslot; n++) {
+    const double* hn = h + (size_t)(n - 1) * nx * ny;
+    double tdif = (double)abs(slot - n);
+    if (tlocal < 0.0) tdif = 0.0;
+    for (i = 1; i <= ny; i++) {
+      double mx = hn[(size_t)0 * ny + (i - 1)];
+      for (j = 2; j <= nx; j++)
+        if (hn[(size_t)(j - 1) * ny + (i - 1)] > mx) mx = hn[(size_t)(j - 1) * ny + (i - 1)];
+      for (j = 1; j <= nx; j++)
+        if (mx == hn[(size_t)(j - 1) * ny + (i - 1)]) break;
+      {
+        int a = abs(j - ix), b = nx - abs(j - ix);
+        double dist = (double)(a < b ? a : b);
+        if (dist < xmaxloc) {
+          const int row = (n - 1) * ny + (i - 1);
+          const double* hr = hdxf + (size_t)row * ne;
+          double r;
+          if (msw_local == 0) {
+            r = exp(-0.5 * ((dist / xlocal) * (dist / xlocal))) * exp(-0.5 * ((tdif / tlocal) * (tdif / tlocal)));
+          } else {
+            const double c1 = oracle_com_correl(nbv2, hr, dxf);
+            const double c2 = oracle_com_correl(ne - nbv2, hr + nbv2, dxf + nbv2);
+            const double c3 = oracle_com_correl(ne, hr, dxf);
+            const double wb = fabs(c3);
+            const double wa = 1.0 - (0.5 * fabs(c1 - c2));
+            r = pow(wa, sa) * pow(wb, sb);
+            if (msw_local == 2)
+              r = r * exp(-0.5 * ((dist / xlocal) * (dist / xlocal))) *
+                  exp(-0.5 * ((tdif / tlocal) * (tdif / tlocal)));
+          }
+          ny_loc++;
+          idx[ny_loc - 1] = row;
+          rloc[ny_loc - 1] = r;
+          if (r < 0.0001) ny_loc--;
+        }
+      }
+    }
+  }
+  return ny_loc;
+}
+
 /* speedy/common/common_speedy.f90:335-370 and letkf_tools.f90:96-112 */
 void oracle_ensmean(int npts, int ne, const double* x, double* mean, double* pert) {
   int p, m;

@@ -49,6 +49,11 @@ def lib():
         _lib.oracle_l96_select_4d.restype = C.c_int
         _lib.oracle_l96_select_4d.argtypes = [C.c_int, C.c_int, C.c_int, pd, C.c_int, C.c_int, d, d, pi, pd]
         _lib.oracle_l96_select.restype = C.c_int
+        _lib.oracle_com_correl.restype = d
+        _lib.oracle_com_correl.argtypes = [C.c_int, pd, pd]
+        _lib.oracle_l96_select_adaptive.restype = C.c_int
+        _lib.oracle_l96_select_adaptive.argtypes = [C.c_int, C.c_int, C.c_int, pd, pd, pd, C.c_int, C.c_int, C.c_int,
+                                                    d, d, C.c_int, d, d, pi, pd]
         _lib.oracle_l96_select.argtypes = [C.c_int, C.c_int, pd, C.c_int, d, d, pi, pd]
         _lib.oracle_ensmean.argtypes = [C.c_int, C.c_int, pd, pd, pd]
         _lib.oracle_scale_sweep.restype = C.c_int
@@ -319,6 +324,32 @@ def l96_select_4d(h4d, slot, ix, xlocal=3.0, tlocal=2.0):
     rloc = np.zeros(max(nslot * ny, 1))
     n = lib().oracle_l96_select_4d(nx, ny, nslot, _pd(hf), int(slot), int(ix), float(xlocal), float(tlocal),
                                    _pi(idx), _pd(rloc))
+    return idx[:n].copy(), rloc[:n].copy()
+
+
+def com_correl(v1, v2):
+    """common/common.f90:111-128 (sequential sums)."""
+    v1, v2 = _f64(v1), _f64(v2)
+    return float(lib().oracle_com_correl(v1.size, _pd(v1), _pd(v2)))
+
+
+def l96_select_adaptive(h4d, hdxf, dxf, slot, ix, msw_local, sa=1.0, sb=1.0, xlocal=3.0, tlocal=2.0):
+    """Lorenz-96 selection with msw_local (0 fixed, 1 adaptive, 2 both).
+    h4d (nslot, ny, nx); hdxf (nslot*ny, ne) slot-stacked obs-space
+    perturbations; dxf (ne,) first-guess perturbations of point ix at the
+    analysis slot; slot and ix 1-based."""
+    h4d = np.asarray(h4d, dtype=np.float64)
+    if h4d.ndim == 2:
+        h4d = h4d[None]
+    nslot, ny, nx = h4d.shape
+    hf = np.ascontiguousarray(np.stack([np.asfortranarray(h4d[n]).ravel(order="F") for n in range(nslot)]))
+    hd = _f64(hdxf)
+    dx = _f64(dxf)
+    idx = np.zeros(max(nslot * ny, 1), dtype=np.int32)
+    rloc = np.zeros(max(nslot * ny, 1))
+    n = lib().oracle_l96_select_adaptive(nx, ny, nslot, _pd(hf), _pd(hd), _pd(dx), dx.size, int(slot), int(ix),
+                                         float(xlocal), float(tlocal), int(msw_local), float(sa), float(sb),
+                                         _pi(idx), _pd(rloc))
     return idx[:n].copy(), rloc[:n].copy()
 
 

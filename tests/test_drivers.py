@@ -298,3 +298,196 @@ def test_oracle_l96_select_4d_reduces_to_one_slot_and_weights_time():
     np.testing.assert_allclose(r3[:n], r1 * np.exp(-0.5 * 0.25), rtol=1e-15)       # tdif = 1
     _, rneg = O.l96_select_4d(np.stack([h, h, h]), 2, 7, 3.0, -1.0)
     np.testing.assert_allclose(rneg[:n], r1, rtol=1e-15)                          # no time localisation
+
+
+# -------------------------------------------------- adaptive localisation (L96)
+def _np_correl(a, b):
+    return np.corrcoef(a, b)[0, 1]
+
+
+def _l96_adapt_case(seed, nslot=1, nx=40, ny=40, ne=20):
+    """Random H with one cell per observation, correlated members: returns
+    (h4d, hdxf [nslot*ny, ne], xf [nslot, nx, ne])."""
+    rng = np.random.default_rng(seed)
+    h4d = np.zeros((nslot, ny, nx))
+    for n in range(nslot):
+        cells = rng.integers(1, nx + 1, ny)
+        h4d[n, np.arange(ny), cells - 1] = 1.0
+    xf = 8.0 + 2.0 * rng.standard_normal((nslot, nx, ne))
+    hd = []
+    for n in range(nslot):
+        hx = h4d[n] @ xf[n] + 0.3 * rng.standard_normal((ny, ne))
+        m = hx[:, 0].copy()
+        for k in range(1, ne):
+            m = m + hx[:, k]
+        hd.append(hx - (m / ne)[:, None])
+    return h4d, np.concatenate(hd), xf
+
+
+def _dxf(xrow):
+    m = xrow[0]
+    for v in xrow[1:]:
+        m = m + v
+    return xrow - m / xrow.size
+
+
+def test_oracle_l96_adaptive_mode0_is_the_fixed_selection():
+    h4d, hdxf, xf = _l96_adapt_case(3, nslot=3)
+    for ix in (1, 17, 40):
+        for slot in (1, 2, 3):
+            i0, r0 = O.l96_select_4d(h4d, slot, ix, 3.0, 2.0)
+            i1, r1 = O.l96_select_adaptive(h4d, hdxf, _dxf(xf[slot - 1, ix - 1]), slot, ix, 0)
+            np.testing.assert_array_equal(i0, i1)
+            np.testing.assert_array_equal(r0, r1)
+
+
+@pytest.mark.parametrize("mode,sa,sb", [(1, 1.0, 1.0), (2, 1.0, 1.0), (1, 0.5, 2.0), (2, 2.0, 0.5)])
+def test_oracle_l96_adaptive_weights_are_the_correlations(mode, sa, sb):
+    """msw_local 1/2 (lorenz96/letkf/letkf.f90:237-249) against numpy's
+    correlation coefficients: every observation within xmaxloc is a candidate,
+    weighted wa**sa * wb**sb (times the fixed weights in mode 2), kept from 1e-4."""
+    nslot, ne = 2, 21          # odd k: ceil(k/2) = 11 members in the first half
+    h4d, hdxf, xf = _l96_adapt_case(5, nslot=nslot, ne=ne)
+    nx, ny = h4d.shape[2], h4d.shape[1]
+    xmaxloc = 3.0 * 2.0 * np.sqrt(10.0 / 3.0)
+    for slot in (1, 2):
+        for ix in (1, 9, 33):
+            d = _dxf(xf[slot - 1, ix - 1])
+            idx, rloc = O.l96_select_adaptive(h4d, hdxf, d, slot, ix, mode, sa, sb)
+            exp_i, exp_r = [], []
+            for n in range(nslot):
+                for i in range(ny):
+                    j = int(np.argmax(h4d[n, i])) + 1
+                    dist = min(abs(j - ix), nx - abs(j - ix))
+                    if dist >= xmaxloc:
+                        continue
+                    row = hdxf[n * ny + i]
+                    c1 = _np_correl(row[:11], d[:11])
+                    c2 = _np_correl(row[11:], d[11:])
+                    c3 = _np_correl(row, d)
+                    r = (1.0 - 0.5 * abs(c1 - c2)) ** sa * abs(c3) ** sb
+                    if mode == 2:
+                        r *= np.exp(-0.5 * (dist / 3.0) ** 2) * np.exp(-0.5 * (abs(slot - 1 - n) / 2.0) ** 2)
+                    if r >= 1e-4:
+                        exp_i.append(n * ny + i)
+                        exp_r.append(r)
+            np.testing.assert_array_equal(idx, exp_i)
+            np.testing.assert_allclose(rloc, exp_r, rtol=1e-12)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nslot,mode,sa,sb", [(1, 1, 1.0, 1.0), (1, 2, 1.0, 1.0), (3, 1, 1.0, 1.0),
+                                               (3, 2, 0.5, 2.0), (3, 0, 1.0, 1.0), (1, 1, 2.0, 0.5)])
+def test_l96_search_adaptive_matches_oracle(cuda, nslot, mode, sa, sb):
+    """Device selection with msw_local against the oracle for every point and
+    analysis slot: lists bit-exact; weights bit-exact with sa = sb = 1 (the
+    same rounded operations), within 1e-14 otherwise (pow)."""
+    import torch
+
+    from letkf_gb300.core import l96_obs_cell, search_l96_adaptive
+
+    ne = 21
+    h4d, hdxf, xf = _l96_adapt_case(11 + nslot + mode, nslot=nslot, nx=60, ny=70, ne=ne)
+    nx = h4d.shape[2]
+    cell = torch.stack([l96_obs_cell(_t(h4d[n], torch.float64, cuda)) for n in range(nslot)])
+    pix = torch.arange(1, nx + 1, dtype=torch.int32, device=cuda)
+    hd = _t(hdxf, torch.float64, cuda)
+    for slot in range(nslot):
+        offs, idx, rloc, rdiag = search_l96_adaptive(nx, cell, pix, slot, hd, _t(xf[slot], torch.float64, cuda),
+                                                     mode, sa, sb, 3.0, 0.5, 2.0)
+        offs, idx, rloc = offs.cpu().numpy(), idx.cpu().numpy(), rloc.cpu().numpy()
+        assert np.all(rdiag.cpu().numpy() == 0.25)
+        for ix in range(1, nx + 1):
+            ri, rl = O.l96_select_adaptive(h4d, hdxf, _dxf(xf[slot, ix - 1]), slot + 1, ix, mode, sa, sb)
+            s = slice(offs[ix - 1], offs[ix])
+            np.testing.assert_array_equal(idx[s], ri, err_msg=f"slot {slot} ix {ix}")
+            if mode == 1 and sa == 1.0 and sb == 1.0:
+                np.testing.assert_array_equal(rloc[s], rl)
+            else:
+                np.testing.assert_allclose(rloc[s], rl, rtol=1e-14, atol=0)
+
+
+@pytest.mark.gpu
+def test_l96_search_adaptive_rejects_unknown_mode(cuda):
+    import torch
+
+    from letkf_gb300.core import search_l96_adaptive
+    from letkf_gb300.lib import LETKF_ERR_ARG, LetkfError
+
+    cell = torch.ones(4, dtype=torch.int32, device=cuda)
+    pix = torch.arange(1, 9, dtype=torch.int32, device=cuda)
+    with pytest.raises(LetkfError) as e:
+        search_l96_adaptive(8, cell, pix, 0, torch.zeros(4, 6, dtype=torch.float64, device=cuda),
+                            torch.zeros(8, 6, dtype=torch.float64, device=cuda), 3)
+    assert e.value.status == LETKF_ERR_ARG
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", [1, 2])
+def test_l96_letkf_adaptive_matches_oracle(cuda, mode):
+    """Lorenz-96 analysis with adaptive localisation (msw_local 1, 2) against
+    the oracle's selection + core + update at every point (FP64, 1e-10)."""
+    import torch
+
+    from letkf_gb300.core import l96_obs_cell
+    from letkf_gb300.drivers import l96_letkf
+
+    rng = np.random.default_rng(29 + mode)
+    nx, ne = 40, 20
+    xf = 8.0 + 2.0 * rng.standard_normal((nx, ne))
+    h = np.eye(nx)[::2]                               # every other variable observed
+    hxf = h @ xf
+    y = 8.0 + rng.standard_normal(h.shape[0])
+    cell = l96_obs_cell(_t(h, torch.float64, cuda))
+    xa, infl = l96_letkf(_t(xf, torch.float64, cuda), _t(hxf, torch.float64, cuda), _t(y, torch.float64, cuda),
+                         cell, obserr=1.0, xlocal=3.0, msw_local=mode)
+    xa = xa.cpu().numpy()
+    assert np.all(infl.cpu().numpy() == 1.05)
+    m = hxf[:, 0].copy()
+    for k in range(1, ne):
+        m = m + hxf[:, k]
+    m = m / ne
+    hdxf, dep = hxf - m[:, None], y - m
+    for ix in range(1, nx + 1):
+        d = _dxf(xf[ix - 1])
+        ri, rl = O.l96_select_adaptive(h, hdxf, d, 1, ix, mode)
+        r = O.letkf_core(hdxf[ri], np.ones(ri.size), rl, dep[ri], 1.05)
+        ref = (xf[ix - 1] - d) + d @ r["trans"]
+        _close(xa[ix - 1], ref, 1e-10)
+
+
+@pytest.mark.gpu
+def test_l96_letkf_4d_adaptive_matches_oracle(cuda):
+    """Two-slot 4D-LETKF with msw_local = 2 against the oracle chain."""
+    import torch
+
+    from letkf_gb300.core import l96_obs_cell
+    from letkf_gb300.drivers import l96_letkf_4d
+
+    rng = np.random.default_rng(31)
+    nslot, nx, ne = 2, 40, 20
+    xf = 8.0 + 2.0 * rng.standard_normal((nslot, nx, ne))
+    h = np.eye(nx)
+    hxf = np.stack([h @ xf[n] for n in range(nslot)])
+    y = 8.0 + rng.standard_normal((nslot, nx))
+    cell = torch.stack([l96_obs_cell(_t(h, torch.float64, cuda))] * nslot)
+    xa, _ = l96_letkf_4d(_t(xf, torch.float64, cuda), _t(hxf, torch.float64, cuda), _t(y, torch.float64, cuda),
+                         cell, obserr=1.0, xlocal=3.0, tlocal=2.0, msw_local=2)
+    xa = xa.cpu().numpy()
+    hdxf, dep = [], []
+    for n in range(nslot):
+        m = hxf[n][:, 0].copy()
+        for k in range(1, ne):
+            m = m + hxf[n][:, k]
+        m = m / ne
+        hdxf.append(hxf[n] - m[:, None])
+        dep.append(y[n] - m)
+    hdxf, dep = np.concatenate(hdxf), np.concatenate(dep)
+    h4d = np.stack([h, h])
+    for nn in range(nslot):
+        for ix in range(1, nx + 1):
+            d = _dxf(xf[nn, ix - 1])
+            ri, rl = O.l96_select_adaptive(h4d, hdxf, d, nn + 1, ix, 2, 1.0, 1.0, 3.0, 2.0)
+            r = O.letkf_core(hdxf[ri], np.ones(ri.size), rl, dep[ri], 1.05)
+            ref = (xf[nn, ix - 1] - d) + d @ r["trans"]
+            _close(xa[nn, ix - 1], ref, 1e-10)
