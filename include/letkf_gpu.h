@@ -391,6 +391,17 @@ int letkf_sweep_set_inflation(letkf_sweep_t h, const double* infl, int on_device
 int letkf_sweep_set_option(letkf_sweep_t h, int option, int value);
 /* analyse every point; asynchronous on `stream` (NULL: the handle's stream) */
 int letkf_sweep_run(letkf_sweep_t h, void* stream);
+/* One analysis from host buffers with the copies overlapped: the processing
+ * order is cut into nchunks pieces; the background rows a piece reads go in
+ * on a copy stream while earlier pieces are analysed on `stream`, and analysis
+ * rows go out on a second copy stream once every point below them is done.
+ * xb and xa are host arrays [nv][npts][ne] as in letkf_sweep_set_background /
+ * letkf_sweep_get_analysis; the result equals those two calls around
+ * letkf_sweep_run bit for bit.  Returns when xa holds the analysis.
+ * Page-locked host buffers let the copies run beside the analysis.  The
+ * plain form and nchunks = 1 run the three calls in sequence; the points
+ * must be set (LETKF_ERR_ARG otherwise). */
+int letkf_sweep_run_host(letkf_sweep_t h, const void* xb, void* xa, int nchunks, void* stream);
 /* Autotuner of the mixed form: times every kernel / eigensolver variant the
  * handle can run (tensor-core sweep with spectrum-scaled or plain
  * Newton-Schulz steps when ne <= 64; SIMT sweep with Newton-Schulz or

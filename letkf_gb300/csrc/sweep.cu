@@ -124,6 +124,8 @@ struct letkf_sweep_s {
   // points
   double *pri = nullptr, *prj = nullptr, *prlev = nullptr, *prz = nullptr, *plogr = nullptr;
   int* order = nullptr;
+  std::vector<int> horder;     // the processing order, host copy
+  std::vector<int64_t> hband;  // per order position: its band (tile row; the position itself without tiles)
   // sorted observations
   double *ori = nullptr, *orj = nullptr, *olev = nullptr, *odat = nullptr, *oerr = nullptr, *odep = nullptr;
   int *ocls = nullptr, *ovarloc = nullptr, *G = nullptr;
@@ -156,6 +158,13 @@ struct letkf_sweep_s {
   cudaGraphExec_t gexec = nullptr;
   std::vector<unsigned char> gkey;
   int64_t glaunches = 0;  // kernels in the captured graph
+  // run from host buffers: copy-in and copy-out streams, events (two per
+  // chunk and two more), and the chunk plan
+  cudaStream_t cs_in = nullptr, cs_out = nullptr;
+  std::vector<cudaEvent_t> hev;
+  int plan_n = 0;
+  std::vector<int64_t> plan;   // per chunk: order range [o0, o1), its copies [c0, c1)
+  std::vector<int64_t> pcopy;  // per copy: first row, rows, row stride, count (a strided block of point rows)
 };
 
 // Stream-ordered allocation: no call of a handle synchronises the whole
@@ -244,6 +253,12 @@ int letkf_sweep_destroy(letkf_sweep_t h) {
   }
   if (h->ran) cudaEventDestroy(h->ran);
   if (h->gexec) cudaGraphExecDestroy(h->gexec);
+  for (cudaStream_t cs : {h->cs_in, h->cs_out})
+    if (cs) {
+      cudaStreamSynchronize(cs);
+      cudaStreamDestroy(cs);
+    }
+  for (cudaEvent_t e : h->hev) cudaEventDestroy(e);
   delete h;
   return LETKF_OK;
 }
@@ -257,6 +272,8 @@ int letkf_sweep_set_points(letkf_sweep_t h, const double* ri, const double* rj, 
   // processing order: column tiles of tile x tile cells, input order inside a tile
   std::vector<int> order(np);
   std::iota(order.begin(), order.end(), 0);
+  std::vector<int64_t> band(np);
+  std::iota(band.begin(), band.end(), (int64_t)0);
   if (tile > 0) {
     std::vector<int64_t> key(np);
     const int64_t ntx = (h->d.nlon + tile - 1) / tile + 1;
@@ -265,6 +282,7 @@ int letkf_sweep_set_points(letkf_sweep_t h, const double* ri, const double* rj, 
       key[p] = (tj + 1) * (ntx + 1) + (ti + 1);
     }
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key[a] < key[b]; });
+    for (int o = 0; o < np; o++) band[o] = key[order[o]] / (ntx + 1);
   }
   std::vector<double> lg(np);
   for (int p = 0; p < np; p++) lg[p] = std::log(rlev[p]);
@@ -275,7 +293,11 @@ int letkf_sweep_set_points(letkf_sweep_t h, const double* ri, const double* rj, 
   cudaMemcpyAsync(h->prlev, rlev, sizeof(double) * np, cudaMemcpyHostToDevice, s);
   if (rz) cudaMemcpyAsync(h->prz, rz, sizeof(double) * np, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(h->order, order.data(), sizeof(int) * np, cudaMemcpyHostToDevice, s);
-  return cuda_status(cudaStreamSynchronize(s));
+  const int st = cuda_status(cudaStreamSynchronize(s));
+  h->horder.swap(order);
+  h->hband.swap(band);
+  h->plan_n = 0;
+  return st;
 }
 
 int letkf_sweep_set_obs(letkf_sweep_t h, int nobs, const double* ri, const double* rj, const double* lev,
@@ -563,6 +585,7 @@ static void build_args(letkf_sweep_t h, SweepArgs& a) {
   a.n = h->d.ne;
   a.nv = h->d.nv;
   a.npts = h->d.npts;
+  a.nwork = h->d.npts;
   a.nlon = h->d.nlon;
   a.nlat = h->d.nlat;
   a.nobs = h->nobs;
@@ -673,6 +696,142 @@ static int run_on(letkf_sweep_t h, cudaStream_t s) {
   return cuda_status(r);
 }
 
+// Chunk plan of the host-buffer run: about nchunks pieces of the processing
+// order, cut where its band (tile row) changes.  A point's background row is
+// read and its analysis row written by its own analysis only, so piece c
+// copies exactly its points' rows in before it and out after it: the sorted
+// rows form runs, and runs of equal length at a constant stride one strided
+// copy (with level-major points and tile-row pieces: one copy per variable).
+static void plan_host_run(letkf_sweep_t h, int nc) {
+  const int64_t np = h->d.npts;
+  std::vector<int64_t> cut{0};
+  for (int c = 1; c < nc; c++) {
+    int64_t o = np * c / nc;
+    while (o < np && o > 0 && h->hband[(size_t)o] == h->hband[(size_t)o - 1]) o++;
+    if (o > cut.back() && o < np) cut.push_back(o);
+  }
+  cut.push_back(np);
+  h->plan.clear();
+  h->pcopy.clear();
+  std::vector<int> rows;
+  for (size_t c = 0; c + 1 < cut.size(); c++) {
+    const int64_t o0 = cut[c], o1 = cut[c + 1];
+    rows.assign(h->horder.begin() + o0, h->horder.begin() + o1);
+    std::sort(rows.begin(), rows.end());
+    const int64_t c0 = (int64_t)h->pcopy.size() / 4;
+    // runs of consecutive rows, merged into strided blocks
+    int64_t bstart = -1, blen = 0, bstride = 0, bcount = 0;
+    auto flush = [&]() {
+      if (bcount > 0) h->pcopy.insert(h->pcopy.end(), {bstart, blen, bcount > 1 ? bstride : blen, bcount});
+      bcount = 0;
+    };
+    size_t i = 0;
+    while (i < rows.size()) {
+      size_t j = i + 1;
+      while (j < rows.size() && rows[j] == rows[j - 1] + 1) j++;
+      const int64_t rs = rows[i], rl = (int64_t)(j - i);
+      if (bcount == 1 && rl == blen) {
+        bstride = rs - bstart;
+        bcount = 2;
+      } else if (bcount > 1 && rl == blen && rs == bstart + bcount * bstride) {
+        bcount++;
+      } else {
+        flush();
+        bstart = rs;
+        blen = rl;
+        bcount = 1;
+      }
+      i = j;
+    }
+    flush();
+    h->plan.insert(h->plan.end(), {o0, o1, c0, (int64_t)h->pcopy.size() / 4});
+  }
+  h->plan_n = nc;
+}
+
+// the point rows of one strided block, for every variable, in one direction
+static int copy_rows(const int64_t* cp, int nv, int64_t np, size_t row, void* dst, const void* src,
+                     cudaMemcpyKind kind, cudaStream_t s) {
+  for (int v = 0; v < nv; v++) {
+    const size_t off = ((size_t)v * np + (size_t)cp[0]) * row;
+    cudaError_t e;
+    if (cp[3] == 1)
+      e = cudaMemcpyAsync((char*)dst + off, (const char*)src + off, (size_t)cp[1] * row, kind, s);
+    else
+      e = cudaMemcpy2DAsync((char*)dst + off, (size_t)cp[2] * row, (const char*)src + off, (size_t)cp[2] * row,
+                            (size_t)cp[1] * row, (size_t)cp[3], kind, s);
+    if (e != cudaSuccess) return cuda_status(e);
+  }
+  return LETKF_OK;
+}
+
+int letkf_sweep_run_host(letkf_sweep_t h, const void* xb, void* xa, int nchunks, void* stream) {
+  if (!h || !xb || !xa || nchunks < 1) return LETKF_ERR_ARG;
+  const int np = h->d.npts;
+  if (h->d.precision == LETKF_PREC_F64 || np == 0 || nchunks == 1) {
+    int st = letkf_sweep_set_background(h, xb, 0);
+    if (st == LETKF_OK) st = letkf_sweep_run(h, stream);
+    if (st == LETKF_OK) st = letkf_sweep_get_analysis(h, xa, 0);
+    return st;
+  }
+  if ((int)h->horder.size() != np) return LETKF_ERR_ARG;  // points not set
+  if (nchunks > np) nchunks = np;
+  if (nchunks > 1024) nchunks = 1024;
+  cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+  for (cudaStream_t* cs : {&h->cs_in, &h->cs_out})
+    if (!*cs && cudaStreamCreateWithFlags(cs, cudaStreamNonBlocking) != cudaSuccess) return LETKF_ERR_CUDA;
+  while (h->hev.size() < (size_t)(2 * nchunks + 2)) {
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return LETKF_ERR_CUDA;
+    h->hev.push_back(e);
+  }
+  if (h->plan_n != nchunks) plan_host_run(h, nchunks);
+  const int npc = (int)(h->plan.size() / 4);
+  cudaEvent_t* ev = h->hev.data();  // per piece: copied in, analysed; then entry and exit marks
+  // work issued earlier on the handle's stream and on s comes first
+  if (s != h->stream) {
+    cudaEventRecord(h->ran, h->stream);
+    cudaStreamWaitEvent(s, h->ran, 0);
+  }
+  cudaEventRecord(ev[2 * npc], s);
+  cudaStreamWaitEvent(h->cs_in, ev[2 * npc], 0);
+  cudaStreamWaitEvent(h->cs_out, ev[2 * npc], 0);
+  SweepArgs a;
+  build_args(h, a);
+  const size_t row = (size_t)h->d.ne * elem(h);
+  const int nv = h->d.nv;
+  int st = LETKF_OK;
+  for (int c = 0; c < npc && st == LETKF_OK; c++) {
+    const int64_t* e = &h->plan[(size_t)c * 4];
+    for (int64_t k = e[2]; k < e[3] && st == LETKF_OK; k++)
+      st = copy_rows(&h->pcopy[(size_t)k * 4], nv, np, row, h->xb, xb, cudaMemcpyHostToDevice, h->cs_in);
+    if (st != LETKF_OK) break;
+    cudaEventRecord(ev[2 * c], h->cs_in);
+    cudaStreamWaitEvent(s, ev[2 * c], 0);
+    SweepArgs b = a;
+    b.order = h->order + e[0];
+    b.nwork = (int)(e[1] - e[0]);
+    st = launch_mixed_run(h, b, s);
+    if (st != LETKF_OK) break;
+    cudaEventRecord(ev[2 * c + 1], s);
+    cudaStreamWaitEvent(h->cs_out, ev[2 * c + 1], 0);
+    for (int64_t k = e[2]; k < e[3] && st == LETKF_OK; k++)
+      st = copy_rows(&h->pcopy[(size_t)k * 4], nv, np, row, xa, h->xa, cudaMemcpyDeviceToHost, h->cs_out);
+  }
+  // s and the handle's stream complete after the last copies
+  cudaEventRecord(ev[2 * npc + 1], h->cs_out);
+  cudaStreamWaitEvent(s, ev[2 * npc + 1], 0);
+  cudaEventRecord(ev[2 * npc], h->cs_in);
+  cudaStreamWaitEvent(s, ev[2 * npc], 0);
+  if (s != h->stream) {
+    cudaEventRecord(h->ran, s);
+    cudaStreamWaitEvent(h->stream, h->ran, 0);
+  }
+  const int st2 = cuda_status(cudaStreamSynchronize(s));
+  if (st == LETKF_OK) st = st2;
+  return st != LETKF_OK ? st : check_err(h);
+}
+
 int letkf_sweep_autotune(letkf_sweep_t h, int sample_points, int* choice) {
   if (!h || sample_points < 1) return LETKF_ERR_ARG;
   if (h->d.precision == LETKF_PREC_F64 || h->d.npts == 0) {
@@ -712,7 +871,7 @@ int letkf_sweep_autotune(letkf_sweep_t h, int sample_points, int* choice) {
     h->tc_ns_scaled = cands[c].scaled;
     SweepArgs a;
     build_args(h, a);
-    a.npts = sample;  // the first `sample` points of the processing order
+    a.nwork = sample;  // the first `sample` points of the processing order
     float ms = 0.f;
     for (int rep = 0; rep < 2 && st == LETKF_OK; rep++) {  // warm-up, then timed
       cudaMemcpyAsync(h->infl, keep, np * sizeof(double), cudaMemcpyDeviceToDevice, s);

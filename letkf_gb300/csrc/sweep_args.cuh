@@ -34,6 +34,7 @@ struct SweepArgs {
   int max_sweeps;   // Jacobi sweeps (fallback eigensolver)
   int max_ns_iter;  // Newton-Schulz iterations
   int use_ns;       // 1: Newton-Schulz inverse square root, 0: Jacobi eigensolver
+  int nwork;            // entries of `order` to process (npts is the row stride of xb / xa)
   const int* npts_dev;  // if set, the number of entries of `order` to process (device scalar)
   int* defer_list;      // tensor-core sweep: points handed to the Jacobi pass
   int* defer_count;

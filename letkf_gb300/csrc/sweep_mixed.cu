@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(MixedCfg<NP>::NT, MixedCfg<NP>::MINB) sweep_mi
   const float band_lo = dzf2 * (1.f - SW_BAND), band_hi = dzf2 * (1.f + SW_BAND);
   const float dx2 = (float)(a.P.dx * a.P.dx), dy2 = (float)(a.P.dy * a.P.dy);
 
-  const int npts_work = a.npts_dev ? *a.npts_dev : a.npts;
+  const int npts_work = a.npts_dev ? *a.npts_dev : a.nwork;
   for (;;) {
     __syncthreads();
     if (tid == 0) ctrl[0] = atomicAdd(a.counter, 1);
@@ -399,7 +399,7 @@ static int launch_sweep_np(const SweepArgs& a, cudaStream_t stream, int grid_cap
   if (per_sm < 1) per_sm = 1;
   int grid = nsm * per_sm;
   if (grid_cap > 0 && grid > grid_cap) grid = grid_cap;
-  if (grid > a.npts) grid = a.npts > 0 ? a.npts : 1;
+  if (grid > a.nwork) grid = a.nwork > 0 ? a.nwork : 1;
   kern<<<grid, MixedCfg<NP>::NT, bytes, stream>>>(a);
   note_launch();
   return cuda_status(cudaGetLastError());
@@ -408,7 +408,7 @@ static int launch_sweep_np(const SweepArgs& a, cudaStream_t stream, int grid_cap
 int launch_sweep_mixed(const SweepArgs& a, cudaStream_t stream, int grid_cap) {
   if (a.n < 2 || a.nv < 1 || a.nv > 8) return LETKF_ERR_ARG;
   if (a.n > LETKF_MAX_NE) return LETKF_ERR_CAPACITY;
-  if (a.npts == 0) return LETKF_OK;
+  if (a.nwork == 0) return LETKF_OK;
   if (a.n <= 32) return launch_sweep_np<32>(a, stream, grid_cap);
   if (a.n <= 64) return launch_sweep_np<64>(a, stream, grid_cap);
   return launch_sweep_np<128>(a, stream, grid_cap);

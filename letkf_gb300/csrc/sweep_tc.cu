@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
   bool xb_outst = false;  // a TMA copy of background rows is in flight
   bool outst[2] = {false, false};
   int tmo = 0;  // this thread saw a bounded wait give up
-  const int npts_work = a.npts_dev ? *a.npts_dev : a.npts;
+  const int npts_work = a.npts_dev ? *a.npts_dev : a.nwork;
 
   auto wait_bar = [&](int i) {
     if (!tc::mbar_wait(&mbar[i], par[i], TC_WAIT)) tmo = 1;
@@ -872,7 +872,7 @@ int prepare_sweep_tc() {
 
 int launch_sweep_tc(const SweepArgs& a, cudaStream_t stream, int grid_cap) {
   if (a.n < 2 || a.n > TC_NP || a.nv < 1 || a.nv > 8) return LETKF_ERR_ARG;
-  if (a.npts == 0) return LETKF_OK;
+  if (a.nwork == 0) return LETKF_OK;
   constexpr size_t bytes = TcLayout::TOTAL;
   cudaError_t err = set_smem_once(sweep_tc_kernel, bytes, g_tc_attr);
   if (err != cudaSuccess) return cuda_status(err);
@@ -896,7 +896,7 @@ int launch_sweep_tc(const SweepArgs& a, cudaStream_t stream, int grid_cap) {
   if (per_sm > (int)(512 / TC_TMEM_COLS)) per_sm = 512 / TC_TMEM_COLS;
   int grid = nsm * per_sm;
   if (grid_cap > 0 && grid > grid_cap) grid = grid_cap;
-  if (grid > a.npts) grid = a.npts;
+  if (grid > a.nwork) grid = a.nwork;
   sweep_tc_kernel<<<grid, TC_NT, bytes, stream>>>(a);
   note_launch();
   return cuda_status(cudaGetLastError());

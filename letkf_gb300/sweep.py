@@ -46,6 +46,7 @@ _SIGS = {
     "letkf_sweep_set_inflation": [C.c_void_p, C.c_void_p, C.c_int],
     "letkf_sweep_set_option": [C.c_void_p, C.c_int, C.c_int],
     "letkf_sweep_run": [C.c_void_p, C.c_void_p],
+    "letkf_sweep_run_host": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p],
     "letkf_sweep_autotune": [C.c_void_p, C.c_int, C.c_void_p],
     "letkf_sweep_get_analysis": [C.c_void_p, C.c_void_p, C.c_int],
     "letkf_sweep_get_diagnostics": [C.c_void_p] * 5,
@@ -129,6 +130,29 @@ class Sweep:
     def run(self, stream=None):
         s = None if stream is None else C.c_void_p(stream)
         check(_L().letkf_sweep_run(self.h, s), "letkf_sweep_run")
+
+    def run_host(self, xb, xa=None, nchunks=16, stream=None):
+        """One analysis from host memory with the copies overlapped
+        (letkf_sweep_run_host): xb is an array [nv, npts, ne] or a host
+        address; xa likewise (a new array when None).  Page-locked buffers
+        (torch pin_memory) let the copies run beside the analysis.  Returns xa."""
+        d = self.desc
+        if isinstance(xb, int):
+            pb = C.c_void_p(xb)
+        else:
+            xb = np.ascontiguousarray(xb, dtype=self.dtype)
+            if xb.size != d.nv * d.npts * d.ne:
+                raise ValueError("run_host: xb must hold nv * npts * ne values")
+            pb = _p(xb)
+        if xa is None:
+            xa = np.empty((d.nv, d.npts, d.ne), dtype=self.dtype)
+        if not isinstance(xa, int) and (xa.dtype != self.dtype or not xa.flags.c_contiguous
+                                        or xa.size != d.nv * d.npts * d.ne):
+            raise ValueError("run_host: xa must be a contiguous [nv, npts, ne] array of the handle's type")
+        pa = C.c_void_p(xa) if isinstance(xa, int) else _p(xa)
+        s = None if stream is None else C.c_void_p(stream)
+        check(_L().letkf_sweep_run_host(self.h, pb, pa, int(nchunks), s), "letkf_sweep_run_host")
+        return xa
 
     def autotune(self, sample_points=32768):
         """Time the kernel / eigensolver variants on the first sample_points

@@ -328,3 +328,46 @@ def test_tile_handles_reproduce_the_single_domain_sweep(cuda, precision):
         np.testing.assert_array_equal(nobsl, dg_all["nobsl"])
         np.testing.assert_array_equal(infl, dg_all["infl"])
         np.testing.assert_array_equal(xa, xa_all)
+
+
+@pytest.mark.parametrize("tile,shuffle,ne,prec", [(4, False, 40, 1), (0, True, 64, 1), (8, False, 100, 1),
+                                                  (4, False, 50, 1), (4, True, 20, 0)])
+def test_run_host_overlapped_equals_run(cuda, tile, shuffle, ne, prec):
+    """letkf_sweep_run_host (background in, analysis and copies out in pieces
+    overlapped with the sweep) equals set_background + run + get_analysis bit
+    for bit: banded and scattered processing orders, several piece counts,
+    page-locked and pageable host buffers; the plain form runs the three calls."""
+    import torch
+
+    from letkf_gb300.sweep import PREC_F64, PREC_MIXED, Sweep
+
+    case, prm, perm, grd, so, varloc, hdxf, dep = _setup(ne=ne, f32=True)
+    npts = case["pri"].size
+    order = np.random.default_rng(5).permutation(npts) if shuffle else np.arange(npts)
+    pri, prj, prlev = (np.ascontiguousarray(case[k][order]) for k in ("pri", "prj", "prlev"))
+    dt = np.float32 if prec == 1 else np.float64
+    xbh = np.ascontiguousarray(case["xb"][:, order].astype(dt))
+    infl0 = np.full(npts, 1.05)
+    sw = Sweep(ne, case["nvar"], case["nlon"], case["nlat"], npts, prm, precision=PREC_MIXED if prec else PREC_F64)
+    try:
+        sw.set_points(pri, prj, prlev, tile=tile)
+        sw.set_obs(case["ri"], case["rj"], case["lev"], case["dat"], case["err"], dep, case["cls"],
+                   hdxf.astype(np.float32) if prec else hdxf)
+        sw.set_background(xbh)
+        sw.set_inflation(infl0)
+        sw.run()
+        ref = sw.analysis()
+        infl_ref = sw.diagnostics()["infl"]
+        pin_b = torch.from_numpy(xbh).pin_memory()
+        for nchunks in (1, 3, 7, 16):
+            pin_a = torch.zeros(xbh.shape, dtype=pin_b.dtype).pin_memory()
+            sw.set_background(np.zeros_like(xbh))      # the run must bring the background in itself
+            sw.set_inflation(infl0)
+            sw.run_host(pin_b.data_ptr(), pin_a.data_ptr(), nchunks)
+            np.testing.assert_array_equal(pin_a.numpy(), ref, err_msg=f"nchunks {nchunks}")
+            np.testing.assert_array_equal(sw.diagnostics()["infl"], infl_ref)
+        sw.set_background(np.zeros_like(xbh))
+        sw.set_inflation(infl0)
+        np.testing.assert_array_equal(sw.run_host(xbh, nchunks=5), ref)   # pageable buffers
+    finally:
+        sw.close()
