@@ -70,6 +70,10 @@ def parse():
                     help="1: spectrum-scaled tensor-core Newton-Schulz steps; 0: plain steps")
     ap.add_argument("--tc-tol", type=int, default=None, help="tensor-core phase exit at ||ZY-I||^2 < 10^-v")
     ap.add_argument("--polish-tol", type=int, default=None, help="FP32 polish last step at ||ZAZ/s-I||^2 < 10^-v")
+    ap.add_argument("--polish-probe", type=int, default=None,
+                    help="skip the FP32 polish where the anchored probe residual is below 10^-v (0: always polish)")
+    ap.add_argument("--ns-cond", type=int, default=None,
+                    help="Newton-Schulz only where the spectrum bound s/c < 10^v (0: no bound)")
     ap.add_argument("--tune-points", type=int, default=32768,
                     help="run the autotuner on this many points before timing (0: the options given)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
@@ -486,8 +490,8 @@ def run_gpu(args, rank, world, dist):
     import torch
 
     from letkf_gb300 import lib as L
-    from letkf_gb300.sweep import (OPT_EIGENSOLVER, OPT_POLISH_TOL, OPT_TC_NS_ITERS, OPT_TC_NS_SCALING, OPT_TC_NS_TOL,
-                                   OPT_TENSOR_CORES, PREC_F64, PREC_MIXED, Sweep)
+    from letkf_gb300.sweep import (OPT_EIGENSOLVER, OPT_NS_COND, OPT_POLISH_PROBE, OPT_POLISH_TOL, OPT_TC_NS_ITERS,
+                                   OPT_TC_NS_SCALING, OPT_TC_NS_TOL, OPT_TENSOR_CORES, PREC_F64, PREC_MIXED, Sweep)
     from letkf_gb300.workload import RegionalWorkload
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
@@ -508,6 +512,10 @@ def run_gpu(args, rank, world, dist):
         sw.set_option(OPT_TC_NS_TOL, args.tc_tol)
     if args.polish_tol is not None:
         sw.set_option(OPT_POLISH_TOL, args.polish_tol)
+    if args.polish_probe is not None:
+        sw.set_option(OPT_POLISH_PROBE, args.polish_probe)
+    if args.ns_cond is not None:
+        sw.set_option(OPT_NS_COND, args.ns_cond)
     sw.set_background_device(xb.data_ptr())
     infl0 = np.ones(wl.npts)
     sw.set_inflation(infl0)
@@ -570,6 +578,7 @@ def run_gpu(args, rank, world, dist):
                         "p99": float(np.percentile(nl, 99)), "max": int(nl.max()), "zero_frac": float((nl == 0).mean())}
     out["transform"] = {"method": args.eig, "tensor_cores": bool(args.tc and args.ne <= 64 and args.eig == "newton-schulz"),
                         "scaled_steps": bool(args.tc_scaling), "autotune": tuned,
+                        "deferred_to_jacobi": sw.deferred(),
                         "iterations_mean": float(dg["sweeps"][nobsl > 0].mean()) if (nobsl > 0).any() else 0.0,
                         "iterations_max": int(dg["sweeps"].max())}
     if args.no_extras:

@@ -357,6 +357,12 @@ int letkf_l96_obs_cell(int nx, int ny, const double* h, int* cell, void* stream)
 #define LETKF_OPT_GRAPH 9         /* 1 (default): the mixed-form run is a CUDA graph, replayed while arguments stay the same */
 #define LETKF_OPT_TC_POLISH 10    /* 1: the anchored polish step of the tensor-core sweep on the tensor cores; 0 (default): FP32 */
 #define LETKF_OPT_TC_SCALE_BOUND 11 /* 1 (default): tensor-core scale s = min(||A||_F, Gershgorin), every step scaled; 0: power iteration */
+#define LETKF_OPT_POLISH_PROBE 12  /* tensor-core sweep, v > 0 (default 9): a point skips the FP32 polish when
+                                      ||Z (A/s) Z p - p||^2 < 10^-v ||p||^2 for a fixed pseudo-random p (three matvecs
+                                      against the exact A); 0: every point polished */
+#define LETKF_OPT_NS_COND 13       /* v > 0 (default 5): Newton-Schulz only where the spectrum bound s / c < 10^v, other
+                                      points go to the Jacobi pass; 0: no bound.  Either way a point whose transform is
+                                      not certified (no convergence, a large anchored residual) goes to the Jacobi pass */
 
 typedef struct letkf_sweep_desc {
   int ne;           /* ensemble size (MEMBER) */
@@ -413,6 +419,10 @@ int letkf_sweep_run_host(letkf_sweep_t h, const void* xb, void* xa, int nchunks,
  * 1000 points of the winner}.  The plain form has nothing to tune. */
 int letkf_sweep_autotune(letkf_sweep_t h, int sample_points, int* choice);
 int letkf_sweep_get_analysis(letkf_sweep_t h, void* xa, int on_device);
+/* points the last mixed-form run handed from the Newton-Schulz transform to the
+ * Jacobi pass (spectrum bound beyond the option, or a transform that did not
+ * certify); waits for the handle's stream.  0 for the plain form. */
+int letkf_sweep_deferred(letkf_sweep_t h, int* count);
 /* per-point updated inflation, local obs count, status and Jacobi sweeps (any may be NULL) */
 int letkf_sweep_get_diagnostics(letkf_sweep_t h, double* infl, int* nobsl, int* status, int* sweeps);
 /* the device-side nobsgrd table [(nlon+1)*nlat] after set_obs */

@@ -3,8 +3,8 @@
 // One CTA per point (persistent grid).  FP32 Gram on chip; the transform by
 // spectrum-scaled Newton-Schulz (W = sqrt((k-1)/s) (A/s)^(-1/2),
 // wbar = Z (Z b) / s) where mtx_eigen's truncation cannot act (c > 0 and
-// tr(G) < 1e6 c), else the parallel Jacobi eigensolver with the reference's
-// truncation; FP64 for the inflation sums.  Outputs FP32 trans / transm with
+// tr(G) < 1e6 c) and the iteration converges, else the parallel Jacobi
+// eigensolver with the reference's truncation; FP64 for the inflation sums.  Outputs FP32 trans / transm with
 // the semantics of common/common_letkf.f90:50-243 (transm present: trans = T,
 // transm = wbar; absent: trans = T + wbar 1^T).
 #include "mixed_core.cuh"
@@ -34,6 +34,11 @@ __global__ void __launch_bounds__(MixedCfg<NP>::NT) core_mixed_kernel(
       if (tid == 0) status[p] = LETKF_OK;
       continue;
     }
+    // Newton-Schulz first where it applies; a point it does not converge for
+    // is done again with the eigensolver (its Gram recomputed: the iteration
+    // overwrote A)
+    bool try_ns = use_ns != 0;
+  gram_again:
     GramAcc<NP> acc;
     acc.zero();
     for (int c0 = 0; c0 < L; c0 += S::CH) {
@@ -59,9 +64,15 @@ __global__ void __launch_bounds__(MixedCfg<NP>::NT) core_mixed_kernel(
     const float c = (float)((double)(n - 1) / infl);
     for (int i = tid; i < NP; i += C::NT) sm[S::A + i * NP + i] += c;
     __syncthreads();
-    if (use_ns && c > 0.f && trace < 1.0e6 * (double)c) {
+    if (try_ns && c > 0.f && trace < 1.0e6 * (double)c) {
       int its = 0;
-      const float s = ns_invsqrt<NP>(sm, c, 24, &its);
+      bool ok = false;
+      const float s = ns_invsqrt<NP>(sm, c, 24, &its, 0.f, &ok);
+      if (!ok) {
+        try_ns = false;  // uniform over the CTA
+        __syncthreads();
+        goto gram_again;
+      }
       const float* Z = sm + S::V;
       if (tid < NP) {
         float g = 0.f;

@@ -325,7 +325,8 @@ __device__ __forceinline__ void sym_gemm_tile(const float* X, const float* Yb, i
 // quadratic convergence then reaches the FP32 floor) or max_iter.  Returns the
 // iterations done; Y, Z hold the last iterate.
 template <int NP>
-__device__ int ns_iterate(float* Y, float* Z, float* T, float* redf, int max_iter, float lo = -1.f) {
+__device__ int ns_iterate(float* Y, float* Z, float* T, float* redf, int max_iter, float lo = -1.f,
+                           bool* conv = nullptr) {
   // lo >= 0: the spectrum of ZY starts in [lo, 1] and every step is
   // spectrum-scaled (Y' = sqrt(a) Y (3I - aT) / 2, likewise Z; see ns_scale);
   // lo < 0: plain steps
@@ -384,6 +385,7 @@ __device__ int ns_iterate(float* Y, float* Z, float* T, float* redf, int max_ite
       break;
     }
   }
+  if (conv) *conv = last;  // uniform: e2 is a block sum
   return it;
 }
 
@@ -392,7 +394,8 @@ __device__ int ns_iterate(float* Y, float* Z, float* T, float* redf, int max_ite
 // symmetrised.  Stops after the step following ||Q - I||_F < 1e-4 or after
 // max_iter; returns the iterations done.  P is scratch (NP x NP).
 template <int NP>
-__device__ int ns_polish(const float* As, float* Z, float* P, float* redf, int max_iter, float tol = 1.0e-8f) {
+__device__ int ns_polish(const float* As, float* Z, float* P, float* redf, int max_iter, float tol = 1.0e-8f,
+                         bool* conv = nullptr) {
   using C = MixedCfg<NP>;
   constexpr int NTI = NP / C::TR;
   const int tid = threadIdx.x;
@@ -458,14 +461,20 @@ __device__ int ns_polish(const float* As, float* Z, float* P, float* redf, int m
       break;
     }
   }
+  if (conv) *conv = last;
   return it;
 }
 
 // Newton-Schulz on sm[A] (SPD, all eigenvalues >= cdiag > 0).  Leaves
 // Z = (A/s)^(-1/2) in sm[V] (row-major, symmetric), scratch in sm[NS::T], and
-// returns s (> 0); *iters gets the iterations used.
+// returns s (> 0); *iters gets the iterations used.  *ok (may be NULL) tells
+// whether Z is good: false when the spectrum bound s / cdiag is not below
+// cond_max (> 0; A is then left untouched) or when the iteration did not
+// converge within max_iter (A is then overwritten).  Either way the caller
+// needs the eigensolver for this point.
 template <int NP>
-__device__ float ns_invsqrt(float* sm, float cdiag, int max_iter, int* iters) {
+__device__ float ns_invsqrt(float* sm, float cdiag, int max_iter, int* iters, float cond_max = 0.f,
+                            bool* ok = nullptr) {
   using C = MixedCfg<NP>;
   using S = MixedSmem<NP>;
   using N = NSSmem<NP>;
@@ -498,6 +507,11 @@ __device__ float ns_invsqrt(float* sm, float cdiag, int max_iter, int* iters) {
   __syncthreads();
   const float fro = sqrtf(block_sum<float, C::NT>(f2, redf));
   const float s = fminf(gmax, fro);
+  if (cond_max > 0.f && !(s < cond_max * cdiag)) {
+    if (iters) *iters = 0;
+    if (ok) *ok = false;
+    return s;
+  }
   const float inv_s = 1.f / s;
   // Y0 = A/s (in place), Z0 = I
   for (int idx = tid; idx < NP * NP; idx += C::NT) {
@@ -505,8 +519,10 @@ __device__ float ns_invsqrt(float* sm, float cdiag, int max_iter, int* iters) {
     Z[idx] = (idx / NP == idx % NP) ? 1.f : 0.f;
   }
   __syncthreads();
-  const int it = ns_iterate<NP>(A, Z, T, redf, max_iter, 0.9f * cdiag * inv_s);
+  bool conv = false;
+  const int it = ns_iterate<NP>(A, Z, T, redf, max_iter, 0.9f * cdiag * inv_s, &conv);
   if (iters) *iters = it;
+  if (ok) *ok = conv;
   return s;
 }
 

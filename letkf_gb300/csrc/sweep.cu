@@ -139,7 +139,7 @@ struct letkf_sweep_s {
   void *xb = nullptr, *xa = nullptr;
   double* infl = nullptr;
   int *status = nullptr, *nobsl = nullptr, *sweeps = nullptr, *counter = nullptr;
-  int *defer_list = nullptr, *defer_count = nullptr, *err_flag = nullptr;
+  int *defer_list = nullptr, *defer_count = nullptr, *defer_total = nullptr, *err_flag = nullptr;
   cudaStream_t stream = nullptr;
   cudaEvent_t ran = nullptr;  // recorded after a run issued on another stream
   int grid_cap = 0;
@@ -152,6 +152,8 @@ struct letkf_sweep_s {
   int polish_tol_exp = 7;
   int tc_polish = 0;
   int tc_scale_bound = 1;
+  int polish_probe_exp = 9;
+  int ns_cond_exp = 5;
   // CUDA graph of the mixed-form run: replayed while the kernel arguments,
   // launch choices and stream stay the same, captured again otherwise
   int use_graph = 1;
@@ -220,6 +222,7 @@ int letkf_sweep_create(letkf_sweep_t* out, const letkf_sweep_desc* d) {
   st |= dalloc(&h->counter, 1, s);
   st |= dalloc(&h->defer_list, np, s);
   st |= dalloc(&h->defer_count, 1, s);
+  st |= dalloc(&h->defer_total, 1, s);
   st |= dalloc(&h->err_flag, 1, s);
   st |= dalloc(&h->G, (size_t)(d->nlon + 1) * d->nlat, s);
   if (st != LETKF_OK) {
@@ -229,6 +232,7 @@ int letkf_sweep_create(letkf_sweep_t* out, const letkf_sweep_desc* d) {
   cudaMemsetAsync(h->prz, 0, np * sizeof(double), s);
   cudaMemsetAsync(h->G, 0, sizeof(int) * (d->nlon + 1) * d->nlat, s);
   cudaMemsetAsync(h->err_flag, 0, sizeof(int), s);
+  cudaMemsetAsync(h->defer_total, 0, sizeof(int), s);
   std::vector<double> one(np, 1.0);
   cudaMemcpyAsync(h->infl, one.data(), np * sizeof(double), cudaMemcpyHostToDevice, s);
   st = cuda_status(cudaStreamSynchronize(s));
@@ -245,7 +249,7 @@ int letkf_sweep_destroy(letkf_sweep_t h) {
   void* ptrs[] = {h->pri,  h->prj,   h->prlev, h->prz,   h->plogr,   h->order, h->ori,     h->orj,    h->olev,
                   h->odat, h->oerr,  h->odep,  h->ocls,  h->ovarloc, h->G,     h->var_local, h->obsF,
                   h->obsA, h->meta,  h->ens32, h->ens64, h->xb,    h->xa,      h->infl,   h->status,
-                  h->nobsl, h->sweeps, h->counter, h->defer_list, h->defer_count, h->err_flag};
+                  h->nobsl, h->sweeps, h->counter, h->defer_list, h->defer_count, h->defer_total, h->err_flag};
   if (h->stream) {
     for (void* p : ptrs) dfree(p, h->stream);
     cudaStreamSynchronize(h->stream);
@@ -489,6 +493,14 @@ int letkf_sweep_set_option(letkf_sweep_t h, int option, int value) {
       if (value != 0 && value != 1) return LETKF_ERR_ARG;
       h->tc_scale_bound = value;
       return LETKF_OK;
+    case LETKF_OPT_POLISH_PROBE:
+      if (value < 0 || value > 14) return LETKF_ERR_ARG;
+      h->polish_probe_exp = value;
+      return LETKF_OK;
+    case LETKF_OPT_NS_COND:
+      if (value < 0 || value > 8) return LETKF_ERR_ARG;
+      h->ns_cond_exp = value;
+      return LETKF_OK;
     case LETKF_OPT_GRAPH:
       if (value != 0 && value != 1) return LETKF_ERR_ARG;
       h->use_graph = value;
@@ -626,6 +638,9 @@ static void build_args(letkf_sweep_t h, SweepArgs& a) {
   a.polish_tol = (float)std::pow(10.0, -h->polish_tol_exp);
   a.tc_polish = h->tc_polish;
   a.tc_scale_bound = h->tc_scale_bound;
+  a.polish_probe = h->polish_probe_exp > 0 ? (float)std::pow(10.0, -h->polish_probe_exp) : 0.f;
+  a.ns_cond_max = h->ns_cond_exp > 0 ? (float)std::pow(10.0, h->ns_cond_exp) : 0.f;
+  a.defer_total = h->defer_total;
   a.defer_list = h->defer_list;  // read by the tensor-core sweep only
   a.defer_count = h->defer_count;
 }
@@ -634,25 +649,26 @@ static bool tc_path(letkf_sweep_t h) { return h->use_tc && h->use_ns && h->d.ne 
 
 static int launch_mixed_run(letkf_sweep_t h, const SweepArgs& a, cudaStream_t s) {
   cudaMemsetAsync(h->counter, 0, sizeof(int), s);
-  if (tc_path(h)) {
-    // tensor-core sweep, then the Jacobi pass over the points it deferred
-    cudaMemsetAsync(h->defer_count, 0, sizeof(int), s);
-    int st = launch_sweep_tc(a, s, h->grid_cap);
-    if (st != LETKF_OK) return st;
-    SweepArgs b = a;
-    b.order = h->defer_list;
-    b.npts_dev = h->defer_count;
-    b.use_ns = 0;
-    cudaMemsetAsync(h->counter, 0, sizeof(int), s);
-    return launch_sweep_mixed(b, s, h->grid_cap);
-  }
-  return launch_sweep_mixed(a, s, h->grid_cap);
+  const bool tc = tc_path(h);
+  if (!tc && !a.use_ns) return launch_sweep_mixed(a, s, h->grid_cap);
+  // Newton-Schulz sweep (tensor-core or SIMT), then the Jacobi pass over the
+  // points it deferred
+  cudaMemsetAsync(h->defer_count, 0, sizeof(int), s);
+  int st = tc ? launch_sweep_tc(a, s, h->grid_cap) : launch_sweep_mixed(a, s, h->grid_cap);
+  if (st != LETKF_OK) return st;
+  SweepArgs b = a;
+  b.order = h->defer_list;
+  b.npts_dev = h->defer_count;
+  b.use_ns = 0;
+  cudaMemsetAsync(h->counter, 0, sizeof(int), s);
+  return launch_sweep_mixed(b, s, h->grid_cap);
 }
 
 static int run_on(letkf_sweep_t h, cudaStream_t s) {
   if (h->d.precision == LETKF_PREC_F64) return run_f64(h, s);
   SweepArgs a;
   build_args(h, a);
+  cudaMemsetAsync(h->defer_total, 0, sizeof(int), s);
   if (!h->use_graph) return launch_mixed_run(h, a, s);
   // key: kernel arguments, launch choices and stream
   std::vector<unsigned char> key(sizeof(a) + 3 * sizeof(int) + sizeof(s));
@@ -798,6 +814,7 @@ int letkf_sweep_run_host(letkf_sweep_t h, const void* xb, void* xa, int nchunks,
   cudaStreamWaitEvent(h->cs_out, ev[2 * npc], 0);
   SweepArgs a;
   build_args(h, a);
+  cudaMemsetAsync(h->defer_total, 0, sizeof(int), s);
   const size_t row = (size_t)h->d.ne * elem(h);
   const int nv = h->d.nv;
   int st = LETKF_OK;
@@ -922,6 +939,15 @@ int letkf_sweep_get_analysis(letkf_sweep_t h, void* xa, int on_device) {
   cudaMemcpyAsync(xa, h->xa, bytes, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream);
   const int st = cuda_status(cudaStreamSynchronize(h->stream));
   return st != LETKF_OK ? st : check_err(h);
+}
+
+int letkf_sweep_deferred(letkf_sweep_t h, int* count) {
+  if (!h || !count) return LETKF_ERR_ARG;
+  *count = 0;
+  if (h->d.precision == LETKF_PREC_F64) return LETKF_OK;
+  if (cudaMemcpyAsync(count, h->defer_total, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
+    return LETKF_ERR_CUDA;
+  return cuda_status(cudaStreamSynchronize(h->stream));
 }
 
 int letkf_sweep_get_diagnostics(letkf_sweep_t h, double* infl, int* nobsl, int* status, int* sweeps) {

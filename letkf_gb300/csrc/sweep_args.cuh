@@ -45,6 +45,10 @@ struct SweepArgs {
   float polish_tol;     // FP32 polish: last step once ||Z A Z / s - I||_F^2 < polish_tol
   int tc_polish;        // the anchored polish step on the tensor cores (1) or in FP32 (0)
   int tc_scale_bound;   // scale s from min(||A||_F, Gershgorin), every step scaled (1); power iteration (0)
+  float polish_probe;   // FP32 polish skipped where the anchored probe residual is below this (0: always polished)
+  float ns_cond_max;    // Newton-Schulz only while the spectrum bound s / c is below this (0: no bound); a
+                        // larger bound, or an iteration that does not converge, sends the point to the Jacobi pass
+  int* defer_total;     // points handed to the Jacobi pass in this run (the deferred pass adds its count)
 };
 
 }  // namespace letkf

@@ -279,7 +279,18 @@ __global__ void __launch_bounds__(MixedCfg<NP>::NT, MixedCfg<NP>::MINB) sweep_mi
         // Newton-Schulz: spectrum within [c, c + tr(G)], far from the
         // mtx_eigen truncation threshold lambda_max * sqrt(eps)
         int its = 0;
-        const float s = ns_invsqrt<NP>(sm, cdiag, a.max_ns_iter, &its);
+        bool ok = false;
+        const float s = ns_invsqrt<NP>(sm, cdiag, a.max_ns_iter, &its, a.ns_cond_max, &ok);
+        if (!ok) {
+          // spectrum bound beyond the iteration's range, or no convergence:
+          // the point goes to the Jacobi pass (ok is uniform over the CTA)
+          if (tid == 0) {
+            a.defer_list[atomicAdd(a.defer_count, 1)] = pt;
+            if (a.defer_total) atomicAdd(a.defer_total, 1);
+            if (a.nobsl_out) a.nobsl_out[pt] = L;
+          }
+          continue;
+        }
         sweeps = its;
         const float* Z = sm + S::V;
         if (tid < NP) {

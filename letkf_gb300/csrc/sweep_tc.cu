@@ -93,6 +93,13 @@ __device__ __forceinline__ float col_dot64(const float* M, const float* x, int c
   return (a0 + a1) + (a2 + a3);
 }
 
+// component j of the fixed probe vector: a multiplicative hash of j mapped to
+// [-1, 1), so the vector has weight in every eigen-direction of a point's A
+__device__ __forceinline__ float probe_component(int j) {
+  const uint32_t h = (uint32_t)(j + 1) * 2654435761u;
+  return (float)(h >> 8) * (2.0f / 16777216.0f) - 1.0f;
+}
+
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
   const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
   return *reinterpret_cast<const uint32_t*>(&v);
@@ -455,6 +462,13 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
         tc::fence_before_sync();
         __syncthreads();
         const float coef = sqrtf((float)(n - 1) / s);
+        // ok: Z is certified (the probe or the polish residual against the exact
+        // A is small).  A spectrum bound s / c beyond what the 16-bit products
+        // resolve skips the iteration; that point, and one whose certificate
+        // fails (no convergence, a non-finite residual), goes to the Jacobi pass.
+        bool ok = a.ns_cond_max > 0.f ? (s < a.ns_cond_max * cdiag) : true;
+        int it = 0;
+        if (ok) {
         // tensor-core phase: the iterations that move the small eigenvalues of
         // ZY towards 1; stop once ||ZY - I||_F^2 < tc_ns_tol (or after TC_NS_MAX).
         // Spectrum scaling: with X = ZY = (A/s) Z^2 and f(x) = x (3 - x)^2 / 4,
@@ -471,7 +485,6 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
         // keeps a x < 3 for the rounding of the 16-bit products.
         float lo = 0.9f * cdiag * inv_s;
         const float lo_top = f_ns(fminf(gmax * inv_s, 2.f));
-        int it = 0;
         const int tc_max = a.tc_ns_max;
         for (bool done = tc_max <= 0; !done; it++) {
           if (it == tc_max - 1) done = true;
@@ -665,7 +678,8 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
             tc::fence_before_sync();
             e2 = block_sum<float, TC_NT>(e2, red);
             pit++;
-            last = e2 < 1.0e-6f || pit >= TC_POLISH_MAX;
+            ok = e2 < 1.0e-6f;
+            last = ok || pit >= TC_POLISH_MAX;
             if (tid == 0) {
               tc::fence_after_sync();
               ns_mma(D0, sbase + L::S_HI, sbase + L::S_LO, sbase + L::B_HI, sbase + L::B_LO, idesc);
@@ -760,25 +774,58 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
           }
           tc::fence_before_sync();
           __syncthreads();
-          it += ns_polish<TC_NP>(Af, Zf, Pf, red, tc_max > 0 ? TC_POLISH_MAX : a.max_ns_iter, a.polish_tol);
+          // Probe of the anchored residual, three matvecs: e = ||Z (A/s) Z p - p||^2
+          // / ||p||^2 for a fixed pseudo-random p.  With Z = (A/s)^(-1/2) (I + E),
+          // Z (A/s) Z p - p = 2 E p to first order, so e estimates 4 ||E p||^2 /
+          // ||p||^2, the relative error the transform would carry into the
+          // analysis; a point whose estimate is below the probe tolerance already
+          // has the accuracy the polish would restore.  Z and A are symmetric, so
+          // the products read columns (consecutive lanes, no bank conflicts).
+          bool polish = true;
+          if (a.polish_probe > 0.f) {
+            float* pv = Pf;
+            float* pu = Pf + 64;
+            float* pw = Pf + 128;
+            if (tid < 64) pv[tid] = probe_component(tid);
+            __syncthreads();
+            if (tid < 64) pu[tid] = col_dot64(Zf, pv, tid);
+            __syncthreads();
+            if (tid < 64) pw[tid] = col_dot64(Af, pu, tid);
+            __syncthreads();
+            float q2[2] = {0.f, 0.f};
+            if (tid < 64) {
+              const float d = col_dot64(Zf, pw, tid) - pv[tid];
+              q2[0] = d * d;
+              q2[1] = pv[tid] * pv[tid];
+            }
+            block_sum_k<float, TC_NT, 2>(q2, red);
+            polish = !(q2[0] < a.polish_probe * q2[1]);  // a NaN residual polishes
+          }
+          if (polish)
+            it += ns_polish<TC_NP>(Af, Zf, Pf, red, tc_max > 0 ? TC_POLISH_MAX : a.max_ns_iter, a.polish_tol, &ok);
           for (int idx = tid; idx < 64 * 64; idx += TC_NT) Wm[idx] = coef * Zf[idx];
           __syncthreads();
         }
+        }  // ok: Newton-Schulz attempted
         if (tmo) break;
-        // wbar = Z (Z b) / s with Z = W / coef (W symmetric: column reads)
-        if (tid < 64) {
-          const float acc = col_dot64(Wm, vb, tid);
-          vg[tid] = acc / coef;
-        }
-        __syncthreads();
-        if (tid < 64) {
-          const float acc = col_dot64(Wm, vg, tid);
-          vwb[tid] = acc / (coef * s);
-        }
-        if (tid == 0) {
-          a.infl[pt] = infl_update(n, infl, (double)p1, (double)trace, (double)p3);
-          a.status[pt] = LETKF_OK;
-          if (a.sweeps_out) a.sweeps_out[pt] = it;
+        if (!ok) {
+          deferred = true;
+        } else {
+          // wbar = Z (Z b) / s with Z = W / coef (W symmetric: column reads)
+          if (tid < 64) {
+            const float acc = col_dot64(Wm, vb, tid);
+            vg[tid] = acc / coef;
+          }
+          __syncthreads();
+          if (tid < 64) {
+            const float acc = col_dot64(Wm, vg, tid);
+            vwb[tid] = acc / (coef * s);
+          }
+          if (tid == 0) {
+            a.infl[pt] = infl_update(n, infl, (double)p1, (double)trace, (double)p3);
+            a.status[pt] = LETKF_OK;
+            if (a.sweeps_out) a.sweeps_out[pt] = it;
+          }
         }
       }
     } else {
@@ -792,7 +839,10 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
     }
     if (tid == 0 && a.nobsl_out) a.nobsl_out[pt] = Lp;
     if (deferred) {
-      if (tid == 0) a.defer_list[atomicAdd(a.defer_count, 1)] = pt;
+      if (tid == 0) {
+        a.defer_list[atomicAdd(a.defer_count, 1)] = pt;
+        if (a.defer_total) atomicAdd(a.defer_total, 1);
+      }
       if (xb_outst) {
         wait_bar(3);
         xb_outst = false;

@@ -30,6 +30,8 @@ OPT_POLISH_TOL = 8
 OPT_GRAPH = 9
 OPT_TC_POLISH = 10
 OPT_TC_SCALE_BOUND = 11
+OPT_POLISH_PROBE = 12
+OPT_NS_COND = 13
 
 
 class SweepDesc(C.Structure):
@@ -50,6 +52,7 @@ _SIGS = {
     "letkf_sweep_autotune": [C.c_void_p, C.c_int, C.c_void_p],
     "letkf_sweep_get_analysis": [C.c_void_p, C.c_void_p, C.c_int],
     "letkf_sweep_get_diagnostics": [C.c_void_p] * 5,
+    "letkf_sweep_deferred": [C.c_void_p, C.c_void_p],
     "letkf_sweep_sorted_obs": [C.c_void_p, C.c_void_p],
     "letkf_sweep_device_buffers": [C.c_void_p] * 5,
 }
@@ -172,6 +175,12 @@ class Sweep:
 
     def analysis_into(self, host_ptr):
         check(_L().letkf_sweep_get_analysis(self.h, C.c_void_p(host_ptr), 0), "get_analysis")
+
+    def deferred(self):
+        """Points the last mixed-form run handed to the Jacobi pass."""
+        n = C.c_int(0)
+        check(_L().letkf_sweep_deferred(self.h, C.byref(n)), "letkf_sweep_deferred")
+        return n.value
 
     def diagnostics(self):
         n = self.desc.npts

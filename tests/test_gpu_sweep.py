@@ -13,9 +13,11 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 
 
-def _setup(seed=3, nlon=24, nlat=20, nlev=6, ne=40, nobs=2500, sigma_obs=10.0e3, f32=False, var_local=None):
+def _setup(seed=3, nlon=24, nlat=20, nlev=6, ne=40, nobs=2500, sigma_obs=10.0e3, f32=False, var_local=None,
+           err_scale=1.0):
     case = S.regional_case(seed, nlon=nlon, nlat=nlat, nlev=nlev, ne=ne, nobs=nobs, sigma_obs=sigma_obs,
                            dtype=np.float32 if f32 else np.float64)
+    case["err"] = case["err"] * err_scale
     prm = S.scale_params(case)
     perm, grd = O.scale_sort_obs(nlon, nlat, case["ri"], case["rj"])
     nob = perm.size
@@ -229,7 +231,7 @@ def test_graph_replay_equals_eager_runs(cuda, tc):
         g, gi = run(sw, xb, st.cuda_stream)
         np.testing.assert_array_equal(g, e)
         np.testing.assert_array_equal(gi, i)
-    assert L.launch_count() - n0 == 3 * (2 if tc else 1)      # replays count their kernels
+    assert L.launch_count() - n0 == 3 * 2   # replays count their kernels: sweep + deferred-point pass
     g, _ = run(sw, case["xb"])                                 # the handle's own stream: a new capture
     np.testing.assert_array_equal(g, e1)
     sw.set_option(OPT_TC_NS_SCALING, 0)                        # new kernel arguments: a new capture
@@ -369,5 +371,88 @@ def test_run_host_overlapped_equals_run(cuda, tile, shuffle, ne, prec):
         sw.set_background(np.zeros_like(xbh))
         sw.set_inflation(infl0)
         np.testing.assert_array_equal(sw.run_host(xbh, nchunks=5), ref)   # pageable buffers
+    finally:
+        sw.close()
+
+
+@pytest.mark.parametrize("err_scale", [1.0, 0.1])
+def test_polish_probe_keeps_the_mixed_form_accurate(cuda, err_scale):
+    """The default polish probe (LETKF_OPT_POLISH_PROBE 9) skips the FP32 polish
+    only where the anchored residual shows the tensor-core transform already
+    accurate: on a well- and an ill-conditioned case (observation errors x0.1)
+    the analysis meets the mixed-form bar and stays within 3x (or 1e-5 of
+    spread) of the always-polished sweep, and a probe that never asks for the
+    polish (10^-1) is no more accurate."""
+    from letkf_gb300.sweep import OPT_POLISH_PROBE, PREC_MIXED, Sweep
+
+    ne = 64
+    case, prm, perm, grd, so, varloc, hdxf, dep = _setup(ne=ne, f32=True, err_scale=err_scale)
+    xb = case["xb"].astype(np.float64)
+    npts = case["pri"].size
+    infl0 = np.full(npts, 1.05)
+    xa_ref, _, _ = so.sweep(hdxf[perm], dep[perm], xb, case["pri"], case["prj"], case["prlev"], infl0)
+    spread = _spread(xb)
+    err = {}
+    sw = Sweep(ne, case["nvar"], case["nlon"], case["nlat"], npts, prm, precision=PREC_MIXED)
+    try:
+        sw.set_points(case["pri"], case["prj"], case["prlev"])
+        sw.set_obs(case["ri"], case["rj"], case["lev"], case["dat"], case["err"], dep, case["cls"],
+                   hdxf.astype(np.float32))
+        sw.set_background(case["xb"])
+        for probe in (9, 0, 1):
+            sw.set_option(OPT_POLISH_PROBE, probe)
+            sw.set_inflation(infl0)
+            sw.run()
+            xa = sw.analysis().astype(np.float64)
+            assert (sw.diagnostics()["status"] == 0).all()
+            em = np.sqrt(np.mean((xa.mean(-1) - xa_ref.mean(-1)) ** 2)) / spread
+            ep = np.sqrt(np.mean(((xa - xa.mean(-1, keepdims=True))
+                                  - (xa_ref - xa_ref.mean(-1, keepdims=True))) ** 2)) / spread
+            err[probe] = (em, ep)
+    finally:
+        sw.close()
+    (em9, ep9), (em0, ep0), (em1, ep1) = err[9], err[0], err[1]
+    assert em9 < 1e-4 and ep9 < 1e-4, err
+    assert em9 <= max(3 * em0, 1e-5) and ep9 <= max(3 * ep0, 1e-5), err
+    assert ep1 >= 0.9 * ep9, err
+
+
+@pytest.mark.parametrize("tc", [1, 0])
+def test_ill_conditioned_points_go_to_the_jacobi_pass(cuda, tc):
+    """Observation errors x0.1 give most points a spectrum bound s / c beyond
+    the Newton-Schulz range: the sweep hands them (and any point whose
+    transform does not certify) to the Jacobi pass, so the analysis stays
+    finite and within the mixed-form bar of the oracle, with the local counts
+    bit-exact; LETKF_OPT_NS_COND 0 (no bound) relies on the certificate alone."""
+    from letkf_gb300.sweep import OPT_NS_COND, OPT_TENSOR_CORES, PREC_MIXED, Sweep
+
+    case, prm, perm, grd, so, varloc, hdxf, dep = _setup(ne=64, f32=True, err_scale=0.1)
+    xb = case["xb"].astype(np.float64)
+    npts = case["pri"].size
+    infl0 = np.full(npts, 1.05)
+    xa_ref, infl_ref, nl_ref = so.sweep(hdxf[perm], dep[perm], xb, case["pri"], case["prj"], case["prlev"], infl0)
+    spread = _spread(xb)
+    sw = Sweep(64, case["nvar"], case["nlon"], case["nlat"], npts, prm, precision=PREC_MIXED)
+    try:
+        sw.set_points(case["pri"], case["prj"], case["prlev"])
+        sw.set_obs(case["ri"], case["rj"], case["lev"], case["dat"], case["err"], dep, case["cls"],
+                   hdxf.astype(np.float32))
+        sw.set_background(case["xb"])
+        sw.set_option(OPT_TENSOR_CORES, tc)
+        for cond in (5, 0):
+            sw.set_option(OPT_NS_COND, cond)
+            sw.set_inflation(infl0)
+            sw.run()
+            xa = sw.analysis().astype(np.float64)
+            dg = sw.diagnostics()
+            assert np.isfinite(xa).all()
+            assert (dg["status"] == 0).all()
+            np.testing.assert_array_equal(dg["nobsl"], nl_ref)
+            assert sw.deferred() > npts // 2
+            em = np.sqrt(np.mean((xa.mean(-1) - xa_ref.mean(-1)) ** 2)) / spread
+            ep = np.sqrt(np.mean(((xa - xa.mean(-1, keepdims=True))
+                                  - (xa_ref - xa_ref.mean(-1, keepdims=True))) ** 2)) / spread
+            assert em < 1e-4 and ep < 1e-4, (cond, em, ep)
+            np.testing.assert_allclose(dg["infl"], infl_ref, rtol=1e-4)
     finally:
         sw.close()
