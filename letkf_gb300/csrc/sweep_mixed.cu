@@ -355,19 +355,28 @@ __global__ void __launch_bounds__(MixedCfg<NP>::NT, MixedCfg<NP>::MINB) sweep_mi
       xs[v * NP + m] = a.xb[((size_t)v * a.npts + pt) * n + m];
     }
     __syncthreads();
-    // mean and mean increment in FP64, one warp per variable
+    // mean: FP64 member sum, then an unevaluated FP32 pair mh + ml (xs - mh is
+    // exact for members within a factor of two of the mean); the spread-sized
+    // increment in FP32; the analysis mean kept as a pair for the stores
+    float* meanf = reinterpret_cast<float*>(meanv + 8);  // [v] = {hi, lo}
     for (int v = wid; v < nv; v += NT / 32) {
       double sx = 0.0;
       for (int m = lane; m < n; m += 32) sx += (double)xs[v * NP + m];
       const double mean = warp_sum(sx) / (double)n;
-      double dlt = 0.0;
+      const float mh = (float)mean, ml = (float)(mean - (double)mh);
+      float dlt = 0.f;
       for (int m = lane; m < n; m += 32) {
-        const float xp = (float)((double)xs[v * NP + m] - mean);
+        const float xp = (xs[v * NP + m] - mh) - ml;
         xs[v * NP + m] = xp;
-        dlt += (double)xp * (double)sm[S::WB + m];
+        dlt = fmaf(xp, sm[S::WB + m], dlt);
       }
       dlt = warp_sum(dlt);
-      if (lane == 0) meanv[8 + v] = mean + dlt;  // analysis mean, FP64
+      if (lane == 0) {
+        const double am = mean + (double)dlt;
+        const float ah = (float)am;
+        meanf[2 * v] = ah;
+        meanf[2 * v + 1] = (float)(am - (double)ah);
+      }
     }
     __syncthreads();
     for (int t = tid; t < nv * n; t += NT) {
@@ -375,7 +384,7 @@ __global__ void __launch_bounds__(MixedCfg<NP>::NT, MixedCfg<NP>::MINB) sweep_mi
       float s = 0.f;
       const float* xp = xs + v * NP;
       for (int k = 0; k < n; k++) s = fmaf(xp[k], sm[S::A + k * NP + m], s);
-      a.xa[((size_t)v * a.npts + pt) * n + m] = (float)(meanv[8 + v] + (double)s);
+      a.xa[((size_t)v * a.npts + pt) * n + m] = meanf[2 * v] + (s + meanf[2 * v + 1]);
     }
   }
 }
