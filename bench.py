@@ -414,7 +414,7 @@ def run_largek(args, dev):
     global grid, 6 variables, k = 512, 3e6 observations, SPEEDY lat/lon
     search.  One step = search (count + fill), gather of the local rows, the
     large-k core and the FP32 update of the 6 variables for the sampled
-    points; plus the analysis error of a few points against the FP64 oracle.
+    points; plus the analysis error of 16 points against the FP64 oracle.
     sigma_h = 60 km keeps the local counts in the O(1e2-1e3) range."""
     import torch
 
@@ -457,7 +457,7 @@ def run_largek(args, dev):
     # FP64 oracle on a few points (the same float32 rows and weights)
     from oracle import oracle as O
 
-    sub = np.arange(0, idx.size, max(1, idx.size // 6))[:6]
+    sub = np.arange(0, idx.size, max(1, idx.size // 16))[:16]
     o = offs.cpu().numpy()
     R = rows.double().cpu().numpy()
     rd_, rl_, d_ = (x.double().cpu().numpy() for x in (rdiag.to(torch.float32), rloc.to(torch.float32), dl))
