@@ -234,7 +234,7 @@ def config_block(args, wl):
     return {"workload": f"regional {args.nlon}x{args.nlat}x{args.nlev} (3 km), {args.nv} vars, k={args.ne}, "
                         f"{args.nobs} clustered obs, sigma_h={wl.sigma_obs:.0f} m, sigma_v={wl.sigma_obsv} ln p",
             "points_per_sweep": wl.npts, "ensemble": args.ne, "variables": args.nv, "observations": args.nobs,
-            "local_obs": "0-2000 per point", "form": "mixed (FP32 ensemble, Gram and transform; FP64 member sums, analysis mean carried as an FP32 hi + lo pair)",
+            "local_obs": "0-2000 per point", "form": "mixed (FP32 ensemble, Gram and transform; FP64 member sums and mean-increment accumulation, analysis mean carried as an FP32 hi + lo pair)",
             "l2": "inputs larger than L2 (background ensemble %.1f GB)" % (wl.npts * args.nv * args.ne * 4 / 1e9),
             "parallelism": f"dp{args.gpus} (independent domains per GPU)"}
 

@@ -356,23 +356,23 @@ __global__ void __launch_bounds__(MixedCfg<NP>::NT, MixedCfg<NP>::MINB) sweep_mi
     }
     __syncthreads();
     // mean: FP64 member sum, then an unevaluated FP32 pair mh + ml (xs - mh is
-    // exact for members within a factor of two of the mean); the spread-sized
-    // increment in FP32; the analysis mean kept as a pair for the stores
+    // exact for members within a factor of two of the mean); the increment
+    // accumulated in FP64; the analysis mean kept as a pair for the stores
     float* meanf = reinterpret_cast<float*>(meanv + 8);  // [v] = {hi, lo}
     for (int v = wid; v < nv; v += NT / 32) {
       double sx = 0.0;
       for (int m = lane; m < n; m += 32) sx += (double)xs[v * NP + m];
       const double mean = warp_sum(sx) / (double)n;
       const float mh = (float)mean, ml = (float)(mean - (double)mh);
-      float dlt = 0.f;
+      double dlt = 0.0;
       for (int m = lane; m < n; m += 32) {
         const float xp = (xs[v * NP + m] - mh) - ml;
         xs[v * NP + m] = xp;
-        dlt = fmaf(xp, sm[S::WB + m], dlt);
+        dlt = fma((double)xp, (double)sm[S::WB + m], dlt);
       }
       dlt = warp_sum(dlt);
       if (lane == 0) {
-        const double am = mean + (double)dlt;
+        const double am = mean + dlt;
         const float ah = (float)am;
         meanf[2 * v] = ah;
         meanf[2 * v + 1] = (float)(am - (double)ah);

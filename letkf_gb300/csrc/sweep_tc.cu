@@ -866,26 +866,26 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
       }
     }
     __syncthreads();
-    // The member sum stays FP64; the rest runs in FP32 on the mean as an
-    // unevaluated pair mh + ml (GB300's FP64 pipe is narrow): xs - mh is exact
-    // for members within a factor of two of the mean and ml carries the rest,
-    // the increment sum is spread-sized, and the analysis mean + increment is
-    // kept as a pair again for the stores.
+    // The member sum and the mean-increment accumulation stay FP64; centring
+    // and the stores run in FP32 on the mean as an unevaluated pair mh + ml
+    // (GB300's FP64 pipe is narrow): xs - mh is exact for members within a
+    // factor of two of the mean and ml carries the rest; the analysis mean
+    // (mean + increment) is kept as a pair again for the stores.
     float* meanf = reinterpret_cast<float*>(meanv + 8);  // [v] = {hi, lo}
     for (int v = wid; v < nv; v += TC_NT / 32) {
       double sx = 0.0;
       for (int mm = lane; mm < n; mm += 32) sx += (double)xs[v * 64 + mm];
       const double mean = warp_sum(sx) / (double)n;
       const float mh = (float)mean, ml = (float)(mean - (double)mh);
-      float dlt = 0.f;
+      double dlt = 0.0;
       for (int mm = lane; mm < n; mm += 32) {
         const float xp = (xs[v * 64 + mm] - mh) - ml;
         xs[v * 64 + mm] = xp;
-        dlt = fmaf(xp, vwb[mm], dlt);
+        dlt = fma((double)xp, (double)vwb[mm], dlt);
       }
       dlt = warp_sum(dlt);
       if (lane == 0) {
-        const double am = mean + (double)dlt;
+        const double am = mean + dlt;
         const float ah = (float)am;
         meanf[2 * v] = ah;
         meanf[2 * v + 1] = (float)(am - (double)ah);
