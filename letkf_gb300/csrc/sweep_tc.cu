@@ -202,6 +202,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
   bool outst[2] = {false, false};
   int tmo = 0;  // this thread saw a bounded wait give up
   const int npts_work = a.npts_dev ? *a.npts_dev : a.nwork;
+  const double inv_n = 1.0 / (double)n;  // one FP64 division per kernel, not per variable and point
 
   auto wait_bar = [&](int i) {
     if (!tc::mbar_wait(&mbar[i], par[i], TC_WAIT)) tmo = 1;
@@ -313,7 +314,8 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
     bool deferred = false;
     if (Lp > 0) {
       if (a.minfl > 0.0 && infl < a.minfl) infl = a.minfl;
-      const float cdiag = (float)((double)(n - 1) / infl);
+      // c = (k-1)/rho: one FP64 division by one thread, read after the barrier below
+      if (tid == 0) reinterpret_cast<float*>(ctrl)[1] = (float)((double)(n - 1) / infl);
       // G = D0[r] + D0[r+64] + D1[r] + D1[r+64]: warps 2-3 first, then warps 0-1 add
       if (wid >= 2) {
 #pragma unroll
@@ -330,6 +332,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
       }
       vbp[tid] = bpart;
       __syncthreads();
+      const float cdiag = reinterpret_cast<const float*>(ctrl)[1];
       if (wid < 2) {
 #pragma unroll
         for (int c0 = 0; c0 < 64; c0 += 16) {
@@ -811,20 +814,21 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
         if (!ok) {
           deferred = true;
         } else {
-          // wbar = Z (Z b) / s with Z = W / coef (W symmetric: column reads)
+          // wbar = Z (Z b) / s with Z = W / coef (W symmetric: column reads);
+          // meanwhile a thread of the upper half, idle here, does the FP64
+          // inflation update
           if (tid < 64) {
             const float acc = col_dot64(Wm, vb, tid);
             vg[tid] = acc / coef;
+          } else if (tid == 64) {
+            a.infl[pt] = infl_update(n, infl, (double)p1, (double)trace, (double)p3);
+            a.status[pt] = LETKF_OK;
+            if (a.sweeps_out) a.sweeps_out[pt] = it;
           }
           __syncthreads();
           if (tid < 64) {
             const float acc = col_dot64(Wm, vg, tid);
             vwb[tid] = acc / (coef * s);
-          }
-          if (tid == 0) {
-            a.infl[pt] = infl_update(n, infl, (double)p1, (double)trace, (double)p3);
-            a.status[pt] = LETKF_OK;
-            if (a.sweeps_out) a.sweeps_out[pt] = it;
           }
         }
       }
@@ -875,7 +879,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
     for (int v = wid; v < nv; v += TC_NT / 32) {
       double sx = 0.0;
       for (int mm = lane; mm < n; mm += 32) sx += (double)xs[v * 64 + mm];
-      const double mean = warp_sum(sx) / (double)n;
+      const double mean = warp_sum(sx) * inv_n;
       const float mh = (float)mean, ml = (float)(mean - (double)mh);
       double dlt = 0.0;
       for (int mm = lane; mm < n; mm += 32) {
