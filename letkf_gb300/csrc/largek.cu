@@ -17,7 +17,9 @@
 //      tracked lower spectral bound, as in the tensor-core sweep); a
 //      residual above what a spectrum in [lo, 1] allows restarts the point
 //   4. two uncoupled steps anchored to A:  Z <- 1.5 Z - 0.5 (Z (A/s) Z) Z,
-//      symmetrised
+//      symmetrised; then a certificate: the anchored residual
+//      ||Z (A/s) Z p - p||^2 / ||p||^2 for a fixed probe p must be below 1e-6,
+//      else the point is reported as not converged (LETKF_ERR_EIG)
 //   5. W = sqrt((k-1)/s) Z, wbar = Z (Z Ywᵀdep) / s, inflation update.
 // Points with no local observations take the nobsl = 0 branch; points with
 // c <= 0 or tr(G) >= 1e6 c (where mtx_eigen's truncation could act) are
@@ -33,6 +35,7 @@ constexpr int LKP_NT = 256;
 constexpr float LK_NS_TOL = 1.0e-4f;  // ||ZY - I||_F^2 at which the coupled phase stops
 constexpr int LK_NS_MAX = 40;
 constexpr int LK_POLISH = 2;
+constexpr float LK_CERT_TOL = 1.0e-6f;  // anchored probe residual a finished transform must reach
 
 struct LkPoint {  // per-point scalars of a batch
   double s, c, p1, p3, trace, infl;
@@ -263,6 +266,63 @@ __global__ void lk_restart_kernel(int kp, const float* __restrict__ G, float* Y,
 __global__ void lk_reactivate_kernel(int nb, const LkPoint* __restrict__ pt, int* active) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b < nb) active[b] = pt[b].kind == 0;
+}
+
+// Certificate of a finished transform, three matvecs against the exact A (G
+// holds A): e = ||Z (A/s) Z p - p||^2 / ||p||^2 for the fixed probe vector p on
+// the ensemble coordinates.  With Z = (A/s)^(-1/2) (I + E) the residual is
+// 2 E p to first order; a point with e not below tol (or not finite) is
+// reported as not converged instead of returning its transform.  Column
+// reads of the symmetric matrices keep the loads coalesced.
+__global__ void __launch_bounds__(LKP_NT) lk_certify_kernel(int ne, int kp, const float* __restrict__ Z,
+                                                             const float* __restrict__ G,
+                                                             const float* __restrict__ inv_s, LkPoint* pt,
+                                                             float tol) {
+  __shared__ float vp[LETKF_LARGEK_MAX_NE], vu[LETKF_LARGEK_MAX_NE], vw[LETKF_LARGEK_MAX_NE];
+  __shared__ float red[2 * (LKP_NT / 32)];
+  const int b = blockIdx.x, tid = threadIdx.x;
+  if (pt[b].kind != 0) return;
+  const size_t mo = (size_t)b * kp * kp;
+  const float* Zb = Z + mo;
+  const float* Ab = G + mo;
+  const float is = inv_s[b];
+  for (int i = tid; i < kp; i += LKP_NT) vp[i] = i < ne ? probe_component(i) : 0.f;
+  __syncthreads();
+  for (int i = tid; i < kp; i += LKP_NT) {
+    float acc = 0.f;
+    for (int j = 0; j < kp; j++) acc = fmaf(Zb[(size_t)j * kp + i], vp[j], acc);
+    vu[i] = acc;
+  }
+  __syncthreads();
+  for (int i = tid; i < kp; i += LKP_NT) {
+    float acc = 0.f;
+    for (int j = 0; j < kp; j++) acc = fmaf(Ab[(size_t)j * kp + i], vu[j], acc);
+    vw[i] = acc * is;
+  }
+  __syncthreads();
+  float e = 0.f, pn = 0.f;
+  for (int i = tid; i < kp; i += LKP_NT) {
+    float acc = 0.f;
+    for (int j = 0; j < kp; j++) acc = fmaf(Zb[(size_t)j * kp + i], vw[j], acc);
+    const float d = acc - vp[i];
+    e = fmaf(d, d, e);
+    pn = fmaf(vp[i], vp[i], pn);
+  }
+  e = warp_sum(e);
+  pn = warp_sum(pn);
+  if ((tid & 31) == 0) {
+    red[tid >> 5] = e;
+    red[LKP_NT / 32 + (tid >> 5)] = pn;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    float es = 0.f, ps = 0.f;
+    for (int w = 0; w < LKP_NT / 32; w++) {
+      es += red[w];
+      ps += red[LKP_NT / 32 + w];
+    }
+    if (!(es < tol * ps)) pt[b].kind = 3;
+  }
 }
 
 // Z <- (Zn + Znᵀ) / 2 for active points
@@ -579,6 +639,11 @@ extern "C" int letkf_core_batch_largek(int ne, int npts, const int64_t* offs, co
       if (st) break;
       dim3 sg(64, nb);
       lk_symmetrize_kernel<<<sg, 256, 0, s>>>(kp, Zn, Z, active);
+      note_launch();
+    }
+    // certificate of every transform against the exact A
+    if (st == LETKF_OK) {
+      lk_certify_kernel<<<nb, LKP_NT, 0, s>>>(ne, kp, Z, G, inv_s, pt, LK_CERT_TOL);
       note_launch();
     }
     // 5. transform, mean weights, inflation

@@ -615,6 +615,14 @@ __device__ __forceinline__ void form_w(float* sm, Out out) {
 }
 
 // Adaptive inflation (common/common_letkf.f90:218-239) from FP64 sums.
+// component j of the fixed probe vector of the transform certificates: a
+// multiplicative hash of j mapped to [-1, 1), so the vector has weight in
+// every eigen-direction of a point's A
+__device__ __forceinline__ float probe_component(int j) {
+  const uint32_t h = (uint32_t)(j + 1) * 2654435761u;
+  return (float)(h >> 8) * (2.0f / 16777216.0f) - 1.0f;
+}
+
 __device__ __forceinline__ double infl_update(int n, double infl, double p1, double trace, double p3) {
   const double q2 = trace / (double)(n - 1);
   const double q4 = (p1 - p3) / q2 - infl;

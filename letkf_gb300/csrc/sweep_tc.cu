@@ -93,13 +93,6 @@ __device__ __forceinline__ float col_dot64(const float* M, const float* x, int c
   return (a0 + a1) + (a2 + a3);
 }
 
-// component j of the fixed probe vector: a multiplicative hash of j mapped to
-// [-1, 1), so the vector has weight in every eigen-direction of a point's A
-__device__ __forceinline__ float probe_component(int j) {
-  const uint32_t h = (uint32_t)(j + 1) * 2654435761u;
-  return (float)(h >> 8) * (2.0f / 16777216.0f) - 1.0f;
-}
-
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
   const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
   return *reinterpret_cast<const uint32_t*>(&v);

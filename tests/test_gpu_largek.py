@@ -84,3 +84,34 @@ def test_largek_special_points(cuda):
     ref = O.letkf_core_batch(ne, offs[2:] - offs[2], rows[offs[2]:], rd[offs[2]:], rl[offs[2]:], d[offs[2]:],
                              infl[2:], want_transm=True)
     assert np.abs(tr[2] - ref["trans"][0]).max() <= 1e-4 * np.abs(ref["trans"][0]).max()
+
+
+@pytest.mark.parametrize("rd_scale", [1e-2, 1e-4])
+def test_largek_ill_conditioned_points_are_certified_or_flagged(cuda, rd_scale):
+    """Small observation-error variances stretch the spectrum of A: every point
+    either returns a certified transform (finite, within 1e-3 of the oracle's
+    largest entry) or is flagged (LETKF_ERR_EIG for no convergence,
+    LETKF_ERR_CAPACITY where mtx_eigen's truncation could act); none returns a
+    wrong transform with status OK."""
+    import torch
+
+    from letkf_gb300.core import core_batch_largek
+    from letkf_gb300.lib import LETKF_ERR_CAPACITY, LETKF_ERR_EIG, LETKF_OK
+
+    ne = 256
+    rng = np.random.default_rng(int(1 / rd_scale))
+    Ls = [300, 700, 150, 512, 90, 1000, 33, 400]
+    offs, rows, rd, rl, d, infl = _batch(rng, ne, Ls)
+    rd = (rd * rd_scale).astype(np.float32).astype(np.float64)
+    ref = O.letkf_core_batch(ne, offs, rows, rd, rl, d, infl, want_transm=True)
+    t = lambda a, dt=torch.float32: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=cuda)
+    out = core_batch_largek(ne, t(offs, torch.int64), t(rows), t(rd), t(rl), t(d), t(infl, torch.float64),
+                            want_transm=True)
+    torch.cuda.synchronize()
+    st = out["status"].cpu().numpy()
+    assert set(np.unique(st)) <= {LETKF_OK, LETKF_ERR_EIG, LETKF_ERR_CAPACITY}
+    tr = out["trans"].cpu().numpy().astype(np.float64)
+    for p in np.where(st == LETKF_OK)[0]:
+        assert np.isfinite(tr[p]).all(), p
+        scale = np.abs(ref["trans"][p]).max()
+        assert np.abs(tr[p] - ref["trans"][p]).max() <= 1e-3 * scale, (p, Ls[p])
