@@ -736,36 +736,34 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
           //   Q = Z (A/s) Z,  Z <- (3 Z - Q Z) / 2,
           // which references the exact A (kept in TMEM) at every step and so
           // converges to (A/s)^(-1/2) from the tensor-core estimate.
-          float* Zf = reinterpret_cast<float*>(sm + L::ZF);
+          // Z goes to the free B area (it becomes W in place there: TF == WMAT),
+          // so rows of S are converted straight out of their 16-bit split; A / s
+          // overwrites S_HI once every row of S has been read
+          static_assert(L::TF == L::WMAT, "Z is scaled into W in place");
+          float* Zf = reinterpret_cast<float*>(sm + L::TF);
           float* Af = reinterpret_cast<float*>(sm + L::YF);  // A / s
-          float* Pf = reinterpret_cast<float*>(sm + L::TF);  // A Z, then Q
-          {
-            float row[64];
-            if (r >= 64) {
+          float* Pf = reinterpret_cast<float*>(sm + L::ZF);  // A Z, then Q; the probe vectors
+          if (r >= 64) {
+            float* dst = Zf + (r - 64) * 64;
   #pragma unroll
-              for (int c0 = 0; c0 < 64; c0 += 8) {
-                const uint32_t off = tc::kmajor_off_bf16(r, c0, 64);
-                float sh[8], sl[8];
-                unpack8(*reinterpret_cast<const uint4*>(sm + L::S_HI + off), sh);
-                unpack8(*reinterpret_cast<const uint4*>(sm + L::S_LO + off), sl);
-  #pragma unroll
-                for (int j = 0; j < 8; j++) row[c0 + j] = sh[j] + sl[j];
-              }
+            for (int c0 = 0; c0 < 64; c0 += 8) {
+              const uint32_t off = tc::kmajor_off_bf16(r, c0, 64);
+              float sh[8], sl[8];
+              unpack8(*reinterpret_cast<const uint4*>(sm + L::S_HI + off), sh);
+              unpack8(*reinterpret_cast<const uint4*>(sm + L::S_LO + off), sl);
+              *reinterpret_cast<float4*>(dst + c0) = make_float4(sh[0] + sl[0], sh[1] + sl[1], sh[2] + sl[2], sh[3] + sl[3]);
+              *reinterpret_cast<float4*>(dst + c0 + 4) =
+                  make_float4(sh[4] + sl[4], sh[5] + sl[5], sh[6] + sl[6], sh[7] + sl[7]);
             }
-            __syncthreads();
-            if (r >= 64) {
-              float* dst = Zf + (r - 64) * 64;
+          }
+          __syncthreads();
+          if (r < 64) {
   #pragma unroll
-              for (int j = 0; j < 64; j += 4)
-                *reinterpret_cast<float4*>(dst + j) = make_float4(row[j], row[j + 1], row[j + 2], row[j + 3]);
-            } else {
+            for (int c0 = 0; c0 < 64; c0 += 16) {
+              float v[16];
+              tc::tmem_ld16(D1 + lane_off + c0, v);
   #pragma unroll
-              for (int c0 = 0; c0 < 64; c0 += 16) {
-                float v[16];
-                tc::tmem_ld16(D1 + lane_off + c0, v);
-  #pragma unroll
-                for (int j = 0; j < 16; j++) Af[r * 64 + c0 + j] = v[j] * inv_s;
-              }
+              for (int j = 0; j < 16; j++) Af[r * 64 + c0 + j] = v[j] * inv_s;
             }
           }
           tc::fence_before_sync();
