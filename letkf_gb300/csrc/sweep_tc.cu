@@ -190,16 +190,19 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
   const uint32_t D0 = tbase, D1 = tbase + 64;
   const uint32_t lane_off = (uint32_t)(wid * 32) << 16;
   const int r = tid;  // the tile row this thread owns in TMEM / S
-  uint32_t par[4] = {0u, 0u, 0u, 0u};
+  // mbarrier phase parities (bit i: barrier i) and the Gram stages with MMAs in
+  // flight (bit b: stage buffer b), as bit masks so that a stage index known
+  // only at run time does not put them in local memory
+  uint32_t par = 0u;
   bool xb_outst = false;  // a TMA copy of background rows is in flight
-  bool outst[2] = {false, false};
+  uint32_t outst = 0u;
   int tmo = 0;  // this thread saw a bounded wait give up
   const int npts_work = a.npts_dev ? *a.npts_dev : a.nwork;
   const double inv_n = 1.0 / (double)n;  // one FP64 division per kernel, not per variable and point
 
   auto wait_bar = [&](int i) {
-    if (!tc::mbar_wait(&mbar[i], par[i], TC_WAIT)) tmo = 1;
-    par[i] ^= 1u;
+    if (!tc::mbar_wait(&mbar[i], (par >> i) & 1u, TC_WAIT)) tmo = 1;
+    par ^= 1u << i;
   };
 
   for (;;) {
@@ -219,9 +222,9 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
     bool first = true;
     auto flush = [&](int nr) {
       const int buf = chunk & 1;
-      if (outst[buf]) {
+      if ((outst >> buf) & 1u) {
         wait_bar(buf);
-        outst[buf] = false;
+        outst &= ~(1u << buf);
       }
       tc::fence_after_sync();
       unsigned char* stg = sm + L::STG + buf * L::STG_SIZE;
@@ -273,15 +276,15 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
                        tc::smem_desc(sa + L::STG_BL + s * 256, 128, SBO), idesc_g, (first && s == 0) ? 0u : 1u);
         tc::mma_commit(&mbar[buf]);
       }
-      outst[buf] = true;
+      outst |= 1u << buf;
       first = false;
       chunk++;
     };
     const int Lp = sweep_search<TC_NT, TC_CH, TC_CPT>(a, ri, rj, logr, rz, ss, flush);
     for (int b = 0; b < 2; b++)
-      if (outst[b]) {
+      if ((outst >> b) & 1u) {
         wait_bar(b);
-        outst[b] = false;
+        outst &= ~(1u << b);
       }
     tc::fence_after_sync();
     if (__syncthreads_or(tmo)) {
@@ -910,7 +913,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
   }
   // drain (bounded), report, release tensor memory
   for (int b = 0; b < 2; b++)
-    if (outst[b]) wait_bar(b);
+    if ((outst >> b) & 1u) wait_bar(b);
   if (xb_outst) wait_bar(3);
   if (__syncthreads_or(tmo) && tid == 0 && a.err_flag) atomicExch(a.err_flag, 1);
   tc::fence_before_sync();
