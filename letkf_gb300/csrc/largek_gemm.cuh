@@ -118,8 +118,10 @@ __global__ void __launch_bounds__(LK_NT, 3) largek_gemm_kernel(LkGemmArgs a) {
   const uint32_t tacc = *tmem_holder;
   const uint32_t sbase = tc::smem_u32(sm);
   const uint32_t idesc = tc::idesc_tf32(128, 128);
-  uint32_t par[2] = {0u, 0u};
-  bool outst[2] = {false, false};
+  // phase parities and stages with MMAs in flight as bit masks (bit = stage
+  // buffer): the buffer index is known only at run time, and arrays indexed by
+  // it would live in local memory
+  uint32_t par = 0u, outst = 0u;
   int tmo = 0;
   const int r = tid & 127, h = tid >> 7;  // staging: row r, K half h (8 values)
 
@@ -170,10 +172,10 @@ __global__ void __launch_bounds__(LK_NT, 3) largek_gemm_kernel(LkGemmArgs a) {
       cb[j] = vb[j];
     }
     if (c + 1 < nk) load_stage(c + 1, va, vb);
-    if (outst[buf]) {
-      if (!tc::mbar_wait(&mbar[buf], par[buf], LK_WAIT)) tmo = 1;
-      par[buf] ^= 1u;
-      outst[buf] = false;
+    if ((outst >> buf) & 1u) {
+      if (!tc::mbar_wait(&mbar[buf], (par >> buf) & 1u, LK_WAIT)) tmo = 1;
+      par ^= 1u << buf;
+      outst &= ~(1u << buf);
     }
     tc::fence_after_sync();
     unsigned char* st = sm + buf * LK_STAGE;
@@ -205,13 +207,13 @@ __global__ void __launch_bounds__(LK_NT, 3) largek_gemm_kernel(LkGemmArgs a) {
       }
       tc::mma_commit(&mbar[buf]);
     }
-    outst[buf] = true;
+    outst |= 1u << buf;
   }
   for (int q = 0; q < 2; q++)
-    if (outst[q]) {
-      if (!tc::mbar_wait(&mbar[q], par[q], LK_WAIT)) tmo = 1;
-      par[q] ^= 1u;
-      outst[q] = false;
+    if ((outst >> q) & 1u) {
+      if (!tc::mbar_wait(&mbar[q], (par >> q) & 1u, LK_WAIT)) tmo = 1;
+      par ^= 1u << q;
+      outst &= ~(1u << q);
     }
   tc::fence_after_sync();
   const bool bad = __syncthreads_or(tmo) != 0;
