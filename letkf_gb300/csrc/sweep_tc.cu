@@ -451,12 +451,6 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
           *reinterpret_cast<uint4*>(sm + L::S_HI + off) = h;
           *reinterpret_cast<uint4*>(sm + L::S_LO + off) = l;
         }
-        __syncthreads();
-        // B = Y: rows 0..63 of S have the same K-major offsets in an 8 KB operand
-        for (int i = tid; i < 8192 / 16; i += TC_NT) {
-          reinterpret_cast<uint4*>(sm + L::B_HI)[i] = reinterpret_cast<const uint4*>(sm + L::S_HI)[i];
-          reinterpret_cast<uint4*>(sm + L::B_LO)[i] = reinterpret_cast<const uint4*>(sm + L::S_LO)[i];
-        }
         tc::fence_smem_async();
         tc::fence_before_sync();
         __syncthreads();
@@ -490,7 +484,9 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
           // T = Z Y  (rows 64..127 of S Y)
           if (tid == 0) {
             tc::fence_after_sync();
-            ns_mma(D0, sbase + L::S_HI, sbase + L::S_LO, sbase + L::B_HI, sbase + L::B_LO, idesc);
+            // B = Y read in place: rows 0..63 of S have the K-major offsets of a
+            // 64 x 64 operand with the same strides
+            ns_mma(D0, sbase + L::S_HI, sbase + L::S_LO, sbase + L::S_HI, sbase + L::S_LO, idesc);
             tc::mma_commit(&mbar[2]);
           }
           wait_bar(2);
@@ -567,17 +563,10 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
               *reinterpret_cast<uint4*>(sm + L::S_LO + off) = l;
             }
           }
+          // the new S is the next step's operands (generic stores -> async proxy)
+          tc::fence_smem_async();
           tc::fence_before_sync();
           __syncthreads();
-          if (!done) {
-            for (int i = tid; i < 8192 / 16; i += TC_NT) {
-              reinterpret_cast<uint4*>(sm + L::B_HI)[i] = reinterpret_cast<const uint4*>(sm + L::S_HI)[i];
-              reinterpret_cast<uint4*>(sm + L::B_LO)[i] = reinterpret_cast<const uint4*>(sm + L::S_LO)[i];
-            }
-            tc::fence_smem_async();
-            tc::fence_before_sync();
-            __syncthreads();
-          }
         }
         if (tmo) break;
         if (a.tc_polish) {
