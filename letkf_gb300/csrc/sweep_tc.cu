@@ -343,14 +343,17 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
       }
       tc::fence_before_sync();
       __syncthreads();
-      // symmetrise (pairs owned by one thread) and take the trace
-      for (int idx = tid; idx < 64 * 64; idx += TC_NT) {
-        const int i = idx >> 6, j = idx & 63;
-        if (i < j) {
-          const float v = 0.5f * (Gt[i * 64 + j] + Gt[j * 64 + i]);
-          Gt[i * 64 + j] = v;
-          Gt[j * 64 + i] = v;
-        }
+      // symmetrise (pairs owned by one thread) and take the trace.  The pairs
+      // are walked along diagonals, (i, i + d mod 64) for d = 1..32, so the 32
+      // lanes of a warp touch 32 distinct banks for both the element and its
+      // mirror (a row-by-row walk reads the mirror at a 64-float stride).
+      for (int t = tid; t < 32 * 64; t += TC_NT) {
+        const int d = 1 + (t >> 6), i = t & 63;
+        if (d == 32 && i >= 32) continue;
+        const int j = (i + d) & 63;
+        const float v = 0.5f * (Gt[i * 64 + j] + Gt[j * 64 + i]);
+        Gt[i * 64 + j] = v;
+        Gt[j * 64 + i] = v;
       }
       __syncthreads();
       float sums[3] = {tid < 64 ? Gt[tid * 64 + tid] : 0.f, p1, p3};
