@@ -49,7 +49,7 @@ struct TcLayout {
   static constexpr int S_LO = 16384;
   static constexpr int B_HI = 32768;      // B = Y or T: 64 x 64 bf16 (8 KB)
   static constexpr int B_LO = 40960;
-  static constexpr int GTMP = 32768;      // Gram in FP32, 64 x 64 row-major (over B)
+  static constexpr int GTMP = 32768;      // Gram in FP32, 64 x 64, swizzled rows (gsw; over B)
   static constexpr int WMAT = 32768;      // transform W in FP32, 64 x 64 row-major (over B)
   static constexpr int XS = 0;            // update staging, nv x 64 FP32 (over S)
   static constexpr int YF = 0;            // FP32 polish: Y (64 x 64), Z, T row-major
@@ -89,6 +89,25 @@ __device__ __forceinline__ float col_dot64(const float* M, const float* x, int c
     a1 = fmaf(M[(j + 1) * 64 + c], x[j + 1], a1);
     a2 = fmaf(M[(j + 2) * 64 + c], x[j + 2], a2);
     a3 = fmaf(M[(j + 3) * 64 + c], x[j + 3], a3);
+  }
+  return (a0 + a1) + (a2 + a3);
+}
+
+// The Gram in shared memory: 64 x 64 FP32, row r's 4-float column groups XOR-ed
+// by r & 7 (element (r, c) at r * 64 + (c ^ 4 (r & 7))).  Rows read or written
+// one per lane as float4, columns one per lane, the diagonal and the
+// symmetrising diagonal walk then all fall in distinct banks.
+__device__ __forceinline__ int gsw(int r, int c) { return r * 64 + (c ^ ((r & 7) << 2)); }
+
+// (M x)[c] for the swizzled Gram M (symmetric: column c read as row c)
+__device__ __forceinline__ float col_dot64_g(const float* M, const float* x, int c) {
+  float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll 4
+  for (int j = 0; j < 64; j += 4) {
+    a0 = fmaf(M[gsw(j, c)], x[j], a0);
+    a1 = fmaf(M[gsw(j + 1, c)], x[j + 1], a1);
+    a2 = fmaf(M[gsw(j + 2, c)], x[j + 2], a2);
+    a3 = fmaf(M[gsw(j + 3, c)], x[j + 3], a3);
   }
   return (a0 + a1) + (a2 + a3);
 }
@@ -319,10 +338,9 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
           float v0[16], v1[16];
           tc::tmem_ld16(D0 + lane_off + c0, v0);
           tc::tmem_ld16(D1 + lane_off + c0, v1);
-          float* dst = Gt + (r - 64) * 64 + c0;
 #pragma unroll
           for (int j = 0; j < 16; j += 4)
-            *reinterpret_cast<float4*>(dst + j) =
+            *reinterpret_cast<float4*>(Gt + gsw(r - 64, c0 + j)) =
                 make_float4(v0[j] + v1[j], v0[j + 1] + v1[j + 1], v0[j + 2] + v1[j + 2], v0[j + 3] + v1[j + 3]);
         }
       }
@@ -335,9 +353,16 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
           float v0[16], v1[16];
           tc::tmem_ld16(D0 + lane_off + c0, v0);
           tc::tmem_ld16(D1 + lane_off + c0, v1);
-          float* dst = Gt + r * 64 + c0;
 #pragma unroll
-          for (int j = 0; j < 16; j++) dst[j] += v0[j] + v1[j];
+          for (int j = 0; j < 16; j += 4) {
+            float4* dst = reinterpret_cast<float4*>(Gt + gsw(r, c0 + j));
+            float4 g = *dst;
+            g.x += v0[j] + v1[j];
+            g.y += v0[j + 1] + v1[j + 1];
+            g.z += v0[j + 2] + v1[j + 2];
+            g.w += v0[j + 3] + v1[j + 3];
+            *dst = g;
+          }
         }
         vb[r] = vbp[r] + vbp[r + 64];
       }
@@ -351,12 +376,12 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
         const int d = 1 + (t >> 6), i = t & 63;
         if (d == 32 && i >= 32) continue;
         const int j = (i + d) & 63;
-        const float v = 0.5f * (Gt[i * 64 + j] + Gt[j * 64 + i]);
-        Gt[i * 64 + j] = v;
-        Gt[j * 64 + i] = v;
+        const float v = 0.5f * (Gt[gsw(i, j)] + Gt[gsw(j, i)]);
+        Gt[gsw(i, j)] = v;
+        Gt[gsw(j, i)] = v;
       }
       __syncthreads();
-      float sums[3] = {tid < 64 ? Gt[tid * 64 + tid] : 0.f, p1, p3};
+      float sums[3] = {tid < 64 ? Gt[gsw(tid, tid)] : 0.f, p1, p3};
       block_sum_k<float, TC_NT, 3>(sums, red);
       const float trace = sums[0];
       p1 = sums[1];
@@ -364,7 +389,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
       if (!(cdiag > 0.f) || !((double)trace < 1.0e6 * (double)cdiag)) {
         deferred = true;  // needs the eigensolver with mtx_eigen's truncation
       } else {
-        if (tid < 64) Gt[tid * 64 + tid] += cdiag;
+        if (tid < 64) Gt[gsw(tid, tid)] += cdiag;
         __syncthreads();
         // keep the exact FP32 A in the Gram's second accumulator (lanes 0..63 of
         // columns 64..127); the Newton-Schulz products only use columns 0..63
@@ -373,7 +398,13 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
           for (int c0 = 0; c0 < 64; c0 += 16) {
             float v[16];
 #pragma unroll
-            for (int j = 0; j < 16; j++) v[j] = Gt[r * 64 + c0 + j];
+            for (int j = 0; j < 16; j += 4) {
+              const float4 g = *reinterpret_cast<const float4*>(Gt + gsw(r, c0 + j));
+              v[j] = g.x;
+              v[j + 1] = g.y;
+              v[j + 2] = g.z;
+              v[j + 3] = g.w;
+            }
             tc::tmem_st16(D1 + lane_off + c0, v);
           }
         }
@@ -384,13 +415,13 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
           float g0 = 0.f, g1 = 0.f, g2 = 0.f, g3 = 0.f;
 #pragma unroll 4
           for (int j = 0; j < 64; j += 4) {
-            g0 += fabsf(Gt[j * 64 + tid]);
-            g1 += fabsf(Gt[(j + 1) * 64 + tid]);
-            g2 += fabsf(Gt[(j + 2) * 64 + tid]);
-            g3 += fabsf(Gt[(j + 3) * 64 + tid]);
+            g0 += fabsf(Gt[gsw(j, tid)]);
+            g1 += fabsf(Gt[gsw(j + 1, tid)]);
+            g2 += fabsf(Gt[gsw(j + 2, tid)]);
+            g3 += fabsf(Gt[gsw(j + 3, tid)]);
           }
           gsum = (g0 + g1) + (g2 + g3);
-          vx[tid] = Gt[tid * 64 + tid] * (1.f + 0.25f * __sinf(1.7f * tid));
+          vx[tid] = Gt[gsw(tid, tid)] * (1.f + 0.25f * __sinf(1.7f * tid));
         }
         gsum = warp_max(gsum);
         __syncthreads();
@@ -406,8 +437,8 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
             float q0 = 0.f, q1 = 0.f, q2 = 0.f, q3 = 0.f;
 #pragma unroll 4
             for (int j = 0; j < 64; j += 4) {
-              const float x0 = Gt[j * 64 + tid], x1 = Gt[(j + 1) * 64 + tid];
-              const float x2 = Gt[(j + 2) * 64 + tid], x3 = Gt[(j + 3) * 64 + tid];
+              const float x0 = Gt[gsw(j, tid)], x1 = Gt[gsw(j + 1, tid)];
+              const float x2 = Gt[gsw(j + 2, tid)], x3 = Gt[gsw(j + 3, tid)];
               q0 = fmaf(x0, x0, q0);
               q1 = fmaf(x1, x1, q1);
               q2 = fmaf(x2, x2, q2);
@@ -420,7 +451,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
         for (int it = 0; it < (a.tc_scale_bound ? 0 : 8); it++) {
           float part = 0.f, xx = 0.f;
           if (tid < 64) {
-            const float acc = col_dot64(Gt, vx, tid);
+            const float acc = col_dot64_g(Gt, vx, tid);
             vy[tid] = acc;
             part = acc * acc;
             xx = vx[tid] * vx[tid];
@@ -440,8 +471,8 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
         for (int c0 = 0; c0 < 64; c0 += 8) {
           float v[8];
           if (r < 64) {
-            const float4 x0 = *reinterpret_cast<const float4*>(Gt + r * 64 + c0);
-            const float4 x1 = *reinterpret_cast<const float4*>(Gt + r * 64 + c0 + 4);
+            const float4 x0 = *reinterpret_cast<const float4*>(Gt + gsw(r, c0));
+            const float4 x1 = *reinterpret_cast<const float4*>(Gt + gsw(r, c0 + 4));
             v[0] = x0.x * inv_s; v[1] = x0.y * inv_s; v[2] = x0.z * inv_s; v[3] = x0.w * inv_s;
             v[4] = x1.x * inv_s; v[5] = x1.y * inv_s; v[6] = x1.z * inv_s; v[7] = x1.w * inv_s;
           } else {
