@@ -142,10 +142,15 @@ __device__ __forceinline__ double gram_finish(float* sm, GramAcc<NP>& acc) {
     for (int b = 0; b < C::TC; b++) A[(i0 + a) * NP + j0 + b] = acc.a[a][b];
   if (tid < NP) sm[S::B + tid] = acc.bacc;
   __syncthreads();
-  // mirror the lower triangle (i > j) onto the upper one
-  for (int idx = tid; idx < NP * NP; idx += C::NT) {
-    const int i = idx / NP, j = idx - i * NP;
-    if (i < j) A[idx] = A[j * NP + i];
+  // mirror the lower triangle onto the upper one, walking the pairs along
+  // diagonals (i, i + d mod NP), d = 1..NP/2, so a warp's lanes read and write
+  // distinct banks (a row walk reads the mirror at an NP-float stride)
+  for (int t = tid; t < (NP / 2) * NP; t += C::NT) {
+    const int d = 1 + t / NP, i = t - (d - 1) * NP;
+    if (d == NP / 2 && i >= NP / 2) continue;
+    const int j = (i + d) & (NP - 1);
+    const int lo = i < j ? i : j, hi = i < j ? j : i;
+    A[lo * NP + hi] = A[hi * NP + lo];
   }
   float tr = 0.f;
   for (int i = tid; i < NP; i += C::NT) tr += A[i * NP + i];
