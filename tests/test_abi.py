@@ -91,3 +91,31 @@ def test_server_without_gpu_is_an_error():
     with pytest.raises(LetkfError) as e:
         Server(nslots=2)
     assert e.value.status == LETKF_ERR_NOGPU
+
+
+def test_new_entry_points_check_arguments_before_the_device():
+    """letkf_sweep_run_host, letkf_sweep_deferred and letkf_search_l96_adaptive
+    reject invalid arguments with LETKF_ERR_ARG before any device call (so the
+    check holds on a machine without a GPU)."""
+    import ctypes as C
+
+    from letkf_gb300 import lib as L
+    from letkf_gb300.sweep import _L
+
+    lib = _L()
+    assert lib.letkf_sweep_run_host(None, None, None, 4, None) == L.LETKF_ERR_ARG
+    n = C.c_int(7)
+    assert lib.letkf_sweep_deferred(None, C.byref(n)) == L.LETKF_ERR_ARG
+    raw = L.lib()
+    ad = raw.letkf_search_l96_adaptive
+    for msw in (-1, 3):
+        assert ad(40, 1, 40, None, 0, None, 0, 3.0, 2.0, 1.0, msw, 1.0, 1.0, 20, None, None, None, None, None, None,
+                  None, None) == L.LETKF_ERR_ARG
+    # adaptive modes need the perturbations
+    cell = (C.c_int * 4)(1, 2, 3, 4)
+    pix = (C.c_int * 2)(1, 2)
+    assert ad(8, 1, 4, cell, 2, pix, 0, 3.0, 2.0, 1.0, 1, 1.0, 1.0, 20, None, None, None, None, None, None, None,
+              None) == L.LETKF_ERR_ARG
+    # slot out of range
+    assert ad(8, 1, 4, cell, 2, pix, 1, 3.0, 2.0, 1.0, 0, 1.0, 1.0, 20, None, None, None, None, None, None, None,
+              None) == L.LETKF_ERR_ARG
