@@ -6,7 +6,7 @@ Workload (per rank): the regional configuration -- 256 x 256 x 40 grid at
 clustered observations (0-2000 local obs per point).  One step = one full
 analysis sweep: local search, letkf_core and the update of every grid point
 (scale/letkf/letkf_tools.f90:38-476 with relax_beta = 1), mixed precision,
-one persistent CUDA launch.
+one persistent CUDA launch (and the Jacobi pass over any deferred points).
 
   value     device-resident throughput (points/s), CUDA events on the launch
             stream, inputs (4 GB background ensemble) larger than L2
