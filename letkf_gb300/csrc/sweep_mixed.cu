@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(MixedCfg<NP>::NT, MixedCfg<NP>::MINB) sweep_mi
     const int q = ctrl[0];
     if (q >= npts_work) break;
     const int pt = a.order[q];
-    const double ri = a.pri[pt], rj = a.prj[pt], rlev = a.prlev[pt], rz = a.prz ? a.prz[pt] : 0.0;
+    const double ri = a.pri[pt], rj = a.prj[pt], rz = a.prz ? a.prz[pt] : 0.0;
     const double logr = a.plogr[pt];
     const float rif = (float)ri, rjf = (float)rj, logrf = (float)logr, rzf = (float)rz;
     int imin = (int)floor(ri - a.P.dlon_zero), imax = (int)ceil(ri + a.P.dlon_zero);
