@@ -184,11 +184,13 @@ def cpu_oracle_setup(wl, obs):
     return so, np.ascontiguousarray(hdxf[perm], dtype=np.float64), np.ascontiguousarray(dep[perm])
 
 
-def cpu_oracle_run(wl, so, hd, dp, idx, nthreads, infl=1.0):
+def cpu_oracle_run(wl, so, hd, dp, idx, nthreads, infl=1.0, timed=False):
+    """The oracle's SCALE grid loop on the points idx.  timed=True runs the
+    -O3 build the CPU baseline is timed with; the parity build otherwise."""
     i, j, p = wl.points(idx)
     xb = wl.background_numpy(idx).astype(np.float64)
     t = time.perf_counter()
-    xa, inf, nl = so.sweep(hd, dp, xb, i, j, p, np.full(idx.size, infl), nthreads=nthreads)
+    xa, inf, nl = so.sweep(hd, dp, xb, i, j, p, np.full(idx.size, infl), nthreads=nthreads, timed=timed)
     return time.perf_counter() - t, xb, xa, inf, nl
 
 
@@ -209,12 +211,12 @@ def run_reference(args, rank, world):
     nthreads = os.cpu_count() or 1
     # size each step's sample from a probe so that a step takes about 1 s
     probe = sample_points(wl, 64, seed=99)
-    dt, *_ = cpu_oracle_run(wl, so, hd, dp, probe, nthreads)
+    dt, *_ = cpu_oracle_run(wl, so, hd, dp, probe, nthreads, timed=True)
     per_step = int(max(64, min(wl.npts, 64 * 1.0 / max(dt, 1e-6))))
     times, npts_done = [], 0
     for s in range(args.warmup + args.steps):
         idx = sample_points(wl, per_step, seed=1000 + s)
-        dt, *_ = cpu_oracle_run(wl, so, hd, dp, idx, nthreads)
+        dt, *_ = cpu_oracle_run(wl, so, hd, dp, idx, nthreads, timed=True)
         if s >= args.warmup:
             times.append(dt)
             npts_done += idx.size
@@ -223,18 +225,25 @@ def run_reference(args, rank, world):
     line = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": config_block(args, wl),
-            "cpu_baseline": {"value": val, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "config": config_block(args, wl, form=REF_FORM),
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": nthreads, "kind": "port", "build": CPU_BUILD,
                              "sample": f"{per_step} random grid points per step of the {wl.npts}-point sweep"},
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     return line
 
 
-def config_block(args, wl):
+GPU_FORM = ("mixed (FP32 ensemble, Gram and transform; FP64 member sums and mean-increment accumulation, "
+            "analysis mean carried as an FP32 hi + lo pair)")
+REF_FORM = ("FP64 plain form: the oracle's restatement of letkf_core, EISPACK rs and the SCALE obs_local, "
+            "OpenMP over points (scale/letkf/letkf_tools.f90:175)")
+CPU_BUILD = "gcc -O3 -ffp-contract=fast -fopenmp (oracle/_build/liboracle_timed.so; no -march=native)"
+
+
+def config_block(args, wl, form=GPU_FORM):
     return {"workload": f"regional {args.nlon}x{args.nlat}x{args.nlev} (3 km), {args.nv} vars, k={args.ne}, "
                         f"{args.nobs} clustered obs, sigma_h={wl.sigma_obs:.0f} m, sigma_v={wl.sigma_obsv} ln p",
             "points_per_sweep": wl.npts, "ensemble": args.ne, "variables": args.nv, "observations": args.nobs,
-            "local_obs": "0-2000 per point", "form": "mixed (FP32 ensemble, Gram and transform; FP64 member sums and mean-increment accumulation, analysis mean carried as an FP32 hi + lo pair)",
+            "local_obs": "0-2000 per point", "form": form,
             "l2": "inputs larger than L2 (background ensemble %.1f GB)" % (wl.npts * args.nv * args.ne * 4 / 1e9),
             "parallelism": f"dp{args.gpus} (independent domains per GPU)"}
 
@@ -485,6 +494,38 @@ def run_largek(args, dev):
                                      "points": int(sub.size), "target": 1e-4}}
 
 
+def check_lists(sw, so, wl, idx, cap, stream, nthreads, chunk=16384):
+    """The fused sweep's accepted observation lists (selection probe) against
+    the oracle's obs_local on the sample points idx: every index in order
+    must be equal; the largest relative rloc difference (FP32 on the device)
+    is reported."""
+    perm = so_perm(wl)
+    entries, worst, equal = 0, 0.0, True
+    for c0 in range(0, idx.size, chunk):
+        pts = idx[c0:c0 + chunk].astype(np.int32)
+        sw.set_probe(pts, cap)
+        sw.run(stream.cuda_stream)
+        cnt, obs, rl = sw.probe()
+        i, j, p = wl.points(pts)
+        ocnt, oidx, orl = so.obs_local_batch(i, j, p, cap=cap, nthreads=nthreads)
+        equal &= bool((cnt == ocnt).all())
+        ok = np.arange(cap)[None, :] < np.minimum(ocnt, cap)[:, None]
+        mapped = np.where(ok, perm[np.maximum(oidx, 0)], -1)
+        equal &= bool((np.where(ok, obs, -1) == mapped).all())
+        if ok.any():
+            worst = max(worst, float(np.max(np.abs(rl[ok] - orl[ok]) / orl[ok])))
+        entries += int(ok.sum())
+    sw.set_probe(np.zeros(0, np.int32), 1)
+    return {"equal": equal, "points": int(idx.size), "entries": entries, "rloc_max_rel": worst}
+
+
+def so_perm(wl):
+    from oracle import oracle as O
+
+    perm, _ = O.scale_sort_obs(wl.nlon, wl.nlat, wl.ri, wl.rj)
+    return perm
+
+
 # ----------------------------------------------------------------- GPU arm
 def run_gpu(args, rank, world, dist):
     import torch
@@ -629,8 +670,11 @@ def run_gpu(args, rank, world, dist):
     dtp, *_ = cpu_oracle_run(wl, so, hd, dp, probe, nthreads)
     nsample = int(max(256, min(131072, 64 * args.cpu_seconds / max(dtp, 1e-6))))
     idx = sample_points(wl, nsample, seed=7)
-    dtc, xb_s, xa_ref, inf_ref, nl_ref = cpu_oracle_run(wl, so, hd, dp, idx, nthreads)
+    # the reference answer from the parity build, the CPU figure from the -O3 build
+    dtc_parity, xb_s, xa_ref, inf_ref, nl_ref = cpu_oracle_run(wl, so, hd, dp, idx, nthreads)
+    dtc, *_ = cpu_oracle_run(wl, so, hd, dp, idx, nthreads, timed=True)
     out["cpu_baseline"] = {"value": idx.size / dtc, "unit": UNIT, "cores": nthreads, "kind": "port",
+                           "build": CPU_BUILD, "parity_build_value": idx.size / dtc_parity,
                            "sample": f"{idx.size} random grid points of the {wl.npts}-point sweep "
                                      f"({dtc:.1f} s, OpenMP dynamic over points)"}
     xg = xa[:, idx, :].astype(np.float64)
@@ -641,9 +685,11 @@ def run_gpu(args, rank, world, dist):
     sa = lambda x: np.sqrt((pert(x) ** 2).sum(-1) / (args.ne - 1))
     es = float(np.sqrt(np.mean((sa(xg) - sa(xa_ref)) ** 2)) / spread)
     dgi = sw.diagnostics()
+    lists = check_lists(sw, so, wl, idx, int(nl_ref.max()) + 1, stream, nthreads)
     out["error_vs_fp64_oracle"] = {"analysis_mean_rms_over_spread": em, "perturbation_rms_over_spread": ep,
                                    "analysis_spread_rms_over_spread": es,
                                    "nobsl_bit_exact": bool((dgi["nobsl"][idx] == nl_ref).all()),
+                                   "lists_bit_exact": lists["equal"], "lists_checked": lists,
                                    "infl_max_rel": float(np.max(np.abs(dgi["infl"][idx] - inf_ref) / inf_ref)),
                                    "sample_points": int(idx.size), "target": 1e-4}
     # ---- FP64 plain form on a strided subset ----

@@ -162,6 +162,26 @@ int letkf_search_scale(int nlon, int nlat, const int* nobsgrd /* [(nlon+1)*nlat]
                        const double* var_local_row, const double* params, const int64_t* offs,
                        int* nobsl, int* idx, double* rloc, double* rdiag, void* stream);
 
+/* SCALE search with the MAX_NOBS_PER_GRID limit (scale/letkf/letkf_tools.f90:
+ * 853-1178 with MAX_NOBS_PER_GRID > 0; allocation :901-906, selection
+ * :1063-1128, emission :1141-1156).  Same arguments as letkf_search_scale plus
+ * each observation's element uid ouid[nobs] (1..nid, the reference's
+ * uid_obs(elm)) and type otyp[nobs] (1..nobtype), nid and the limit M
+ * (1..LETKF_MAX_NOBS_PER_GRID_LIMIT).  Per (uid, type) group the M accepted
+ * observations of smallest rdiag = err^2 / rloc are kept (ties: the earlier
+ * candidate), and the list is emitted grouped by type, then uid, each group
+ * in the reference's slot order.  Count pass (idx == NULL) and fill pass as
+ * for letkf_search_scale; each pass allocates stream-ordered scratch for the
+ * unlimited lists and returns once its results are on the device. */
+#define LETKF_MAX_NOBS_PER_GRID_LIMIT 256
+int letkf_search_scale_limited(int nlon, int nlat, const int* nobsgrd, int nobs, const double* ori,
+                               const double* orj, const double* olev, const double* odat, const double* oerr,
+                               const int* ocls, const int* ovarloc, const int* ouid, const int* otyp, int nid,
+                               int max_nobs_per_grid, int npts, const double* pri, const double* prj,
+                               const double* prlev, const double* prz, const double* var_local_row,
+                               const double* params, const int64_t* offs, int* nobsl, int* idx, double* rloc,
+                               double* rdiag, void* stream);
+
 /* GFS lat/lon search (gfs/letkf/letkf_tools.f90:686-955): the SPEEDY box walk
  * over the same bucket-sorted observations with the GFS tests:
  * dlat_zero = max(dist_zero, dist_zero_rain) / pi / re * 180 and
@@ -194,6 +214,20 @@ int letkf_search_speedy(int nlon, int nlat, const double* lon, const double* lat
                         const double* pdlon_zero, const int* pilev, const double* plogpfm,
                         const double* var_local_row, const double* params, const int64_t* offs,
                         int* nobsl, int* idx, double* rloc, double* rdiag, void* stream);
+
+/* SPEEDY / GFS observation bucket sort on DEVICE buffers (speedy/letkf/
+ * letkf_obs.f90:243-313): observations are ordered by latitude band j
+ * (lat(j) <= y < lat(j+1), j = 1..nlat-1), then longitude cell i (lon(i) <=
+ * x < lon(i+1), the last cell up to 360), input order inside a cell.  qc
+ * [nobs] may be NULL; with it only qc == 1 observations are kept (the
+ * selection of set_letkf_obs).  perm[nobs] receives the input index of each
+ * kept observation in sorted order, *nsorted (host) their count, and
+ * nobsgrd[nlat * nlon] (i fastest) the cumulative counts through each cell
+ * (row nlat 0, as the reference leaves it).  Observations outside every
+ * band or cell are dropped.  Returns when the results are on the device. */
+int letkf_sort_obs_latlon(int nlon, int nlat, const double* lon, const double* lat, int nobs,
+                          const double* olon, const double* olat, const int* qc, int* perm, int* nsorted,
+                          int* nobsgrd, void* stream);
 
 /* Observation-space perturbations and departures on DEVICE buffers
  * (speedy/letkf/letkf_obs.f90:157-174; lorenz96/letkf/letkf.f90:196-212):
@@ -363,6 +397,13 @@ int letkf_l96_obs_cell(int nx, int ny, const double* h, int* cell, void* stream)
 #define LETKF_OPT_NS_COND 13       /* v > 0 (default 5): Newton-Schulz only where the spectrum bound s / c < 10^v, other
                                       points go to the Jacobi pass; 0: no bound.  Either way a point whose transform is
                                       not certified (no convergence, a large anchored residual) goes to the Jacobi pass */
+#define LETKF_OPT_MAX_NOBS_PER_GRID 14 /* M > 0: MAX_NOBS_PER_GRID selection (scale/letkf/letkf_tools.f90:1041-1156)
+                                      with the groups of letkf_sweep_set_obs_groups; the run then searches each piece
+                                      of the processing order first (letkf_search_scale_limited) and analyses it from
+                                      the lists (no CUDA graph); 0 (default): no limit */
+#define LETKF_OPT_FAULT_WAIT 15    /* failure injection, v > 0: the next mixed-form runs on the tensor-core sweep
+                                      wait on a barrier that nothing arrives at and give up after v polls, so the
+                                      run reports LETKF_ERR_TIMEOUT and analyses nothing; 0 (default): off */
 
 typedef struct letkf_sweep_desc {
   int ne;           /* ensemble size (MEMBER) */
@@ -429,6 +470,21 @@ int letkf_sweep_get_diagnostics(letkf_sweep_t h, double* infl, int* nobsl, int* 
 int letkf_sweep_sorted_obs(letkf_sweep_t h, int* nobsgrd);
 /* device pointers of the resident buffers (for callers that stage data themselves) */
 int letkf_sweep_device_buffers(letkf_sweep_t h, void** xb, void** xa, double** infl, int** nobsl);
+/* Observation groups of the MAX_NOBS_PER_GRID limit, after set_obs (input
+ * order, host arrays [nobs]): element uid 1..nid and type 1..ntyp (the
+ * reference's uid_obs(elm) and obs%typ). */
+int letkf_sweep_set_obs_groups(letkf_sweep_t h, const int* uid, const int* typ, int nid, int ntyp);
+/* Selection probe (checks the fused search of the mixed-form sweeps): for
+ * the npts_probe grid points points[] (host, point indices) the next runs
+ * also record what their search accepted, in the order it enters the Gram:
+ * up to cap entries per point.  npts_probe = 0 switches the probe off.  The
+ * probe adds stores only; the analysis is unchanged. */
+int letkf_sweep_set_probe(letkf_sweep_t h, int npts_probe, const int* points, int cap);
+/* after a run: count[npts_probe] accepted observations per probed point (may
+ * exceed cap), obs[npts_probe * cap] their indices in the observation input
+ * order of letkf_sweep_set_obs, rloc[npts_probe * cap] the FP32 localisation
+ * weights (either array may be NULL); host arrays */
+int letkf_sweep_get_probe(letkf_sweep_t h, int* count, int* obs, float* rloc);
 /* upper bound of the device bytes a handle with this descriptor and nobs
  * observations holds, including the staging of set_obs and run */
 int letkf_sweep_footprint(const letkf_sweep_desc* desc, int nobs, size_t* bytes);
@@ -502,7 +558,9 @@ typedef struct letkf_server_s* letkf_server_t;
 int letkf_server_create(letkf_server_t* server, const letkf_server_desc* desc);
 /* copies the descriptor (not the arrays) and queues the job; *job_id >= 0 */
 int letkf_server_submit(letkf_server_t server, const letkf_job_desc* job, int64_t* job_id);
-/* waits up to timeout_s (< 0: no limit) for the job; LETKF_PENDING on timeout */
+/* waits up to timeout_s (< 0: no limit) for the job; LETKF_PENDING on timeout.
+ * Once it has returned a finished job's result the job's record is released:
+ * a later wait on that id returns LETKF_ERR_ARG. */
 int letkf_server_wait(letkf_server_t server, int64_t job_id, double timeout_s, letkf_job_result* result);
 int letkf_server_stats_get(letkf_server_t server, letkf_server_stats* stats);
 /* finishes every queued job, then releases the device state */
@@ -518,7 +576,8 @@ int letkf_exclusive_scan(int n, const int* counts, int64_t* offs, void* stream);
  * array inside the library instead of an allocation.
  *   - n <= LETKF_SCAN_STATIC_MAX_N, else LETKF_ERR_CAPACITY;
  *   - the first call on a device looks up that array's device address, so
- *     make it before any stream capture;
+ *     make it before any stream capture; the address is kept for the life of
+ *     the process and is not valid after cudaDeviceReset of that device;
  *   - every call shares the array: calls that overlap on the GPU (other
  *     streams, other threads) race, so serialise them. */
 #define LETKF_SCAN_STATIC_MAX_N (16 * 1024 * 1024)

@@ -323,6 +323,54 @@ def search_scale(nlon, nlat, nobsgrd, obs, pts, params, var_local_row=None, stre
     return offs, idx[:total], rloc[:total], rdiag[:total]
 
 
+def search_scale_limited(nlon, nlat, nobsgrd, obs, pts, params, max_nobs_per_grid, nid, var_local_row=None,
+                         stream=None):
+    """SCALE search with the MAX_NOBS_PER_GRID limit (letkf_search_scale_limited).
+    obs as for search_scale plus uid, typ (int32, 1-based element uid and obs
+    type of each sorted observation); nid is the number of element uids.
+    Returns (offs, idx, rloc, rdiag) as search_scale."""
+    import torch
+
+    dev = obs["ri"].device
+    npts = pts["ri"].numel()
+    nobs = obs["ri"].numel()
+    P = torch.tensor([float(params[k]) for k in SCALE_PARAM_ORDER] + [0.0], dtype=torch.float64)
+    vl = None if var_local_row is None else torch.as_tensor(var_local_row, dtype=torch.float64, device=dev)
+    nobsl = torch.empty(npts, dtype=torch.int32, device=dev)
+    args = (nlon, nlat, _dptr(nobsgrd), nobs, _dptr(obs["ri"]), _dptr(obs["rj"]), _dptr(obs["lev"]),
+            _dptr(obs["dat"]), _dptr(obs["err"]), _dptr(obs["cls"]), _dptr(obs["varloc"]), _dptr(obs["uid"]),
+            _dptr(obs["typ"]), int(nid), int(max_nobs_per_grid), npts, _dptr(pts["ri"]), _dptr(pts["rj"]),
+            _dptr(pts["rlev"]), _dptr(pts.get("rz")), _dptr(vl), C.c_void_p(P.data_ptr()))
+    check(lib().letkf_search_scale_limited(*args, None, _dptr(nobsl), None, None, None, _stream(stream)),
+          "search_scale_limited")
+    offs = exclusive_scan(nobsl, stream)
+    total = int(offs[-1].item())
+    idx = torch.empty(max(total, 1), dtype=torch.int32, device=dev)
+    rloc = torch.empty(max(total, 1), dtype=torch.float64, device=dev)
+    rdiag = torch.empty(max(total, 1), dtype=torch.float64, device=dev)
+    check(lib().letkf_search_scale_limited(*args, _dptr(offs), _dptr(nobsl), _dptr(idx), _dptr(rloc),
+                                           _dptr(rdiag), _stream(stream)), "search_scale_limited")
+    return offs, idx[:total], rloc[:total], rdiag[:total]
+
+
+def sort_obs_latlon(lon, lat, olon, olat, qc=None, stream=None):
+    """SPEEDY / GFS bucket sort on the device (letkf_sort_obs_latlon): lon
+    [nlon], lat [nlat], olon, olat [nobs] float64 tensors, qc optional int32
+    (only qc == 1 kept).  Returns (perm int32 [nsorted]: input index of each
+    kept observation in sorted order, nobsgrd int32 [nlat, nlon])."""
+    import torch
+
+    dev = olon.device
+    nlon, nlat, nobs = lon.numel(), lat.numel(), olon.numel()
+    perm = torch.empty(max(nobs, 1), dtype=torch.int32, device=dev)
+    grd = torch.empty((nlat, nlon), dtype=torch.int32, device=dev)
+    ns = C.c_int(0)
+    check(lib().letkf_sort_obs_latlon(nlon, nlat, _dptr(lon), _dptr(lat), nobs, _dptr(olon), _dptr(olat),
+                                      _dptr(qc), _dptr(perm), C.byref(ns), _dptr(grd), _stream(stream)),
+          "sort_obs_latlon")
+    return perm[:ns.value], grd
+
+
 def search_speedy(grid, obs, pts, params, var_local_row, stream=None):
     """SPEEDY lat/lon local search on device tensors.
     grid: dict lon, lat (float64), nobsgrd (int32 [nlat, nlon]).

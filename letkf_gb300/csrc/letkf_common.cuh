@@ -26,6 +26,13 @@ inline cudaError_t set_smem_once(K kern, size_t bytes, std::atomic<uint32_t>& do
   return e;
 }
 
+// x*x + y*y with each operation rounded on its own (no FMA contraction), as
+// the reference computes it without FMA and the oracle does with
+// -ffp-contract=off: a distance exactly at a cut-off then tests the same way
+__device__ __forceinline__ double sumsq_rn(double x, double y) {
+  return __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y));
+}
+
 constexpr double kSigmaB = 0.04;  // common/common_letkf.f90:75 error stdev of parm_infl
 
 // Newton-Schulz map of one eigenvalue of ZY, x (3 - x)^2 / 4

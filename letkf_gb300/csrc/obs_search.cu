@@ -53,7 +53,7 @@ __global__ void search_scale_kernel(int nlon, int nlat, const int* __restrict__ 
         const int vl = ovarloc[ob];
         if (var_local && var_local[vl] < 2.2250738585072014e-308) continue;
         const double rdx = (ri - ori[ob]) * P.dx, rdy = (rj - orj[ob]) * P.dy;
-        double nd_h = sqrt(rdx * rdx + rdy * rdy), nd_v;
+        double nd_h = sqrt(sumsq_rn(rdx, rdy)), nd_v;
         const int cls = ocls[ob];
         if (cls == 1) {
           nd_h = nd_h / P.sigma_obs;
@@ -74,7 +74,7 @@ __global__ void search_scale_kernel(int nlon, int nlat, const int* __restrict__ 
           nd_h = nd_h / P.sigma_obs;
           nd_v = fabs(log(olev[ob]) - logr) / P.sigma_obsv;
         }
-        const double ndist = nd_h * nd_h + nd_v * nd_v;
+        const double ndist = sumsq_rn(nd_h, nd_v);
         if (ndist > dzf2) continue;
         if (idx) {
           double nrloc = exp(-0.5 * ndist);
@@ -95,7 +95,7 @@ __device__ __forceinline__ double distll(double alon, double alat, double blon, 
   const double pi = 3.1415926535, re = 6371.3e3, r180 = 1.0 / 180.0;
   const double lon1 = alon * pi * r180, lon2 = blon * pi * r180;
   const double lat1 = alat * pi * r180, lat2 = blat * pi * r180;
-  double cosd = sin(lat1) * sin(lat2) + cos(lat1) * cos(lat2) * cos(lon2 - lon1);
+  double cosd = __dadd_rn(__dmul_rn(sin(lat1), sin(lat2)), __dmul_rn(__dmul_rn(cos(lat1), cos(lat2)), cos(lon2 - lon1)));
   cosd = fmin(1.0, cosd);
   cosd = fmax(-1.0, cosd);
   return acos(cosd) * re;
@@ -412,15 +412,29 @@ __global__ void scan_blocks_kernel(int n, const int* __restrict__ in, int64_t* o
   if (threadIdx.x == SCAN_BS - 1) bsum[blockIdx.x] = s[threadIdx.x];
 }
 
+// exclusive scan of the nb block sums by one block of SCAN_BS threads: each
+// thread sums a contiguous chunk of ceil(nb / SCAN_BS) sums, the chunk totals
+// are scanned in shared memory, and each thread rewrites its chunk
 __global__ void scan_sums_kernel(int nb, int64_t* bsum) {
-  // single thread: nb is small (n / 1024)
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    int64_t run = 0;
-    for (int b = 0; b < nb; b++) {
-      int64_t v = bsum[b];
-      bsum[b] = run;
-      run += v;
-    }
+  __shared__ int64_t s[SCAN_BS];
+  const int t = threadIdx.x;
+  const int per = (nb + SCAN_BS - 1) / SCAN_BS;
+  const int b0 = min(nb, t * per), b1 = min(nb, b0 + per);
+  int64_t tot = 0;
+  for (int b = b0; b < b1; b++) tot += bsum[b];
+  s[t] = tot;
+  __syncthreads();
+  for (int o = 1; o < SCAN_BS; o <<= 1) {
+    const int64_t v = t >= o ? s[t - o] : 0;
+    __syncthreads();
+    s[t] += v;
+    __syncthreads();
+  }
+  int64_t run = s[t] - tot;
+  for (int b = b0; b < b1; b++) {
+    const int64_t v = bsum[b];
+    bsum[b] = run;
+    run += v;
   }
 }
 
@@ -437,7 +451,7 @@ int launch_exclusive_scan(int n, const int* counts, int64_t* offs, int64_t* scra
   }
   const int nb = (n + SCAN_BS - 1) / SCAN_BS;
   scan_blocks_kernel<<<nb, SCAN_BS, 0, stream>>>(n, counts, offs, scratch);
-  scan_sums_kernel<<<1, 32, 0, stream>>>(nb, scratch);
+  scan_sums_kernel<<<1, SCAN_BS, 0, stream>>>(nb, scratch);
   scan_add_kernel<<<nb, SCAN_BS, 0, stream>>>(n, offs, scratch);
   note_launch();
   note_launch();

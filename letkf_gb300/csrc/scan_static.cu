@@ -26,7 +26,10 @@ static int64_t* g_scan_ptr[kMaxDevices] = {nullptr};
 
 // Device address of g_scan_block_sums on the current device.  The array's
 // name in host code only stands for the symbol; the address that kernels may
-// use has to be asked for once per device, with that device current.
+// use has to be asked for once per device, with that device current.  The
+// address belongs to the device's primary context: it is cached per device for
+// the life of the process, so it is not valid across cudaDeviceReset (a
+// process that resets a device must not call this entry point afterwards).
 static int scan_scratch_address(int64_t** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {

@@ -398,10 +398,12 @@ static void worker_main(letkf_server_s* S) {
       S->running++;
     }
     if (id < 0 && victims.empty()) break;  // stopping and nothing queued
+    letkf_job_desc jd{};
+    if (id >= 0) jd = S->jobs[id].d;  // copied under the lock: submits insert into the map meanwhile
     lk.unlock();
     for (Domain* v : victims) release_domain(S, v);
     int rc = LETKF_OK;
-    if (id >= 0) rc = run_job(S, S->jobs[id].d, dm, s);
+    if (id >= 0) rc = run_job(S, jd, dm, s);
     lk.lock();
     if (id < 0) continue;
     JobRec& jr = S->jobs[id];
@@ -505,7 +507,12 @@ int letkf_server_wait(letkf_server_t S, int64_t id, double timeout_s, letkf_job_
   if (timeout_s < 0.0) S->cv_done.wait(lk, done);
   else S->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), done);
   if (res) *res = it->second.r;
-  return it->second.done ? it->second.r.status : LETKF_PENDING;
+  if (!it->second.done) return LETKF_PENDING;
+  // the result has been handed out: release the record, so a long-lived
+  // server keeps only unfinished and unclaimed jobs
+  const int st = it->second.r.status;
+  S->jobs.erase(it);
+  return st;
 }
 
 int letkf_server_stats_get(letkf_server_t S, letkf_server_stats* st) {

@@ -37,6 +37,13 @@ int launch_core_f64(int, int, const int64_t*, const double*, const double*, cons
 int launch_update_f64_range(int ne, int npts_total, int p0, int cnt, int nv, const double* xb, const double* trans,
                             const double* transm, double* xa, cudaStream_t stream);
 int launch_gather_rows(int, int64_t, const int*, const void*, const void*, int, void*, void*, cudaStream_t);
+int launch_limit_select(int, const int64_t*, const int*, const double*, const double*, const int*, int,
+                        const int64_t*, int*, int*, double*, double*, cudaStream_t);
+int launch_obs_group(int, const int*, const int*, int, const int*, int*, cudaStream_t);
+int unlimited_lists(int, int, const int*, int, const double*, const double*, const double*, const double*,
+                    const double*, const int*, const int*, int, const double*, const double*, const double*,
+                    const double*, const double*, const double*, cudaStream_t, int64_t**, int**, double**, double**);
+void free_unlimited(cudaStream_t, int64_t*, int*, double*, double*);
 
 }  // namespace letkf
 
@@ -92,6 +99,57 @@ __global__ void obs_grd_kernel(int nlon, int nlat, const int64_t* __restrict__ s
   G[t] = (int)start[j * nlon + i];       // cumulative count before cell (i+1, j+1) == through cell (i, j+1)
 }
 
+// SPEEDY / GFS cell of an observation (speedy/letkf/letkf_obs.f90:243-313):
+// band j with lat(j) <= y < lat(j+1) (j = 1..nlat-1), cell i with lon(i) <= x <
+// lon(i+1) (i < nlon) or lon(nlon) <= x < 360 (i = nlon); key (j-1) nlon +
+// (i-1), or -1 for an observation in no band or cell, or with qc /= 1
+__global__ void latlon_cell_kernel(int nobs, int nlon, int nlat, const double* __restrict__ lon,
+                                   const double* __restrict__ lat, const double* __restrict__ olon,
+                                   const double* __restrict__ olat, const int* __restrict__ qc, int* cell,
+                                   int* counts) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nobs) return;
+  const double x = olon[n], y = olat[n];
+  int c = -1;
+  if ((!qc || qc[n] == 1) && y >= lat[0] && y < lat[nlat - 1]) {
+    int lo = 0, hi = nlat - 2;  // the band j - 1 = lo with lat[lo] <= y < lat[lo + 1]
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (lat[mid] <= y) lo = mid;
+      else hi = mid - 1;
+    }
+    const int jb = lo;
+    if (x >= lon[0] && x < 360.0) {
+      int a = 0, b = nlon - 1;  // the last cell runs to 360
+      while (a < b) {
+        const int mid = (a + b + 1) >> 1;
+        if (lon[mid] <= x) a = mid;
+        else b = mid - 1;
+      }
+      c = jb * nlon + a;
+    }
+  }
+  cell[n] = c;
+  if (c >= 0) atomicAdd(&counts[c], 1);
+}
+
+__global__ void latlon_scatter_kernel(int nobs, const int* __restrict__ cell, const int64_t* __restrict__ start,
+                                      int* cursor, int* perm) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nobs) return;
+  const int c = cell[n];
+  if (c < 0) return;
+  perm[(int)start[c] + atomicAdd(&cursor[c], 1)] = n;
+}
+
+// nobsgrd(i, j): cumulative count through cell (i, j) for the bands j < nlat;
+// row nlat is not a band (the reference leaves it 0)
+__global__ void latlon_grd_kernel(int nlon, int nlat, const int64_t* __restrict__ start, int* G) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nlon * nlat) return;
+  G[t] = t < nlon * (nlat - 1) ? (int)start[t + 1] : 0;
+}
+
 template <typename T>
 __global__ void permute_kernel(int n, int width, const int* __restrict__ perm, const T* __restrict__ src, T* dst) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -114,6 +172,20 @@ __global__ void f64_to_f32_kernel(int64_t n, const double* __restrict__ a, float
   if (t < n) b[t] = (float)a[t];
 }
 
+// coordinates of the points at processing positions order[0..n-1]
+__global__ void gather_points_kernel(int n, const int* __restrict__ order, const double* __restrict__ ri,
+                                     const double* __restrict__ rj, const double* __restrict__ rlev,
+                                     const double* __restrict__ rz, double* ori, double* orj, double* orlev,
+                                     double* orz) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int p = order[t];
+  ori[t] = ri[p];
+  orj[t] = rj[p];
+  orlev[t] = rlev[p];
+  orz[t] = rz[p];
+}
+
 }  // namespace letkf
 
 using namespace letkf;
@@ -134,7 +206,16 @@ struct letkf_sweep_s {
   int* meta = nullptr;
   float* ens32 = nullptr;
   double* ens64 = nullptr;
+  int* operm = nullptr;  // sorted position -> input index of set_obs
+  int* ogrp = nullptr;   // MAX_NOBS_PER_GRID group key per sorted observation (set_obs_groups)
+  bool groups_set = false;
   size_t obs_cap = 0;  // observations the resident buffers hold (kept across set_obs calls)
+  int max_nobs = 0;    // MAX_NOBS_PER_GRID (0: no limit)
+  uint32_t fault_wait = 0;
+  // selection probe
+  int nprobe = 0, probe_cap = 0;
+  int *probe_slot = nullptr, *probe_idx = nullptr, *probe_count = nullptr;
+  float* probe_rloc = nullptr;
   // ensemble
   void *xb = nullptr, *xa = nullptr;
   double* infl = nullptr;
@@ -249,7 +330,8 @@ int letkf_sweep_destroy(letkf_sweep_t h) {
   void* ptrs[] = {h->pri,  h->prj,   h->prlev, h->prz,   h->plogr,   h->order, h->ori,     h->orj,    h->olev,
                   h->odat, h->oerr,  h->odep,  h->ocls,  h->ovarloc, h->G,     h->var_local, h->obsF,
                   h->obsA, h->meta,  h->ens32, h->ens64, h->xb,    h->xa,      h->infl,   h->status,
-                  h->nobsl, h->sweeps, h->counter, h->defer_list, h->defer_count, h->defer_total, h->err_flag};
+                  h->nobsl, h->sweeps, h->counter, h->defer_list, h->defer_count, h->defer_total, h->err_flag,
+                  h->operm, h->ogrp, h->probe_slot, h->probe_idx, h->probe_count, h->probe_rloc};
   if (h->stream) {
     for (void* p : ptrs) dfree(p, h->stream);
     cudaStreamSynchronize(h->stream);
@@ -324,10 +406,10 @@ int letkf_sweep_set_obs(letkf_sweep_t h, int nobs, const double* ri, const doubl
   // (and the captured run graph stays valid)
   if (n > h->obs_cap || h->ori == nullptr) {
     void* old[] = {h->ori, h->orj, h->olev, h->odat, h->oerr, h->odep, h->ocls, h->ovarloc,
-                   h->obsF, h->obsA, h->meta, h->ens32, h->ens64};
+                   h->obsF, h->obsA, h->meta, h->ens32, h->ens64, h->operm, h->ogrp};
     for (void* p : old) dfree(p, s);
     h->ori = h->orj = h->olev = h->odat = h->oerr = h->odep = nullptr;
-    h->ocls = h->ovarloc = h->meta = nullptr;
+    h->ocls = h->ovarloc = h->meta = h->operm = h->ogrp = nullptr;
     h->obsF = h->obsA = nullptr;
     h->ens32 = nullptr;
     h->ens64 = nullptr;
@@ -343,12 +425,15 @@ int letkf_sweep_set_obs(letkf_sweep_t h, int nobs, const double* ri, const doubl
     st |= dalloc(&h->obsF, n, s);
     st |= dalloc(&h->obsA, n, s);
     st |= dalloc(&h->meta, n, s);
+    st |= dalloc(&h->operm, n, s);
+    st |= dalloc(&h->ogrp, n, s);
     if (h->d.precision == LETKF_PREC_MIXED) st |= dalloc(&h->ens32, n * ne, s);
     else st |= dalloc(&h->ens64, n * ne, s);
     if (st != LETKF_OK) return LETKF_ERR_CUDA;
     h->obs_cap = n;
   }
   h->nobs = nobs;
+  h->groups_set = false;  // groups belong to an observation set
   dfree(h->var_local, s);  // variable localisation row (read by the record preparation and the plain form)
   h->var_local = nullptr;
   if (var_local_row && dalloc(&h->var_local, (size_t)nvarloc, s) != LETKF_OK) return LETKF_ERR_CUDA;
@@ -403,6 +488,7 @@ int letkf_sweep_set_obs(letkf_sweep_t h, int nobs, const double* ri, const doubl
   note_launch();
   note_launch();
   note_launch();
+  cudaMemcpyAsync(h->operm, perm, sizeof(int) * n, cudaMemcpyDeviceToDevice, s);
   permute<double>(nobs, 1, perm, t_ri, h->ori, s);
   permute<double>(nobs, 1, perm, t_rj, h->orj, s);
   permute<double>(nobs, 1, perm, t_lev, h->olev, s);
@@ -505,6 +591,15 @@ int letkf_sweep_set_option(letkf_sweep_t h, int option, int value) {
       if (value != 0 && value != 1) return LETKF_ERR_ARG;
       h->use_graph = value;
       return LETKF_OK;
+    case LETKF_OPT_MAX_NOBS_PER_GRID:
+      if (value < 0) return LETKF_ERR_ARG;
+      if (value > LETKF_MAX_NOBS_PER_GRID_LIMIT) return LETKF_ERR_CAPACITY;
+      h->max_nobs = value;
+      return LETKF_OK;
+    case LETKF_OPT_FAULT_WAIT:
+      if (value < 0) return LETKF_ERR_ARG;
+      h->fault_wait = (uint32_t)value;
+      return LETKF_OK;
     case LETKF_OPT_EIGENSOLVER:
       if (value != LETKF_EIG_NEWTON_SCHULZ && value != LETKF_EIG_JACOBI) return LETKF_ERR_ARG;
       h->use_ns = value == LETKF_EIG_NEWTON_SCHULZ;
@@ -528,12 +623,30 @@ static int run_f64(letkf_sweep_t h, cudaStream_t s) {
   st |= dalloc(&transm, (size_t)chunk * ne, s);
   if (st != LETKF_OK) return LETKF_ERR_CUDA;
   size_t cap = 0;
+  const bool limited = h->max_nobs > 0;
+  if (limited && !h->groups_set && nobs > 0) st = LETKF_ERR_ARG;
   for (int p0 = 0; p0 < np && st == LETKF_OK; p0 += chunk) {
     const int c = std::min(chunk, np - p0);
-    st = launch_search_scale(h->d.nlon, h->d.nlat, h->G, nobs, h->ori, h->orj, h->olev, h->odat, h->oerr, h->ocls,
-                             h->ovarloc, c, h->pri + p0, h->prj + p0, h->prlev + p0, h->prz + p0, h->var_local,
-                             h->d.params, nullptr, cnt, nullptr, nullptr, nullptr, s);
-    if (st) break;
+    // MAX_NOBS_PER_GRID: the plain lists first, then the limited selection
+    int64_t* uoffs = nullptr;
+    int* uidx = nullptr;
+    double *url = nullptr, *urd = nullptr;
+    if (limited) {
+      st = unlimited_lists(h->d.nlon, h->d.nlat, h->G, nobs, h->ori, h->orj, h->olev, h->odat, h->oerr, h->ocls,
+                           h->ovarloc, c, h->pri + p0, h->prj + p0, h->prlev + p0, h->prz + p0, h->var_local,
+                           h->d.params, s, &uoffs, &uidx, &url, &urd);
+      if (st == LETKF_OK)
+        st = launch_limit_select(c, uoffs, uidx, url, urd, h->ogrp, h->max_nobs, nullptr, cnt, nullptr, nullptr,
+                                 nullptr, s);
+    } else {
+      st = launch_search_scale(h->d.nlon, h->d.nlat, h->G, nobs, h->ori, h->orj, h->olev, h->odat, h->oerr, h->ocls,
+                               h->ovarloc, c, h->pri + p0, h->prj + p0, h->prlev + p0, h->prz + p0, h->var_local,
+                               h->d.params, nullptr, cnt, nullptr, nullptr, nullptr, s);
+    }
+    if (st) {
+      free_unlimited(s, uoffs, uidx, url, urd);
+      break;
+    }
     st = launch_exclusive_scan(c, cnt, offs, scr, s);
     int64_t total = 0;
     cudaMemcpyAsync(&total, offs + c, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
@@ -551,11 +664,19 @@ static int run_f64(letkf_sweep_t h, cudaStream_t s) {
       st |= dalloc(&rdiag, cap, s);
       st |= dalloc(&rows, cap * ne, s);
       st |= dalloc(&dep, cap, s);
-      if (st) break;
+      if (st) {
+        free_unlimited(s, uoffs, uidx, url, urd);
+        break;
+      }
     }
-    st = launch_search_scale(h->d.nlon, h->d.nlat, h->G, nobs, h->ori, h->orj, h->olev, h->odat, h->oerr, h->ocls,
-                             h->ovarloc, c, h->pri + p0, h->prj + p0, h->prlev + p0, h->prz + p0, h->var_local,
-                             h->d.params, offs, cnt, idx, rloc, rdiag, s);
+    if (limited) {
+      st = launch_limit_select(c, uoffs, uidx, url, urd, h->ogrp, h->max_nobs, offs, nullptr, idx, rloc, rdiag, s);
+      free_unlimited(s, uoffs, uidx, url, urd);
+    } else {
+      st = launch_search_scale(h->d.nlon, h->d.nlat, h->G, nobs, h->ori, h->orj, h->olev, h->odat, h->oerr,
+                               h->ocls, h->ovarloc, c, h->pri + p0, h->prj + p0, h->prlev + p0, h->prz + p0,
+                               h->var_local, h->d.params, offs, cnt, idx, rloc, rdiag, s);
+    }
     if (st) break;
     if (total > 0) {
       st = letkf::launch_gather_rows(ne, total, idx, h->ens64, h->odep, 8, rows, dep, s);
@@ -643,6 +764,12 @@ static void build_args(letkf_sweep_t h, SweepArgs& a) {
   a.defer_total = h->defer_total;
   a.defer_list = h->defer_list;  // read by the tensor-core sweep only
   a.defer_count = h->defer_count;
+  a.probe_slot = h->nprobe > 0 ? h->probe_slot : nullptr;
+  a.probe_cap = h->probe_cap;
+  a.probe_idx = h->probe_idx;
+  a.probe_rloc = h->probe_rloc;
+  a.probe_count = h->probe_count;
+  a.fault_wait_polls = h->fault_wait;
 }
 
 static bool tc_path(letkf_sweep_t h) { return h->use_tc && h->use_ns && h->d.ne <= 64; }
@@ -657,18 +784,95 @@ static int launch_mixed_run(letkf_sweep_t h, const SweepArgs& a, cudaStream_t s)
   int st = tc ? launch_sweep_tc(a, s, h->grid_cap) : launch_sweep_mixed(a, s, h->grid_cap);
   if (st != LETKF_OK) return st;
   SweepArgs b = a;
-  b.order = h->defer_list;
+  if (a.list_offs) {
+    b.qmap = h->defer_list;  // list mode: the deferred points are order positions
+  } else {
+    b.order = h->defer_list;
+  }
   b.npts_dev = h->defer_count;
   b.use_ns = 0;
   cudaMemsetAsync(h->counter, 0, sizeof(int), s);
   return launch_sweep_mixed(b, s, h->grid_cap);
 }
 
+// The mixed-form run with the MAX_NOBS_PER_GRID limit: per piece of the
+// processing order, the SCALE search of its points with the limit
+// (letkf_search_scale_limited's two passes) into lists, then the sweep kernels
+// analyse the piece from the lists.  Host synchronisation sizes the lists, so
+// this run is not a CUDA graph.
+static int run_limited(letkf_sweep_t h, const SweepArgs& a, cudaStream_t s) {
+  const int np = h->d.npts;
+  if (!h->groups_set && h->nobs > 0) return LETKF_ERR_ARG;
+  const int chunk = std::min(np, 65536);
+  double *cri = nullptr, *crj = nullptr, *crl = nullptr, *crz = nullptr;
+  int* lcnt = nullptr;
+  int64_t *lofs = nullptr, *scr = nullptr;
+  int* lidx = nullptr;
+  double *lrl = nullptr, *lrd = nullptr;
+  size_t cap = 0;
+  int st = LETKF_OK;
+  st |= dalloc(&cri, (size_t)chunk, s);
+  st |= dalloc(&crj, (size_t)chunk, s);
+  st |= dalloc(&crl, (size_t)chunk, s);
+  st |= dalloc(&crz, (size_t)chunk, s);
+  st |= dalloc(&lcnt, (size_t)chunk, s);
+  st |= dalloc(&lofs, (size_t)chunk + 1, s);
+  st |= dalloc(&scr, (size_t)chunk / 1024 + 2, s);
+  for (int o0 = 0; o0 < np && st == LETKF_OK; o0 += chunk) {
+    const int c = std::min(chunk, np - o0);
+    gather_points_kernel<<<(c + 255) / 256, 256, 0, s>>>(c, h->order + o0, h->pri, h->prj, h->prlev, h->prz, cri,
+                                                         crj, crl, crz);
+    note_launch();
+    int64_t* uoffs = nullptr;
+    int* uidx = nullptr;
+    double *url = nullptr, *urd = nullptr;
+    st = unlimited_lists(h->d.nlon, h->d.nlat, h->G, h->nobs, h->ori, h->orj, h->olev, h->odat, h->oerr, h->ocls,
+                         h->ovarloc, c, cri, crj, crl, crz, h->var_local, h->d.params, s, &uoffs, &uidx, &url, &urd);
+    if (st == LETKF_OK)
+      st = launch_limit_select(c, uoffs, uidx, url, urd, h->ogrp, h->max_nobs, nullptr, lcnt, nullptr, nullptr,
+                               nullptr, s);
+    if (st == LETKF_OK) st = launch_exclusive_scan(c, lcnt, lofs, scr, s);
+    int64_t total = 0;
+    if (st == LETKF_OK) {
+      cudaMemcpyAsync(&total, lofs + c, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+      st = cuda_status(cudaStreamSynchronize(s));
+    }
+    if (st == LETKF_OK && (size_t)total + 1 > cap) {
+      dfree(lidx, s);
+      dfree(lrl, s);
+      dfree(lrd, s);
+      cap = (size_t)total + (size_t)total / 4 + 1024;
+      st |= dalloc(&lidx, cap, s);
+      st |= dalloc(&lrl, cap, s);
+      st |= dalloc(&lrd, cap, s);
+    }
+    if (st == LETKF_OK)
+      st = launch_limit_select(c, uoffs, uidx, url, urd, h->ogrp, h->max_nobs, lofs, nullptr, lidx, lrl, lrd, s);
+    free_unlimited(s, uoffs, uidx, url, urd);
+    if (st != LETKF_OK) break;
+    SweepArgs b = a;
+    b.order = h->order + o0;
+    b.nwork = c;
+    b.list_offs = lofs;
+    b.list_idx = lidx;
+    b.list_rloc = lrl;
+    st = launch_mixed_run(h, b, s);
+    // the next piece's search reuses the point and list buffers
+    if (st == LETKF_OK) st = cuda_status(cudaStreamSynchronize(s));
+  }
+  void* fr[] = {cri, crj, crl, crz, lcnt, lofs, scr, lidx, lrl, lrd};
+  for (void* p : fr) dfree(p, s);
+  return st;
+}
+
 static int run_on(letkf_sweep_t h, cudaStream_t s) {
+  // a run reports only its own bounded-wait timeouts
+  cudaMemsetAsync(h->err_flag, 0, sizeof(int), s);
   if (h->d.precision == LETKF_PREC_F64) return run_f64(h, s);
   SweepArgs a;
   build_args(h, a);
   cudaMemsetAsync(h->defer_total, 0, sizeof(int), s);
+  if (h->max_nobs > 0) return run_limited(h, a, s);
   if (!h->use_graph) return launch_mixed_run(h, a, s);
   // key: kernel arguments, launch choices and stream
   std::vector<unsigned char> key(sizeof(a) + 3 * sizeof(int) + sizeof(s));
@@ -784,7 +988,7 @@ static int copy_rows(const int64_t* cp, int nv, int64_t np, size_t row, void* ds
 int letkf_sweep_run_host(letkf_sweep_t h, const void* xb, void* xa, int nchunks, void* stream) {
   if (!h || !xb || !xa || nchunks < 1) return LETKF_ERR_ARG;
   const int np = h->d.npts;
-  if (h->d.precision == LETKF_PREC_F64 || np == 0 || nchunks == 1) {
+  if (h->d.precision == LETKF_PREC_F64 || np == 0 || nchunks == 1 || h->max_nobs > 0) {
     int st = letkf_sweep_set_background(h, xb, 0);
     if (st == LETKF_OK) st = letkf_sweep_run(h, stream);
     if (st == LETKF_OK) st = letkf_sweep_get_analysis(h, xa, 0);
@@ -815,6 +1019,7 @@ int letkf_sweep_run_host(letkf_sweep_t h, const void* xb, void* xa, int nchunks,
   SweepArgs a;
   build_args(h, a);
   cudaMemsetAsync(h->defer_total, 0, sizeof(int), s);
+  cudaMemsetAsync(h->err_flag, 0, sizeof(int), s);
   const size_t row = (size_t)h->d.ne * elem(h);
   const int nv = h->d.nv;
   int st = LETKF_OK;
@@ -851,7 +1056,8 @@ int letkf_sweep_run_host(letkf_sweep_t h, const void* xb, void* xa, int nchunks,
 
 int letkf_sweep_autotune(letkf_sweep_t h, int sample_points, int* choice) {
   if (!h || sample_points < 1) return LETKF_ERR_ARG;
-  if (h->d.precision == LETKF_PREC_F64 || h->d.npts == 0) {
+  if (h->d.precision == LETKF_PREC_F64 || h->d.npts == 0 || h->max_nobs > 0) {
+    // nothing to tune (the plain form; the limited run keeps the handle's choice)
     if (choice) {
       choice[0] = 0;
       choice[1] = 0;
@@ -962,6 +1168,80 @@ int letkf_sweep_get_diagnostics(letkf_sweep_t h, double* infl, int* nobsl, int* 
   return st != LETKF_OK ? st : check_err(h);
 }
 
+int letkf_sweep_set_obs_groups(letkf_sweep_t h, const int* uid, const int* typ, int nid, int ntyp) {
+  if (!h || nid < 1 || ntyp < 1 || (int64_t)nid * ntyp >= (int64_t)INT32_MAX) return LETKF_ERR_ARG;
+  const int n = h->nobs;
+  if (n > 0 && (!uid || !typ)) return LETKF_ERR_ARG;
+  for (int i = 0; i < n; i++)
+    if (uid[i] < 1 || uid[i] > nid || typ[i] < 1 || typ[i] > ntyp) return LETKF_ERR_ARG;
+  h->groups_set = true;
+  if (n == 0) return LETKF_OK;
+  cudaStream_t s = h->stream;
+  int *du = nullptr, *dt = nullptr;
+  int st = dalloc(&du, (size_t)n, s);
+  st |= dalloc(&dt, (size_t)n, s);
+  if (st != LETKF_OK) return LETKF_ERR_CUDA;
+  cudaMemcpyAsync(du, uid, sizeof(int) * n, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(dt, typ, sizeof(int) * n, cudaMemcpyHostToDevice, s);
+  st = launch_obs_group(n, du, dt, nid, h->operm, h->ogrp, s);
+  dfree(du, s);
+  dfree(dt, s);
+  const int st2 = cuda_status(cudaStreamSynchronize(s));
+  if (st != LETKF_OK || st2 != LETKF_OK) h->groups_set = false;
+  return st != LETKF_OK ? st : st2;
+}
+
+int letkf_sweep_set_probe(letkf_sweep_t h, int npts_probe, const int* points, int cap) {
+  if (!h || npts_probe < 0 || (npts_probe > 0 && (!points || cap < 1))) return LETKF_ERR_ARG;
+  if ((int64_t)npts_probe * cap > ((int64_t)1 << 31)) return LETKF_ERR_CAPACITY;
+  const int np = h->d.npts;
+  std::vector<int> slot(np, -1);
+  for (int i = 0; i < npts_probe; i++) {
+    const int p = points[i];
+    if (p < 0 || p >= np || slot[p] >= 0) return LETKF_ERR_ARG;  // out of range or repeated
+    slot[p] = i;
+  }
+  cudaStream_t s = h->stream;
+  void* old[] = {h->probe_slot, h->probe_idx, h->probe_count, h->probe_rloc};
+  for (void* p : old) dfree(p, s);
+  h->probe_slot = h->probe_idx = h->probe_count = nullptr;
+  h->probe_rloc = nullptr;
+  h->nprobe = 0;
+  h->probe_cap = 0;
+  if (npts_probe == 0) return cuda_status(cudaStreamSynchronize(s));
+  const size_t tot = (size_t)npts_probe * cap;
+  int st = dalloc(&h->probe_slot, (size_t)np, s);
+  st |= dalloc(&h->probe_idx, tot, s);
+  st |= dalloc(&h->probe_rloc, tot, s);
+  st |= dalloc(&h->probe_count, (size_t)npts_probe, s);
+  if (st != LETKF_OK) return LETKF_ERR_CUDA;
+  cudaMemcpyAsync(h->probe_slot, slot.data(), sizeof(int) * np, cudaMemcpyHostToDevice, s);
+  cudaMemsetAsync(h->probe_idx, 0xff, sizeof(int) * tot, s);
+  cudaMemsetAsync(h->probe_count, 0xff, sizeof(int) * npts_probe, s);
+  h->nprobe = npts_probe;
+  h->probe_cap = cap;
+  return cuda_status(cudaStreamSynchronize(s));
+}
+
+int letkf_sweep_get_probe(letkf_sweep_t h, int* count, int* obs, float* rloc) {
+  if (!h || h->nprobe == 0) return LETKF_ERR_ARG;
+  cudaStream_t s = h->stream;
+  const size_t tot = (size_t)h->nprobe * h->probe_cap;
+  std::vector<int> cnt(h->nprobe), idx(obs ? tot : 0), perm(obs ? (size_t)h->nobs : 0);
+  cudaMemcpyAsync(cnt.data(), h->probe_count, sizeof(int) * h->nprobe, cudaMemcpyDeviceToHost, s);
+  if (obs) {
+    cudaMemcpyAsync(idx.data(), h->probe_idx, sizeof(int) * tot, cudaMemcpyDeviceToHost, s);
+    if (h->nobs > 0) cudaMemcpyAsync(perm.data(), h->operm, sizeof(int) * h->nobs, cudaMemcpyDeviceToHost, s);
+  }
+  if (rloc) cudaMemcpyAsync(rloc, h->probe_rloc, sizeof(float) * tot, cudaMemcpyDeviceToHost, s);
+  const int st = cuda_status(cudaStreamSynchronize(s));
+  if (st != LETKF_OK) return st;
+  if (count) memcpy(count, cnt.data(), sizeof(int) * h->nprobe);
+  if (obs)
+    for (size_t i = 0; i < tot; i++) obs[i] = (idx[i] >= 0 && idx[i] < h->nobs) ? perm[(size_t)idx[i]] : -1;
+  return LETKF_OK;
+}
+
 int letkf_sweep_footprint(const letkf_sweep_desc* d, int nobs, size_t* bytes) {
   if (!d || !bytes || nobs < 0 || d->npts < 0 || d->ne < 1 || d->nv < 1) return LETKF_ERR_ARG;
   const size_t np = (size_t)d->npts, n = (size_t)nobs, ne = (size_t)d->ne;
@@ -969,7 +1249,7 @@ int letkf_sweep_footprint(const letkf_sweep_desc* d, int nobs, size_t* bytes) {
   const size_t ncell = (size_t)d->nlon * d->nlat;
   // resident: points, ensembles, per-point outputs, bucket table, sorted observations
   size_t b = np * (6 * 8 + 4 * 5) + 2 * np * d->nv * ne * es + (ncell + d->nlat) * 4 + 64;
-  b += n * (6 * 8 + 2 * 4 + 2 * 16 + 4 + ne * es);
+  b += n * (6 * 8 + 4 * 4 + 2 * 16 + 4 + ne * es);
   // set_obs staging (unsorted records, permutation, cell counts) while the above is live
   size_t stage = n * (6 * 8 + 4 * 4 + ne * 8) + ncell * 16 + 64;
   if (d->precision == LETKF_PREC_F64) {
@@ -980,6 +1260,55 @@ int letkf_sweep_footprint(const letkf_sweep_desc* d, int nobs, size_t* bytes) {
   }
   *bytes = b + stage;
   return LETKF_OK;
+}
+
+int letkf_sort_obs_latlon(int nlon, int nlat, const double* lon, const double* lat, int nobs, const double* olon,
+                          const double* olat, const int* qc, int* perm, int* nsorted, int* nobsgrd, void* stream) {
+  if (nlon < 2 || nlat < 3 || nobs < 0 || !lon || !lat || !perm || !nsorted || !nobsgrd) return LETKF_ERR_ARG;
+  if (nobs > 0 && (!olon || !olat)) return LETKF_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return LETKF_ERR_NOGPU;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const int ncell = nlon * nlat;
+  int *cell = nullptr, *counts = nullptr, *cursor = nullptr;
+  int64_t *start = nullptr, *scr = nullptr;
+  int st = LETKF_OK;
+  st |= dalloc(&cell, (size_t)nobs, s);
+  st |= dalloc(&counts, (size_t)ncell, s);
+  st |= dalloc(&cursor, (size_t)ncell, s);
+  st |= dalloc(&start, (size_t)ncell + 1, s);
+  st |= dalloc(&scr, (size_t)ncell / 1024 + 2, s);
+  if (st == LETKF_OK) {
+    cudaMemsetAsync(counts, 0, sizeof(int) * ncell, s);
+    cudaMemsetAsync(cursor, 0, sizeof(int) * ncell, s);
+    if (nobs > 0) {
+      latlon_cell_kernel<<<(nobs + 255) / 256, 256, 0, s>>>(nobs, nlon, nlat, lon, lat, olon, olat, qc, cell, counts);
+      note_launch();
+    }
+    st = launch_exclusive_scan(ncell, counts, start, scr, s);
+  }
+  if (st == LETKF_OK && nobs > 0) {
+    latlon_scatter_kernel<<<(nobs + 255) / 256, 256, 0, s>>>(nobs, cell, start, cursor, perm);
+    // input order inside each cell, as the reference's sequential loops give
+    obs_stabilize_kernel<<<(ncell + 255) / 256, 256, 0, s>>>(ncell, start, perm);
+    note_launch();
+    note_launch();
+  }
+  if (st == LETKF_OK) {
+    latlon_grd_kernel<<<(ncell + 255) / 256, 256, 0, s>>>(nlon, nlat, start, nobsgrd);
+    note_launch();
+    int64_t total = 0;
+    cudaMemcpyAsync(&total, start + ncell, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+    st = cuda_status(cudaStreamSynchronize(s));
+    *nsorted = (int)total;
+  }
+  void* fr[] = {cell, counts, cursor, start, scr};
+  for (void* p : fr) dfree(p, s);
+  const int st2 = cuda_status(cudaStreamSynchronize(s));
+  return st != LETKF_OK ? st : st2;
 }
 
 int letkf_sweep_sorted_obs(letkf_sweep_t h, int* nobsgrd) {

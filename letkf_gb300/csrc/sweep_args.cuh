@@ -49,6 +49,26 @@ struct SweepArgs {
   float ns_cond_max;    // Newton-Schulz only while the spectrum bound s / c is below this (0: no bound); a
                         // larger bound, or an iteration that does not converge, sends the point to the Jacobi pass
   int* defer_total;     // points handed to the Jacobi pass in this run (the deferred pass adds its count)
+  // selection probe: for points with probe_slot[pt] >= 0 the search also
+  // writes what it accepted, in emitted order (sorted observation index and
+  // FP32 rloc), to probe_idx / probe_rloc[slot * probe_cap + i] for
+  // i < probe_cap, and the accepted count to probe_count[slot]
+  const int* probe_slot;  // [npts] or NULL (no probe)
+  int probe_cap;
+  int* probe_idx;
+  float* probe_rloc;
+  int* probe_count;
+  // list mode: the local observations of order position q are given as
+  // entries list_offs[q] .. list_offs[q+1] - 1 (sorted observation index and
+  // FP64 rloc, in the order they enter letkf_core) instead of being searched
+  const int64_t* list_offs;  // [nwork + 1] or NULL (search)
+  const int* qmap;           // if set, work item q analyses order position qmap[q] (the deferred pass of list mode)
+  const int* list_idx;
+  const double* list_rloc;
+  // failure injection: > 0 makes the tensor-core sweep wait, before its first
+  // point, on a barrier that nothing arrives at, giving up after this many
+  // polls (LETKF_ERR_TIMEOUT through err_flag); 0 in normal runs
+  uint32_t fault_wait_polls;
 };
 
 }  // namespace letkf

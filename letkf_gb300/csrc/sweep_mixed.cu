@@ -33,7 +33,7 @@ constexpr float SW_BAND = 1.0e-3f;
 __device__ double scale_ndist_exact(const SweepArgs& a, int ob, double ri, double rj, double logr, double rz) {
   const SweepScaleParams& P = a.P;
   const double rdx = (ri - a.ori[ob]) * P.dx, rdy = (rj - a.orj[ob]) * P.dy;
-  double nd_h = sqrt(rdx * rdx + rdy * rdy), nd_v;
+  double nd_h = sqrt(sumsq_rn(rdx, rdy)), nd_v;
   const int cls = a.ocls[ob];
   if (cls == 1) {
     nd_h = nd_h / P.sigma_obs;
@@ -54,7 +54,7 @@ __device__ double scale_ndist_exact(const SweepArgs& a, int ob, double ri, doubl
     nd_h = nd_h / P.sigma_obs;
     nd_v = fabs(log(a.olev[ob]) - logr) / P.sigma_obsv;
   }
-  return nd_h * nd_h + nd_v * nd_v;
+  return sumsq_rn(nd_h, nd_v);
 }
 
 template <int NP>
@@ -110,7 +110,8 @@ __global__ void __launch_bounds__(MixedCfg<NP>::NT, MixedCfg<NP>::MINB) sweep_mi
     __syncthreads();
     const int q = ctrl[0];
     if (q >= npts_work) break;
-    const int pt = a.order[q];
+    const int qq = a.qmap ? a.qmap[q] : q;  // position in `order` (and in the list of list mode)
+    const int pt = a.order[qq];
     const double ri = a.pri[pt], rj = a.prj[pt], rz = a.prz ? a.prz[pt] : 0.0;
     const double logr = a.plogr[pt];
     const float rif = (float)ri, rjf = (float)rj, logrf = (float)logr, rzf = (float)rz;
@@ -123,7 +124,42 @@ __global__ void __launch_bounds__(MixedCfg<NP>::NT, MixedCfg<NP>::MINB) sweep_mi
     GramAcc<NP> acc;
     acc.zero();
     int pend = 0, L = 0;
-    const bool any = a.nobs > 0 && a.G[(size_t)(a.nlat - 1) * ld + a.nlon] > 0 && imin <= imax && jmin <= jmax;
+    const int probe = a.probe_slot ? a.probe_slot[pt] : -1;
+    // list mode: the point's local observations come from a list (for instance
+    // the MAX_NOBS_PER_GRID selection), staged CH at a time in list order
+    if (a.list_offs) {
+      const int64_t o0 = a.list_offs[qq], o1 = a.list_offs[qq + 1];
+      for (int64_t b = o0; b < o1; b += CH) {
+        const int nr = (int)min((int64_t)CH, o1 - b);
+        __syncthreads();
+        for (int t = tid; t < nr; t += NT) {
+          const int ob = a.list_idx[b + t];
+          const float rl = (float)a.list_rloc[b + t];
+          const float4 g4 = a.obsA[ob];
+          pidx[t] = ob;
+          pr[t] = rl;
+          pw[t] = rl * g4.y;
+          pd[t] = g4.z;
+        }
+        __syncthreads();
+        for (int t = tid; t < CH * NP; t += NT) {
+          const int r = t / NP, m = t - r * NP;
+          const float y = (r < nr && m < n) ? a.ens_obs[(size_t)pidx[r] * n + m] : 0.f;
+          sm[S::Y + t] = y;
+          sm[S::YW + t] = r < nr ? y * pw[r] : 0.f;
+        }
+        if (tid < nr) {
+          sm[S::WR + tid] = pw[tid];
+          sm[S::DR + tid] = pd[tid];
+          sm[S::RL + tid] = pr[tid];
+        }
+        __syncthreads();
+        gram_chunk<NP>(sm, nr, acc);
+      }
+      L = (int)(o1 - o0);
+    }
+    const bool any = !a.list_offs && a.nobs > 0 && a.G[(size_t)(a.nlat - 1) * ld + a.nlon] > 0 && imin <= imax &&
+                     jmin <= jmax;
     for (int jb = jmin; any && jb <= jmax; jb += SW_MAXROWS) {
       const int nrow = min(SW_MAXROWS, jmax - jb + 1);
       // row table: candidate ranges of obs_choose in row order
@@ -191,11 +227,17 @@ __global__ void __launch_bounds__(MixedCfg<NP>::NT, MixedCfg<NP>::MINB) sweep_mi
         }
         __syncthreads();
         if (acc_ok) {
-          const int slot = pend + wcnt[wid] + before;
+          const int rel = wcnt[wid] + before;
+          const int slot = pend + rel;
           pidx[slot] = ob;
           pw[slot] = w;
           pd[slot] = dv;
           pr[slot] = rl;
+          if (probe >= 0 && L + rel < a.probe_cap) {
+            const size_t at = (size_t)probe * a.probe_cap + (L + rel);
+            a.probe_idx[at] = ob;
+            a.probe_rloc[at] = rl;
+          }
         }
         pend += wcnt[NT / 32];
         L += wcnt[NT / 32];
@@ -265,6 +307,7 @@ __global__ void __launch_bounds__(MixedCfg<NP>::NT, MixedCfg<NP>::MINB) sweep_mi
       __syncthreads();
       gram_chunk<NP>(sm, pend, acc);
     }
+    if (probe >= 0 && tid == 0) a.probe_count[probe] = L;
     // ---- core ----
     double infl = a.infl[pt];
     int sweeps = 0;
@@ -285,7 +328,7 @@ __global__ void __launch_bounds__(MixedCfg<NP>::NT, MixedCfg<NP>::MINB) sweep_mi
           // spectrum bound beyond the iteration's range, or no convergence:
           // the point goes to the Jacobi pass (ok is uniform over the CTA)
           if (tid == 0) {
-            a.defer_list[atomicAdd(a.defer_count, 1)] = pt;
+            a.defer_list[atomicAdd(a.defer_count, 1)] = a.list_offs ? qq : pt;
             if (a.defer_total) atomicAdd(a.defer_total, 1);
             if (a.nobsl_out) a.nobsl_out[pt] = L;
           }

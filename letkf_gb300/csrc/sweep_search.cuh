@@ -8,6 +8,8 @@
 // reference order, into a pending list (index, weight rloc/err^2, departure,
 // rloc); `flush(nr)` consumes the first nr entries whenever CH are pending and
 // once more for the remainder.  Returns the number of accepted observations.
+// With probe >= 0 the accepted entries are also written, in emitted order, to
+// the selection probe of SweepArgs (slot `probe`).
 #pragma once
 #include "sweep_args.cuh"
 
@@ -21,7 +23,7 @@ __device__ __forceinline__ double scale_ndist_exact(const SweepArgs& a, int ob, 
                                                     double rz) {
   const SweepScaleParams& P = a.P;
   const double rdx = (ri - a.ori[ob]) * P.dx, rdy = (rj - a.orj[ob]) * P.dy;
-  double nd_h = sqrt(rdx * rdx + rdy * rdy), nd_v;
+  double nd_h = sqrt(sumsq_rn(rdx, rdy)), nd_v;
   const int cls = a.ocls[ob];
   if (cls == 1) {
     nd_h = nd_h / P.sigma_obs;
@@ -42,7 +44,7 @@ __device__ __forceinline__ double scale_ndist_exact(const SweepArgs& a, int ob, 
     nd_h = nd_h / P.sigma_obs;
     nd_v = fabs(log(a.olev[ob]) - logr) / P.sigma_obsv;
   }
-  return nd_h * nd_h + nd_v * nd_v;
+  return sumsq_rn(nd_h, nd_v);
 }
 
 struct SearchSmem {
@@ -61,7 +63,7 @@ struct SearchSmem {
 // compacted group by group, which keeps the reference's candidate order.
 template <int NT, int CH, int CPT = 1, typename Flush>
 __device__ int sweep_search(const SweepArgs& a, double ri, double rj, double logr, double rz, const SearchSmem& s,
-                            Flush&& flush) {
+                            int probe, Flush&& flush) {
   constexpr int NW = NT / 32;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int ld = a.nlon + 1;
@@ -157,11 +159,17 @@ __device__ int sweep_search(const SweepArgs& a, double ri, double rj, double log
 #pragma unroll
       for (int g = 0; g < CPT; g++)
         if (okg[g]) {
-          const int slot = pend + s.wcnt[g * NW + wid] + before[g];
+          const int rel = s.wcnt[g * NW + wid] + before[g];
+          const int slot = pend + rel;
           s.pidx[slot] = obg[g];
           s.pw[slot] = wg[g];
           s.pd[slot] = dg[g];
           s.pr[slot] = rg[g];
+          if (probe >= 0 && L + rel < a.probe_cap) {
+            const size_t at = (size_t)probe * a.probe_cap + (L + rel);
+            a.probe_idx[at] = obg[g];
+            a.probe_rloc[at] = rg[g];
+          }
         }
       pend += s.wcnt[CPT * NW];
       L += s.wcnt[CPT * NW];
@@ -203,7 +211,35 @@ __device__ int sweep_search(const SweepArgs& a, double ri, double rj, double log
     flush(pend);
     __syncthreads();
   }
+  if (probe >= 0 && threadIdx.x == 0) a.probe_count[probe] = L;
   return L;
+}
+
+// List mode: the point's local observations come from a list made by another
+// search (for instance the MAX_NOBS_PER_GRID selection) instead of the scan
+// above; they are fed to `flush` in stages of CH, in list order, with the same
+// pending-list entries (index, weight rloc / err^2, departure, rloc).
+template <int NT, int CH, typename Flush>
+__device__ int sweep_list(const SweepArgs& a, int q, const SearchSmem& s, Flush&& flush) {
+  const int tid = threadIdx.x;
+  const int64_t o0 = a.list_offs[q], o1 = a.list_offs[q + 1];
+  for (int64_t b = o0; b < o1; b += CH) {
+    const int nr = (int)min((int64_t)CH, o1 - b);
+    __syncthreads();
+    for (int t = tid; t < nr; t += NT) {
+      const int ob = a.list_idx[b + t];
+      const float rl = (float)a.list_rloc[b + t];
+      const float4 q4 = a.obsA[ob];
+      s.pidx[t] = ob;
+      s.pr[t] = rl;
+      s.pw[t] = rl * q4.y;
+      s.pd[t] = q4.z;
+    }
+    __syncthreads();
+    flush(nr);
+    __syncthreads();
+  }
+  return (int)(o1 - o0);
 }
 
 }  // namespace letkf

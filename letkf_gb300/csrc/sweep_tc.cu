@@ -73,8 +73,8 @@ struct TcLayout {
   static constexpr int ROWPRE = ROWIB + 4 * SW_MAXROWS;
   static constexpr int WCNT = ROWPRE + 4 * (SW_MAXROWS + 1);
   static constexpr int MEAN = ((WCNT + 4 * (TC_CPT * TC_NT / 32 + 2)) + 7) & ~7;  // double[16]
-  static constexpr int MBAR = MEAN + 128;        // uint64[4]: Gram stages 0/1, products, background rows
-  static constexpr int TMEMH = MBAR + 32;        // uint32
+  static constexpr int MBAR = MEAN + 128;        // uint64[5]: Gram stages 0/1, products, background rows, drain
+  static constexpr int TMEMH = MBAR + 40;        // uint32
   static constexpr int CTRL = TMEMH + 8;         // int[4]
   static constexpr int TOTAL = CTRL + 16;
 };
@@ -199,6 +199,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
     tc::mbar_init(&mbar[1], 1);
     tc::mbar_init(&mbar[2], 1);
     tc::mbar_init(&mbar[3], 1);
+    tc::mbar_init(&mbar[4], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (wid == 0) tc::tmem_alloc(tmem_holder, TC_TMEM_COLS);
@@ -219,18 +220,33 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
   const int npts_work = a.npts_dev ? *a.npts_dev : a.nwork;
   const double inv_n = 1.0 / (double)n;  // one FP64 division per kernel, not per variable and point
 
+  // A wait that gives up still flips its parity, so that control flow stays
+  // the same in every thread; the drain below then waits (with a long bound)
+  // for what the timed-out wait left in flight before TMEM is released.
+  uint32_t xb_lost = 0u;  // bit 1: a background-row copy whose wait gave up; bit 0: its phase parity
   auto wait_bar = [&](int i) {
-    if (!tc::mbar_wait(&mbar[i], (par >> i) & 1u, TC_WAIT)) tmo = 1;
+    const uint32_t pb = (par >> i) & 1u;
+    if (!tc::mbar_wait(&mbar[i], pb, TC_WAIT)) {
+      tmo = 1;
+      if (i == 3) xb_lost = 2u | pb;
+    }
     par ^= 1u << i;
   };
 
-  for (;;) {
+  // failure injection: a wait on a barrier that nothing arrives at gives up
+  // after the given polls; the CTA then processes no point
+  if (a.fault_wait_polls > 0u && !tc::mbar_wait(&mbar[4], 0u, a.fault_wait_polls)) tmo = 1;
+  const bool skip_all = __syncthreads_or(tmo);  // uniform over the CTA
+  if (skip_all) tmo = 1;
+
+  for (; !skip_all;) {
     __syncthreads();
     if (tid == 0) ctrl[0] = atomicAdd(a.counter, 1);
     __syncthreads();
     const int q = ctrl[0];
     if (q >= npts_work) break;
-    const int pt = a.order[q];
+    const int qq = a.qmap ? a.qmap[q] : q;  // position in `order` (and in the list of list mode)
+    const int pt = a.order[qq];
     const double ri = a.pri[pt], rj = a.prj[pt], rz = a.prz ? a.prz[pt] : 0.0;
     const double logr = a.plogr[pt];
 
@@ -299,7 +315,9 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
       first = false;
       chunk++;
     };
-    const int Lp = sweep_search<TC_NT, TC_CH, TC_CPT>(a, ri, rj, logr, rz, ss, flush);
+    const int probe = a.probe_slot ? a.probe_slot[pt] : -1;
+    const int Lp = a.list_offs ? sweep_list<TC_NT, TC_CH>(a, qq, ss, flush)
+                               : sweep_search<TC_NT, TC_CH, TC_CPT>(a, ri, rj, logr, rz, ss, probe, flush);
     for (int b = 0; b < 2; b++)
       if ((outst >> b) & 1u) {
         wait_bar(b);
@@ -861,7 +879,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
     if (tid == 0 && a.nobsl_out) a.nobsl_out[pt] = Lp;
     if (deferred) {
       if (tid == 0) {
-        a.defer_list[atomicAdd(a.defer_count, 1)] = pt;
+        a.defer_list[atomicAdd(a.defer_count, 1)] = a.list_offs ? qq : pt;
         if (a.defer_total) atomicAdd(a.defer_total, 1);
       }
       if (xb_outst) {
@@ -938,7 +956,19 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
   for (int b = 0; b < 2; b++)
     if ((outst >> b) & 1u) wait_bar(b);
   if (xb_outst) wait_bar(3);
-  if (__syncthreads_or(tmo) && tid == 0 && a.err_flag) atomicExch(a.err_flag, 1);
+  if (__syncthreads_or(tmo)) {
+    // a wait gave up: before TMEM and shared memory are released, every MMA
+    // this CTA issued (one commit on the drain barrier tracks all of them)
+    // and a background-row copy whose wait gave up must have landed; both
+    // always complete, so these waits end
+    if (tid == 0) {
+      tc::fence_after_sync();
+      tc::mma_commit(&mbar[4]);
+      if (a.err_flag) atomicExch(a.err_flag, 1);
+    }
+    tc::mbar_wait(&mbar[4], 0u, TC_WAIT);
+    if (xb_lost) tc::mbar_wait(&mbar[3], xb_lost & 1u, TC_WAIT);
+  }
   tc::fence_before_sync();
   __syncthreads();
   if (wid == 0) {

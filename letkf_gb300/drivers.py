@@ -24,31 +24,23 @@ from . import core as K
 
 
 # ----------------------------------------------------------------------- SPEEDY
-def speedy_sort_obs(lon, lat, olon, olat):
+def speedy_sort_obs(lon, lat, olon, olat, device=None):
     """Stable bucket sort of observations by (latitude band, longitude cell)
-    (speedy/letkf/letkf_obs.f90:243-313).  Band j (1-based, 1..nlat-1) holds
-    lat(j) <= y < lat(j+1); cell i holds lon(i) <= x < lon(i+1), the last cell
-    up to 360.  Returns (perm, nobsgrd[nlat, nlon]) with nobsgrd[j-1, i-1] the
+    (speedy/letkf/letkf_obs.f90:243-313), on the device (letkf_sort_obs_latlon).
+    Band j (1-based, 1..nlat-1) holds lat(j) <= y < lat(j+1); cell i holds
+    lon(i) <= x < lon(i+1), the last cell up to 360.  Host arrays in, host
+    arrays out: (perm, nobsgrd[nlat, nlon]) with nobsgrd[j-1, i-1] the
     cumulative count through cell (i, j); observations outside every band are
     dropped, and row nlat of nobsgrd is never written by the reference (0).
     Longitudes must lie in [0, 360): the reference counts an observation at
     360 in its band but places it in no cell, leaving an unfilled slot that
     the next band's first cell range covers; here it is dropped."""
-    lon = np.asarray(lon, dtype=np.float64)
-    lat = np.asarray(lat, dtype=np.float64)
-    olon = np.asarray(olon, dtype=np.float64)
-    olat = np.asarray(olat, dtype=np.float64)
-    nlon, nlat = lon.size, lat.size
-    j = np.searchsorted(lat, olat, side="right")            # lat[j-1] <= y < lat[j]
-    i = np.searchsorted(lon, olon, side="right")            # lon[i-1] <= x < lon[i] (i < nlon)
-    ok = (j >= 1) & (j <= nlat - 1) & (i >= 1) & ((i < nlon) | (olon < 360.0))
-    key = (j - 1).astype(np.int64) * nlon + (i - 1)
-    sel = np.nonzero(ok)[0]
-    perm = sel[np.argsort(key[sel], kind="stable")].astype(np.int32)
-    counts = np.bincount(key[sel], minlength=nlon * nlat).astype(np.int64)
-    grd = np.cumsum(counts).reshape(nlat, nlon).astype(np.int32)
-    grd[nlat - 1, :] = 0
-    return perm, grd
+    import torch
+
+    dev = torch.device("cuda", torch.cuda.current_device()) if device is None else device
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device=dev)
+    perm, grd = K.sort_obs_latlon(t(lon), t(lat), t(olon), t(olat))
+    return perm.cpu().numpy(), grd.cpu().numpy()
 
 
 def var_local_n2n(var_local):
@@ -184,15 +176,17 @@ def speedy_obs_setup(lon, lat, sig, g3, g2, obs, gross_error=GROSS_ERROR, stream
     hx, qc = K.speedy_obsope(t(lat), t(sig), v3, v2, t(elem_i, torch.int32), t(obs["lon"]), t(obs["lat"]),
                              t(obs["lev"]), t(obs["dat"]), stream=stream)
     hdxf, dep, qc2 = K.obs_departure(hx, t(obs["dat"]), t(obs["err"]), gross_error, qc, stream)
-    qc_h = qc2.cpu().numpy()
-    keep = np.nonzero(qc_h == 1)[0]
-    perm, grd = speedy_sort_obs(lon, lat, obs["lon"][keep], obs["lat"][keep])
-    order = keep[perm]
-    idx = t(order, torch.int64)
-    obs_dev = {"elm": t(obs["elem"][order]), "lon": t(obs["lon"][order]), "lat": t(obs["lat"][order]),
-               "lev": t(obs["lev"][order]), "dat": t(obs["dat"][order]), "err": t(obs["err"][order])}
-    grid = {"lon": t(lon), "lat": t(lat), "nobsgrd": t(grd, torch.int32)}
-    return grid, obs_dev, hdxf.index_select(0, idx).contiguous(), dep.index_select(0, idx).contiguous(), qc_h
+    # selection of qc = 1 and the bucket sort on the device, then the records,
+    # perturbations and departures gathered into the sorted order
+    glon, glat = t(lon), t(lat)
+    olon, olat = t(obs["lon"]), t(obs["lat"])
+    perm, grd = K.sort_obs_latlon(glon, glat, olon, olat, qc2, stream)
+    one = lambda a: K.gather_rows(perm, a.reshape(-1, 1), None, stream)[0].reshape(-1)
+    obs_dev = {"elm": one(t(obs["elem"])), "lon": one(olon), "lat": one(olat), "lev": one(t(obs["lev"])),
+               "dat": one(t(obs["dat"])), "err": one(t(obs["err"]))}
+    hd_s, dep_s = K.gather_rows(perm, hdxf, dep, stream)
+    grid = {"lon": glon, "lat": glat, "nobsgrd": grd}
+    return grid, obs_dev, hd_s, dep_s, qc2.cpu().numpy()
 
 
 def speedy_cycle(gues_paths, obs_path, anal_paths, lon, lat, sig, infl_path=None, cov_infl_mul=-1.01,

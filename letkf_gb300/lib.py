@@ -20,6 +20,7 @@ LETKF_ERR_NOGPU = 5
 LETKF_ERR_TIMEOUT = 6
 LETKF_MAX_NE = 128
 LETKF_LARGEK_MAX_NE = 1024
+LETKF_MAX_NOBS_PER_GRID_LIMIT = 256
 
 HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "letkf_gpu.h")
 
@@ -49,6 +50,9 @@ _SIGS = {
     "letkf_update_f64": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
     "letkf_search_scale": (_i, [_i, _i, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp,
                                 _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "letkf_search_scale_limited": (_i, [_i, _i, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i,
+                                        _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "letkf_sort_obs_latlon": (_i, [_i, _i, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "letkf_search_gfs": (_i, [_i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp,
                               _vp, _vp, _vp, _vp, _vp, _vp]),
     "letkf_search_speedy": (_i, [_i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp,

@@ -155,6 +155,11 @@ class Server:
 
     # ------------------------------------------------------------------ wait
     def wait(self, job, timeout=None, raise_on_error=True):
+        if job.result is not None and job.result["status"] != LETKF_PENDING:
+            # the server released the record when it handed the result out
+            if raise_on_error and job.result["status"] != LETKF_OK:
+                raise LetkfError(job.result["status"], f"server job {job.id}")
+            return job.result
         r = JobResult()
         st = _L().letkf_server_wait(self.h, job.id, -1.0 if timeout is None else float(timeout), C.byref(r))
         job.result = {"status": int(r.status), "t_submit": r.t_submit, "t_start": r.t_start, "t_done": r.t_done,

@@ -32,6 +32,8 @@ OPT_TC_POLISH = 10
 OPT_TC_SCALE_BOUND = 11
 OPT_POLISH_PROBE = 12
 OPT_NS_COND = 13
+OPT_MAX_NOBS_PER_GRID = 14
+OPT_FAULT_WAIT = 15
 
 
 class SweepDesc(C.Structure):
@@ -55,6 +57,9 @@ _SIGS = {
     "letkf_sweep_deferred": [C.c_void_p, C.c_void_p],
     "letkf_sweep_sorted_obs": [C.c_void_p, C.c_void_p],
     "letkf_sweep_device_buffers": [C.c_void_p] * 5,
+    "letkf_sweep_set_obs_groups": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int],
+    "letkf_sweep_set_probe": [C.c_void_p, C.c_int, C.c_void_p, C.c_int],
+    "letkf_sweep_get_probe": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
 }
 
 
@@ -115,6 +120,31 @@ class Sweep:
         self._keep = args
         check(_L().letkf_sweep_set_obs(self.h, int(len(args[0])), *[_p(x) for x in args], _p(vl),
                                        0 if vl is None else vl.size, _p(hd), int(f32)), "set_obs")
+
+    def set_obs_groups(self, uid, typ, nid, ntyp):
+        """Element uid (1..nid) and type (1..ntyp) of each observation of the
+        last set_obs, in its input order: the groups of MAX_NOBS_PER_GRID."""
+        u = np.ascontiguousarray(uid, dtype=np.int32)
+        t = np.ascontiguousarray(typ, dtype=np.int32)
+        check(_L().letkf_sweep_set_obs_groups(self.h, _p(u), _p(t), int(nid), int(ntyp)), "set_obs_groups")
+
+    def set_probe(self, points, cap):
+        """Record, in the next runs, what the fused search accepts for these
+        grid points (up to cap entries each); empty points switch it off."""
+        pts = np.ascontiguousarray(points, dtype=np.int32)
+        self._probe = (pts.size, int(cap))
+        check(_L().letkf_sweep_set_probe(self.h, int(pts.size), _p(pts) if pts.size else None, int(cap)),
+              "set_probe")
+
+    def probe(self):
+        """(count [n], obs [n, cap] input-order indices (-1 past the count),
+        rloc [n, cap] float32) of the probed points after a run."""
+        n, cap = self._probe
+        cnt = np.empty(n, dtype=np.int32)
+        obs = np.empty((n, cap), dtype=np.int32)
+        rl = np.empty((n, cap), dtype=np.float32)
+        check(_L().letkf_sweep_get_probe(self.h, _p(cnt), _p(obs), _p(rl)), "get_probe")
+        return cnt, obs, rl
 
     def set_background(self, xb):
         xb = np.ascontiguousarray(xb, dtype=self.dtype)

@@ -160,6 +160,12 @@ int oracle_scale_sweep(const oracle_scale_obs* o, const double* hdxf, const doub
                        const double* prz, const double* xb, double* xa, double* infl, int* nobsl_out,
                        double minfl, int nthreads);
 
+/* obs_local of npts points (OpenMP over points): cnt[p] = nobsl and the first
+ * min(nobsl, cap) sorted indices and rloc in rows of cap entries */
+int oracle_scale_obs_local_batch(const oracle_scale_obs* o, int npts, const double* pri, const double* prj,
+                                 const double* prlev, const double* prz, int cap, int* cnt, int* idx_out,
+                                 double* rloc_out, int nthreads);
+
 /* relax_beta / RTPP / RTPS (scale/letkf/letkf_tools.f90:1182-1268) */
 void oracle_weight_rtpp(int ne, const double* w, double alpha, double* wrlx);
 void oracle_weight_rtps(int ne, const double* w, const double* pa, const double* xb, double alpha,

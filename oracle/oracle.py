@@ -13,14 +13,18 @@ import numpy as np
 
 from . import build as _build
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
+def lib(timed=False):
+    """The parity build (every operation rounded on its own, -O2), or with
+    timed=True the build the CPU baseline is timed with (-O3, FMA contraction
+    allowed); both export the same functions."""
+    _lib = _libs.get(bool(timed))
     if _lib is None:
-        path = _build.build()
+        path = _build.build(timed=bool(timed))
         _lib = C.CDLL(path)
+        _libs[bool(timed)] = _lib
         d = C.c_double
         pd = C.POINTER(C.c_double)
         pi = C.POINTER(C.c_int)
@@ -59,6 +63,8 @@ def lib():
         _lib.oracle_scale_sweep.restype = C.c_int
         _lib.oracle_scale_sweep.argtypes = [C.c_void_p, pd, pd, C.c_int, C.c_int, C.c_int, pi, C.c_int, pd, pd, pd,
                                             pd, pd, pd, pd, pi, d, C.c_int]
+        _lib.oracle_scale_obs_local_batch.argtypes = [C.c_void_p, C.c_int, pd, pd, pd, pd, C.c_int, pi, pi, pd,
+                                                      C.c_int]
         _lib.oracle_weight_rtpp.argtypes = [C.c_int, pd, d, pd]
         _lib.oracle_weight_rtps.argtypes = [C.c_int, pd, pd, pd, d, pd, pd]
         _lib.oracle_obs_analysis.restype = d
@@ -268,10 +274,11 @@ class ScaleObs:
                            p["sigma_obsv_tc"], None if k[10] is None else k[10].ctypes.data,
                            int(max_nobs_per_grid))
 
-    def sweep(self, hdxf, dep, xb, pri, prj, prlev, infl, prz=None, subset=None, minfl=0.0, nthreads=0):
+    def sweep(self, hdxf, dep, xb, pri, prj, prlev, infl, prz=None, subset=None, minfl=0.0, nthreads=0, timed=False):
         """SCALE grid loop (oracle_scale_sweep).  hdxf (nobs, ne) and dep in
         sorted order; xb (nv, npts, ne).  Returns (xa, infl, nobsl); with a
-        subset only those points' entries are meaningful."""
+        subset only those points' entries are meaningful.  timed=True runs the
+        -O3 build the CPU baseline is timed with (results equal to rounding)."""
         hdxf = _f64(hdxf)
         xb = _f64(xb)
         nv, npts, ne = xb.shape
@@ -279,13 +286,26 @@ class ScaleObs:
         infl = np.array(infl, dtype=np.float64).copy()
         nobsl = np.zeros(npts, dtype=np.int32)
         sub = None if subset is None else np.ascontiguousarray(subset, dtype=np.int32)
-        bad = lib().oracle_scale_sweep(C.byref(self.s), _pd(hdxf), _pd(_f64(dep)), ne, nv, npts, _pi(sub),
+        bad = lib(timed).oracle_scale_sweep(C.byref(self.s), _pd(hdxf), _pd(_f64(dep)), ne, nv, npts, _pi(sub),
                                        0 if sub is None else sub.size, _pd(_f64(pri)), _pd(_f64(prj)),
                                        _pd(_f64(prlev)), None if prz is None else _pd(_f64(prz)), _pd(xb), _pd(xa),
                                        _pd(infl), _pi(nobsl), float(minfl), int(nthreads))
         if bad:
             raise RuntimeError(f"oracle sweep: {bad} points failed")
         return xa, infl, nobsl
+
+    def obs_local_batch(self, ri, rj, rlev, rz=None, cap=4096, nthreads=0):
+        """obs_local of many points (OpenMP): (count [n], idx [n, cap] sorted
+        indices, -1 past the count; rloc [n, cap])."""
+        ri, rj, rlev = _f64(ri), _f64(rj), _f64(rlev)
+        n = ri.size
+        cnt = np.zeros(n, dtype=np.int32)
+        idx = np.full((n, cap), -1, dtype=np.int32)
+        rloc = np.zeros((n, cap))
+        lib().oracle_scale_obs_local_batch(C.byref(self.s), n, _pd(ri), _pd(rj), _pd(rlev),
+                                           None if rz is None else _pd(_f64(rz)), int(cap), _pi(cnt), _pi(idx),
+                                           _pd(rloc), int(nthreads))
+        return cnt, idx, rloc
 
     def obs_local(self, ri, rj, rlev, rz=0.0):
         n = max(self.s.nobs, 1)

@@ -19,9 +19,12 @@ def _close(a, b, rtol):
     assert err <= rtol, f"relative error {err:.3e} > {rtol:.1e}"
 
 
-# ------------------------------------------------------------------- host (CPU)
+# ------------------------------------------------------ bucket sort (device)
+@pytest.mark.gpu
 @pytest.mark.parametrize("seed", [0, 1, 2])
-def test_speedy_sort_matches_oracle(seed):
+def test_speedy_sort_matches_oracle(cuda, seed):
+    """The device bucket sort (letkf_sort_obs_latlon) equals the oracle's
+    restatement of speedy/letkf/letkf_obs.f90:243-313: order and nobsgrd."""
     c = S.speedy_case(seed, nstations=150)
     # observations exactly on grid lines, next to 360, and outside the last band
     olon = np.concatenate([c["olon"], c["lon"][:6], [359.999999, 0.0, 360.0 - 1e-12]])
@@ -32,10 +35,31 @@ def test_speedy_sort_matches_oracle(seed):
     np.testing.assert_array_equal(g1, g2)
 
 
-def test_speedy_sort_empty():
+@pytest.mark.gpu
+def test_speedy_sort_empty(cuda):
     lon, lat = S.speedy_grid()
     p, g = speedy_sort_obs(lon, lat, np.zeros(0), np.zeros(0))
     assert p.size == 0 and not g.any()
+
+
+@pytest.mark.gpu
+def test_speedy_sort_selects_qc_on_the_device(cuda):
+    """With qc the device sort keeps only qc == 1 (set_letkf_obs's selection
+    before the sort): equal to the oracle sort of the selected subset."""
+    import torch
+
+    from letkf_gb300.core import sort_obs_latlon
+
+    c = S.speedy_case(7, nstations=400)
+    rng = np.random.default_rng(3)
+    qc = (rng.uniform(size=c["olon"].size) < 0.8).astype(np.int32)
+    f = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device=cuda)
+    perm, grd = sort_obs_latlon(f(c["lon"]), f(c["lat"]), f(c["olon"]), f(c["olat"]),
+                                torch.as_tensor(qc, device=cuda))
+    keep = np.nonzero(qc == 1)[0]
+    p2, g2 = O.speedy_sort_obs(c["lon"], c["lat"], c["olon"][keep], c["olat"][keep])
+    np.testing.assert_array_equal(perm.cpu().numpy(), keep[p2])
+    np.testing.assert_array_equal(grd.cpu().numpy(), g2)
 
 
 def test_var_local_n2n():
