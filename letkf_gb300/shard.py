@@ -121,4 +121,56 @@ def gather_points(values, points, npts_total, group=None):
     return out
 
 
-__all__ = ["rank_grid", "tile_of", "tile_points", "obs_cells", "halo_mask", "exchange_obs", "gather_points"]
+class RankLost(RuntimeError):
+    """A rank of the decomposition left or did not arrive for a cycle."""
+
+    def __init__(self, step, missing, left):
+        self.step, self.missing, self.left = step, sorted(missing), sorted(left)
+        super().__init__(f"cycle {step}: ranks {self.missing} did not arrive (left: {self.left})")
+
+
+class CycleGuard:
+    """Host-side liveness check between the cycles of a decomposed analysis.
+
+    The reference has no failure detection: an error anywhere stops the MPI
+    job (STOP 2 in common/common_mtx.f90:61-64,75-78, STOP 99 in
+    scale/letkf/letkf_tools.f90:1159-1163).  Here every rank calls
+    ``enter(step)`` before it launches the step's work: it marks itself as
+    present in a key-value store (a ``torch.distributed`` TCPStore, hosted by a
+    rank that stays, normally rank 0) and waits, at most ``timeout`` seconds,
+    for the other ranks' marks.  A rank that leaves between cycles calls
+    ``leave()``; the others then learn of it at once, and of a rank that simply
+    stops arriving after the timeout.  Either way ``enter`` raises
+    ``RankLost`` before any device work or collective of that step is issued,
+    so no rank waits in a collective for a peer that is gone."""
+
+    def __init__(self, store, rank, world, timeout=2.0, prefix="letkf/guard"):
+        self.store, self.rank, self.world = store, int(rank), int(world)
+        self.timeout, self.prefix = float(timeout), prefix
+
+    def _key(self, what, r):
+        return f"{self.prefix}/{what}/r{r}"
+
+    def _left(self):
+        return [r for r in range(self.world) if r != self.rank and self.store.check([self._key("left", r)])]
+
+    def enter(self, step):
+        import datetime
+
+        self.store.set(self._key(f"step{step}", self.rank), "1")
+        left = self._left()
+        if left:
+            raise RankLost(step, left, left)
+        keys = [self._key(f"step{step}", r) for r in range(self.world)]
+        try:
+            self.store.wait(keys, datetime.timedelta(seconds=self.timeout))
+        except RuntimeError:  # the store's timeout error
+            missing = [r for r in range(self.world) if not self.store.check([keys[r]])]
+            raise RankLost(step, missing, self._left()) from None
+
+    def leave(self):
+        self.store.set(self._key("left", self.rank), "1")
+
+
+__all__ = ["rank_grid", "tile_of", "tile_points", "obs_cells", "halo_mask", "exchange_obs", "gather_points",
+           "CycleGuard", "RankLost"]

@@ -124,3 +124,75 @@ def test_sharded_sweep_equals_single_domain(world):
         np.testing.assert_array_equal(got["nobsl"], nobsl)
         np.testing.assert_array_equal(got["infl"], infl)
         np.testing.assert_array_equal(got["xa"], xa)
+
+
+# ------------------------------------------------------------ failure detection
+def _guard_main(rank, world, port, sport, out_dir, mode):
+    """Cycle 0 runs on every rank; then rank world-1 leaves (mode "leave":
+    announces it; mode "vanish": just exits) between cycles, with no device
+    work or collective in flight.  The others must learn of it in their
+    guard before cycle 1's work and exit cleanly instead of hanging."""
+    import datetime
+    import json
+
+    import torch.distributed as dist
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=20))
+    store = dist.TCPStore("127.0.0.1", sport, world, is_master=(rank == 0),
+                          timeout=datetime.timedelta(seconds=20))
+    guard = shard.CycleGuard(store, rank, world, timeout=1.5)
+    result = {"rank": rank}
+    try:
+        case = _case()
+        prm = S.scale_params(case)
+        tile = shard.tile_of(rank, world, case["nlon"], case["nlat"])
+        guard.enter(0)
+        nobs = case["ri"].size
+        uid = np.arange(nobs)
+        mine = uid % world == rank
+        local = {"uid": uid[mine], "ri": case["ri"][mine], "rj": case["rj"][mine]}
+        halo = shard.exchange_obs(local, tile, case["nlon"], case["nlat"], prm["dlon_zero"], prm["dlat_zero"])
+        result["cycle0_halo"] = int(halo["uid"].size)
+        if rank == world - 1:
+            if mode == "leave":
+                guard.leave()
+            result["left"] = True
+        else:
+            try:
+                guard.enter(1)
+                result["cycle1"] = "entered"
+            except shard.RankLost as e:
+                result["cycle1"] = "rank lost"
+                result["missing"] = e.missing
+                result["announced"] = e.left
+        store.set(f"done/r{rank}", "1")
+        if rank == 0:  # the store's host stays until the others are done with it
+            store.wait([f"done/r{r}" for r in range(world - 1)], datetime.timedelta(seconds=20))
+    finally:
+        with open(os.path.join(out_dir, f"r{rank}.json"), "w") as f:
+            json.dump(result, f)
+        dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("mode", ["leave", "vanish"])
+def test_ranks_learn_that_a_rank_left_between_cycles(mode):
+    import json
+    import time
+
+    import torch.multiprocessing as mp
+
+    world = 3
+    with tempfile.TemporaryDirectory() as d:
+        t0 = time.time()
+        mp.spawn(_guard_main, args=(world, _free_port(), _free_port(), d, mode), nprocs=world, join=True)
+        took = time.time() - t0
+        res = [json.load(open(os.path.join(d, f"r{r}.json"))) for r in range(world)]
+    assert res[world - 1].get("left")
+    for r in range(world - 1):
+        assert res[r]["cycle1"] == "rank lost", res[r]
+        assert res[r]["missing"] == [world - 1]
+        assert res[r]["announced"] == ([world - 1] if mode == "leave" else [])
+        assert res[r]["cycle0_halo"] > 0
+    assert took < 60
