@@ -79,7 +79,10 @@ def parse():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
     ap.add_argument("--no-largek", action="store_true", help="skip the large-ensemble measurement")
     ap.add_argument("--no-configs", action="store_true", help="skip the Lorenz-96 and SPEEDY-grid parity lines")
-    ap.add_argument("--largek-points", type=int, default=4096, help="sampled points of the large-ensemble sweep")
+    ap.add_argument("--largek-points", type=int, default=4096,
+                    help="sampled points of the large-ensemble sweep at 60 km")
+    ap.add_argument("--largek-700-points", type=int, default=256,
+                    help="sampled points of the large-ensemble sweep at the stated 700 km")
     ap.add_argument("--serve-requests", type=int, default=48, help="requests of the serving measurement")
     ap.add_argument("--serve-slots", type=int, default=3, help="jobs on the device at once")
     ap.add_argument("--serve-load", type=float, default=0.7,
@@ -419,79 +422,110 @@ def run_configs(args, dev):
 
 
 def run_largek(args, dev):
-    """Large-ensemble configuration on a sample of its points: 360x181x32
-    global grid, 6 variables, k = 512, 3e6 observations, SPEEDY lat/lon
-    search.  One step = search (count + fill), gather of the local rows, the
-    large-k core and the FP32 update of the 6 variables for the sampled
-    points; plus the analysis error of 16 points against the FP64 oracle.
-    sigma_h = 60 km keeps the local counts in the O(1e2-1e3) range."""
+    """Large-ensemble configuration on samples of its points: 360x181x32
+    global grid, 6 variables, k = 512 members stored BF16 (FP32 mean + BF16
+    perturbations for the background and the analysis; BF16 obs-space
+    perturbations), 3e6 observations, SPEEDY lat/lon search.  One step =
+    search (count + fill), the large-k core over the search's index lists
+    (no packed copies of the rows) and the BF16-storage update of the 6
+    variables.  Two localisations: the stated 700 km (about 7e4 local
+    observations per point) and 60 km (O(1e2-1e3), the range the hot-path
+    scope names), each with its error against the FP64 oracle on a subset of
+    the sampled points (same stored inputs)."""
     import torch
 
-    from letkf_gb300.core import core_batch_largek, gather_rows, search_speedy, update_mixed
+    from letkf_gb300.core import (core_batch_largek_indexed, search_speedy, update_bf16, update_mixed)
     from letkf_gb300.workload import GlobalWorkload
+    from oracle import oracle as O
 
     wl = GlobalWorkload(21)
     hdxf, dep, dat = wl.obs_torch(dev)
-    rng = np.random.default_rng(5)
-    idx = np.sort(rng.choice(wl.npts, args.largek_points, replace=False))
-    lon, lat, dlon, ilev, lnp = wl.points(idx)
+    hdxf16 = hdxf.to(torch.bfloat16)
+    del hdxf
+    dep32 = dep.to(torch.float32)
     f = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
     grid = {"lon": f(wl.lon), "lat": f(wl.lat), "nobsgrd": torch.as_tensor(wl.nobsgrd, dtype=torch.int32, device=dev)}
     obs = {"elm": f(wl.elm), "lon": f(wl.olon), "lat": f(wl.olat), "lev": f(wl.olev), "dat": dat, "err": f(wl.err)}
-    pts = {"lon": f(lon), "lat": f(lat), "dlon_zero": f(dlon), "ilev": torch.as_tensor(ilev, device=dev),
-           "logpfm": f(lnp)}
-    xb = wl.background_torch(dev, idx)
     vl = np.ones(7)
-    infl0 = torch.full((idx.size,), 1.05, dtype=torch.float64, device=dev)
+    out = {"storage": "background and analysis: FP32 mean + BF16 perturbations; obs-space perturbations BF16",
+           "workload": f"global {wl.nlon}x{wl.nlat}x{wl.nlev}, {wl.nvar} vars, k={wl.ne}, {wl.nobs} obs, "
+                       f"sigma_v={wl.sigma_obsv} ln p (SPEEDY lat/lon search)"}
+    for sigma, npts_s, nerr in ((700.0e3, args.largek_700_points, 8), (60.0e3, args.largek_points, 256)):
+        params = wl.search_params(sigma)
+        rng = np.random.default_rng(5)
+        idx = np.sort(rng.choice(wl.npts, npts_s, replace=False))
+        lon, lat, dlon, ilev, lnp = wl.points(idx, params)
+        pts = {"lon": f(lon), "lat": f(lat), "dlon_zero": f(dlon), "ilev": torch.as_tensor(ilev, device=dev),
+               "logpfm": f(lnp)}
+        xb = wl.background_torch(dev, idx)
+        xmean = xb.double().mean(-1).to(torch.float32)
+        xpert16 = (xb - xmean[..., None]).to(torch.bfloat16)
+        del xb
+        infl0 = torch.full((idx.size,), 1.05, dtype=torch.float64, device=dev)
 
-    def step():
-        offs, oi, rloc, rdiag = search_speedy(grid, obs, pts, wl.params, vl)
-        rows, dl = gather_rows(oi, hdxf, dep.to(torch.float32))
-        infl = infl0.clone()
-        out = core_batch_largek(wl.ne, offs, rows, rdiag.to(torch.float32), rloc.to(torch.float32), dl, infl,
-                                want_transm=True)
-        xa = update_mixed(xb, out["trans"], out["transm"])
-        return offs, oi, rloc, rdiag, rows, dl, out, xa
+        def step():
+            offs, oi, rloc, rdiag = search_speedy(grid, obs, pts, params, vl)
+            infl = infl0.clone()
+            core = core_batch_largek_indexed(wl.ne, offs, oi, hdxf16, dep32, rdiag.to(torch.float32),
+                                             rloc.to(torch.float32), infl, want_transm=True)
+            am, ap = update_bf16(xmean, xpert16, core["trans"], core["transm"])
+            return offs, oi, rloc, rdiag, core, am, ap
 
-    step()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    offs, oi, rloc, rdiag, rows, dl, out, xa = step()
-    e1.record()
-    torch.cuda.synchronize()
-    t = e0.elapsed_time(e1) / 1e3
-    nl = np.diff(offs.cpu().numpy())
-    status = out["status"].cpu().numpy()
-    # FP64 oracle on a few points (the same float32 rows and weights)
-    from oracle import oracle as O
-
-    sub = np.arange(0, idx.size, max(1, idx.size // 16))[:16]
-    o = offs.cpu().numpy()
-    R = rows.double().cpu().numpy()
-    rd_, rl_, d_ = (x.double().cpu().numpy() for x in (rdiag.to(torch.float32), rloc.to(torch.float32), dl))
-    so = np.concatenate([[0], np.cumsum(nl[sub])]).astype(np.int64)
-    sel = np.concatenate([np.arange(o[p], o[p + 1]) for p in sub]) if nl[sub].sum() else np.zeros(0, np.int64)
-    ref = O.letkf_core_batch(wl.ne, so, R[sel] if sel.size else np.zeros((1, wl.ne)), rd_[sel] if sel.size else
-                             np.ones(1), rl_[sel] if sel.size else np.ones(1), d_[sel] if sel.size else np.zeros(1),
-                             np.full(sub.size, 1.05), want_transm=True)
-    x64 = xb[:, sub, :].double().cpu().numpy()
-    xp = x64 - x64.mean(-1, keepdims=True)
-    want = x64.mean(-1, keepdims=True) + np.einsum("vpk,pmk->vpm", xp, ref["trans"] + ref["transm"][:, None, :])
-    got = xa[:, sub, :].double().cpu().numpy()
-    spread = np.sqrt((xp ** 2).sum(-1) / (wl.ne - 1)).mean()
-    em = float(np.sqrt(np.mean((got.mean(-1) - want.mean(-1)) ** 2)) / spread)
-    pert = lambda x: x - x.mean(-1, keepdims=True)
-    ep = float(np.sqrt(np.mean((pert(got) - pert(want)) ** 2)) / spread)
-    return {"workload": f"global {wl.nlon}x{wl.nlat}x{wl.nlev}, {wl.nvar} vars, k={wl.ne}, {wl.nobs} obs, "
-                        f"sigma_h={wl.sigma_obs:.0f} m, sigma_v={wl.sigma_obsv} ln p (SPEEDY lat/lon search)",
-            "sample_points": int(idx.size), "value": idx.size / t, "unit": UNIT, "ms_per_sample": t * 1e3,
-            "step": "search + gather + large-k core (tensor-core Gram and Newton-Schulz) + FP32 update, CUDA events",
-            "local_obs": {"min": int(nl.min()), "mean": float(nl.mean()), "p50": float(np.median(nl)),
-                          "max": int(nl.max())},
-            "status_ok": int((status == 0).sum()),
-            "error_vs_fp64_oracle": {"analysis_mean_rms_over_spread": em, "perturbation_rms_over_spread": ep,
-                                     "points": int(sub.size), "target": 1e-4}}
+        step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        offs, oi, rloc, rdiag, core, am, ap = step()
+        e1.record()
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3
+        nl = np.diff(offs.cpu().numpy())
+        status = core["status"].cpu().numpy()
+        # FP64 oracle (the same stored BF16 rows, FP32 weights) on a subset
+        sub = np.arange(0, idx.size, max(1, idx.size // nerr))[:nerr]
+        o = offs.cpu().numpy()
+        sel = np.concatenate([np.arange(o[p], o[p + 1]) for p in sub]) if nl[sub].sum() else np.zeros(0, np.int64)
+        obs_rows = oi.cpu().numpy()[sel]
+        R = hdxf16[torch.as_tensor(obs_rows, device=dev, dtype=torch.int64)].double().cpu().numpy() if sel.size \
+            else np.zeros((1, wl.ne))
+        rd_ = rdiag.to(torch.float32).double().cpu().numpy()[sel] if sel.size else np.ones(1)
+        rl_ = rloc.to(torch.float32).double().cpu().numpy()[sel] if sel.size else np.ones(1)
+        d_ = dep32.double().cpu().numpy()[obs_rows] if sel.size else np.zeros(1)
+        so = np.concatenate([[0], np.cumsum(nl[sub])]).astype(np.int64)
+        tc0 = time.perf_counter()
+        ref = O.letkf_core_batch(wl.ne, so, R, rd_, rl_, d_, np.full(sub.size, 1.05), want_transm=True)
+        t_oracle = time.perf_counter() - tc0
+        xs = torch.as_tensor(sub, device=dev)
+        x64 = (xmean[:, xs, None].double() + xpert16[:, xs, :].double()).cpu().numpy()
+        xp = x64 - x64.mean(-1, keepdims=True)
+        want = x64.mean(-1, keepdims=True) + np.einsum("vpk,pmk->vpm", xp, ref["trans"] + ref["transm"][:, None, :])
+        spread = np.sqrt((xp ** 2).sum(-1) / (wl.ne - 1)).mean()
+        pert = lambda x: x - x.mean(-1, keepdims=True)
+        got_mean = am[:, xs].double().cpu().numpy()
+        em = float(np.sqrt(np.mean((got_mean - want.mean(-1)) ** 2)) / spread)
+        got_p16 = ap[:, xs, :].double().cpu().numpy()
+        ep16 = float(np.sqrt(np.mean((got_p16 - pert(want)) ** 2)) / spread)
+        # the same transforms through the FP32 update: the computation's own error
+        xa32 = update_mixed((xmean[:, xs, None] + xpert16[:, xs, :].float()).contiguous(), core["trans"][xs],
+                            core["transm"][xs]).double().cpu().numpy()
+        ep32 = float(np.sqrt(np.mean((pert(xa32) - pert(want)) ** 2)) / spread)
+        key = f"sigma_{sigma / 1e3:.0f}km"
+        out[key] = {"sigma_h_m": sigma, "sample_points": int(idx.size), "value": idx.size / t, "unit": UNIT,
+                    "ms_per_sample": t * 1e3,
+                    "step": "search + large-k core over the index lists (tensor-core Gram and Newton-Schulz) + "
+                            "BF16-storage update, CUDA events",
+                    "local_obs": {"min": int(nl.min()), "mean": float(nl.mean()), "p50": float(np.median(nl)),
+                                  "max": int(nl.max())},
+                    "status_ok": int((status == 0).sum()),
+                    "status_counts": {str(int(k)): int(v) for k, v in zip(*np.unique(status, return_counts=True))},
+                    "error_vs_fp64_oracle": {"analysis_mean_rms_over_spread": em,
+                                             "perturbation_rms_over_spread_bf16_stored": ep16,
+                                             "perturbation_rms_over_spread_fp32_update": ep32,
+                                             "points": int(sub.size), "oracle_seconds": round(t_oracle, 1),
+                                             "target": 1e-4}}
+        del offs, oi, rloc, rdiag, core, am, ap, xpert16, xmean
+        torch.cuda.empty_cache()
+    return out
 
 
 def check_lists(sw, so, wl, idx, cap, stream, nthreads, chunk=16384):

@@ -92,6 +92,28 @@ int letkf_core_batch_largek(int ne, int npts, const int64_t* offs, const float* 
                             double* parm_infl, float* trans, float* transm, int rdiag_wloc,
                             double minfl, int* status, void* stream);
 
+/* The large-ensemble core over the index lists of a local search, without
+ * packed copies of the rows: point p's local observations are idx[offs[p]]
+ * .. idx[offs[p+1]-1] (the search's output), their rows are ens_obs[idx[l]]
+ * ([nobs][ne]: FP32, or BF16 when ens_bf16) and their departures
+ * dep_obs[idx[l]]; rdiag, rloc are per list entry.  Otherwise as
+ * letkf_core_batch_largek.  With BF16 rows the Gram's operands are exact
+ * BF16 values weighted in FP32. */
+int letkf_core_batch_largek_indexed(int ne, int npts, const int64_t* offs, const int* idx, const void* ens_obs,
+                                    int ens_bf16, const float* dep_obs, const float* rdiag, const float* rloc,
+                                    double* parm_infl, float* trans, float* transm, int rdiag_wloc, double minfl,
+                                    int* status, void* stream);
+
+/* Ensemble update with BF16 storage (ne <= 512, nv <= 8): each member is
+ * xmean [nv][npts] (FP32) plus its perturbation xpert [nv][npts][ne] (BF16);
+ * the analysis is written the same way: amean = mean + xb' transm (FP64
+ * sums) and apert = xb' trans (FP32 products, rounded to BF16), with xb' the
+ * stored perturbations minus their mean.  The mean stays FP32 because BF16
+ * values (8-bit mantissa) cannot hold a field's mean to a small fraction of
+ * its spread. */
+int letkf_update_bf16(int ne, int npts, int nv, const float* xmean, const void* xpert, const float* trans,
+                      const float* transm, float* amean, void* apert, void* stream);
+
 /* FP32 ensemble update for any ne <= 512: xb, xa [nv][npts][ne] float32,
  * trans [npts][ne*ne] column-major, transm [npts][ne] or NULL; FP32 products,
  * FP64 mean and mean increment (nv <= 8). */
@@ -383,7 +405,8 @@ int letkf_l96_obs_cell(int nx, int ny, const double* h, int* cell, void* stream)
 #define LETKF_OPT_EIGENSOLVER 3 /* transform of the mixed form: */
 #define LETKF_EIG_NEWTON_SCHULZ 0 /*   W = sqrt((k-1)) A^(-1/2) by Newton-Schulz (default) */
 #define LETKF_EIG_JACOBI 1        /*   eigen-decomposition by parallel Jacobi */
-#define LETKF_OPT_TENSOR_CORES 4  /* 1 (default): Gram and Newton-Schulz on tcgen05 for ne <= 64 */
+#define LETKF_OPT_TENSOR_CORES 4  /* 1 (default): Gram and Newton-Schulz on tcgen05 for ne <= 128 (ne <= 64:
+                                     four CTAs per SM; 64 < ne <= 128: one CTA of 256 threads per SM) */
 #define LETKF_OPT_TC_NS_ITERS 5   /* tensor-core Newton-Schulz iterations before the FP32 ones (default 14) */
 #define LETKF_OPT_TC_NS_SCALING 6 /* 1 (default): spectrum-scaled tensor-core Newton-Schulz steps; 0: plain */
 #define LETKF_OPT_TC_NS_TOL 7     /* v: the tensor-core phase ends once ||ZY - I||_F^2 < 10^-v (1..7, default 3) */
@@ -401,6 +424,8 @@ int letkf_l96_obs_cell(int nx, int ny, const double* h, int* cell, void* stream)
                                       with the groups of letkf_sweep_set_obs_groups; the run then searches each piece
                                       of the processing order first (letkf_search_scale_limited) and analyses it from
                                       the lists (no CUDA graph); 0 (default): no limit */
+#define LETKF_OPT_GRID_SHARE 16    /* v >= 1: each persistent sweep launch takes 1/v of the CTAs its kernel can keep
+                                      resident (the server's slots share the SMs this way); replaces a grid cap */
 #define LETKF_OPT_FAULT_WAIT 15    /* failure injection, v > 0: the next mixed-form runs on the tensor-core sweep
                                       wait on a barrier that nothing arrives at and give up after v polls, so the
                                       run reports LETKF_ERR_TIMEOUT and analyses nothing; 0 (default): off */

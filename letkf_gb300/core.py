@@ -132,6 +132,41 @@ def core_batch_largek(ne, offs, rows, rdiag, rloc, dep, parm_infl, want_transm=F
     return dict(trans=trans, transm=tm, status=status, parm_infl=parm_infl)
 
 
+def core_batch_largek_indexed(ne, offs, idx, ens_obs, dep_obs, rdiag, rloc, parm_infl, want_transm=False,
+                              rdiag_wloc=False, minfl=0.0, stream=None):
+    """Large-ensemble core over a search's index lists (letkf_core_batch_largek_indexed):
+    offs int64 [npts+1], idx int32 [nrows] (observation of each entry),
+    ens_obs [nobs, ne] float32 or bfloat16, dep_obs float32 [nobs], rdiag and
+    rloc float32 [nrows], parm_infl float64 (in place)."""
+    import torch
+
+    npts = offs.numel() - 1
+    dev = ens_obs.device
+    trans = torch.empty((npts, ne, ne), dtype=torch.float32, device=dev)
+    tm = torch.empty((npts, ne), dtype=torch.float32, device=dev) if want_transm else None
+    status = torch.empty(npts, dtype=torch.int32, device=dev)
+    bf = ens_obs.dtype == torch.bfloat16
+    st = lib().letkf_core_batch_largek_indexed(ne, npts, _dptr(offs), _dptr(idx), _dptr(ens_obs), int(bf),
+                                               _dptr(dep_obs), _dptr(rdiag), _dptr(rloc), _dptr(parm_infl),
+                                               _dptr(trans), _dptr(tm), int(bool(rdiag_wloc)), float(minfl),
+                                               _dptr(status), _stream(stream))
+    check(st, "letkf_core_batch_largek_indexed")
+    return dict(trans=trans, transm=tm, status=status, parm_infl=parm_infl)
+
+
+def update_bf16(xmean, xpert, trans, transm=None, stream=None):
+    """Update with BF16 storage (letkf_update_bf16): xmean float32 [nv, npts],
+    xpert bfloat16 [nv, npts, ne]; returns (amean float32, apert bfloat16)."""
+    import torch
+
+    nv, npts, ne = xpert.shape
+    amean = torch.empty_like(xmean)
+    apert = torch.empty_like(xpert)
+    check(lib().letkf_update_bf16(ne, npts, nv, _dptr(xmean), _dptr(xpert), _dptr(trans), _dptr(transm),
+                                  _dptr(amean), _dptr(apert), _stream(stream)), "letkf_update_bf16")
+    return amean, apert
+
+
 def update_mixed(xb, trans, transm=None, stream=None):
     """FP32 update for any ne <= 512: xb float32 [nv, npts, ne], trans float32
     [npts, ne, ne] column-major per point; returns xa like xb."""

@@ -56,6 +56,8 @@ __global__ void lk_weights_kernel(int64_t n, const float* __restrict__ rdiag, co
 // per point: p1, p3, b = Ywᵀ dep, trace, branch, A = G + cI, s, Y0, Z0
 __global__ void __launch_bounds__(LKP_NT) lk_prep_kernel(int ne, int kp, const int64_t* __restrict__ offs,
                                                           const float* __restrict__ rows,
+                                                          const __nv_bfloat16* __restrict__ rows16,
+                                                          const int* __restrict__ ridx,
                                                           const float* __restrict__ w,
                                                           const float* __restrict__ dep,
                                                           const float* __restrict__ rloc, const double* infl_in,
@@ -79,9 +81,12 @@ __global__ void __launch_bounds__(LKP_NT) lk_prep_kernel(int ne, int kp, const i
     for (int i = 0; i < LKP_NT / 32; i++) t += red[i];
     return t;
   };
+  // list entry e: its row (packed, or observation ridx[e]) and departure
+  auto row_of = [&](int64_t e) -> size_t { return ridx ? (size_t)ridx[e] : (size_t)e; };
+  auto dep_of = [&](int64_t e) -> float { return dep[row_of(e)]; };
   double p1 = 0.0, p3 = 0.0;
   for (int l = tid; l < L; l += LKP_NT) {
-    const double d = dep[r0 + l];
+    const double d = dep_of(r0 + l);
     p1 += d * d * (double)w[r0 + l];
     p3 += (double)rloc[r0 + l];
   }
@@ -89,8 +94,13 @@ __global__ void __launch_bounds__(LKP_NT) lk_prep_kernel(int ne, int kp, const i
   p3 = bsum(p3);
   for (int m = tid; m < kp; m += LKP_NT) {
     float acc = 0.f;
-    if (m < ne)
-      for (int l = 0; l < L; l++) acc = fmaf(w[r0 + l] * dep[r0 + l], rows[(r0 + l) * ne + m], acc);
+    if (m < ne) {
+      if (rows16)
+        for (int l = 0; l < L; l++)
+          acc = fmaf(w[r0 + l] * dep_of(r0 + l), __bfloat162float(rows16[row_of(r0 + l) * ne + m]), acc);
+      else
+        for (int l = 0; l < L; l++) acc = fmaf(w[r0 + l] * dep_of(r0 + l), rows[row_of(r0 + l) * ne + m], acc);
+    }
     bvec[(size_t)b * kp + m] = acc;
   }
   double tr = 0.0;
@@ -391,9 +401,16 @@ __host__ __device__ constexpr int lku_base_floats(int nv, int ne) {
   return (nv * ne + LKU_KT * (ne + 1) + 1) & ~1;
 }
 
-__global__ void __launch_bounds__(LKP_NT) lk_update_kernel(int ne, int npts, int nv, const float* __restrict__ xb,
+// BF == false: xb, xa [nv][npts][ne] FP32 members.  BF == true: members
+// stored as an FP32 mean xmean [nv][npts] plus BF16 perturbations xb
+// [nv][npts][ne]; the analysis likewise (amean = mean + xb' transm in FP64,
+// xa = xb' trans rounded to BF16)
+template <bool BF>
+__global__ void __launch_bounds__(LKP_NT) lk_update_kernel(int ne, int npts, int nv, const void* __restrict__ xb_,
+                                                            const float* __restrict__ xmean,
                                                             const float* __restrict__ trans,
-                                                            const float* __restrict__ transm, float* xa) {
+                                                            const float* __restrict__ transm, void* xa_,
+                                                            float* amean) {
   extern __shared__ __align__(16) float su[];
   const int ld = ne + 1;                   // padded row of the staged tile (conflict-free columns)
   float* xs = su;                          // [nv][ne] perturbations
@@ -404,13 +421,15 @@ __global__ void __launch_bounds__(LKP_NT) lk_update_kernel(int ne, int npts, int
     __syncthreads();
     for (int t = tid; t < nv * ne; t += LKP_NT) {
       const int v = t / ne, m = t - v * ne;
-      xs[t] = xb[((size_t)v * npts + p) * ne + m];
+      const size_t at = ((size_t)v * npts + p) * ne + m;
+      xs[t] = BF ? __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(xb_)[at])
+                 : reinterpret_cast<const float*>(xb_)[at];
     }
     __syncthreads();
     for (int v = wid; v < nv; v += LKP_NT / 32) {
       double sx = 0.0;
       for (int m = lane; m < ne; m += 32) sx += (double)xs[v * ne + m];
-      const double mean = warp_sum(sx) / (double)ne;
+      const double mean = warp_sum(sx) / (double)ne;  // of the members (BF: of the stored perturbations)
       double dl = 0.0;
       for (int m = lane; m < ne; m += 32) {
         const float x = (float)((double)xs[v * ne + m] - mean);
@@ -418,7 +437,14 @@ __global__ void __launch_bounds__(LKP_NT) lk_update_kernel(int ne, int npts, int
         if (transm) dl += (double)x * (double)transm[(size_t)p * ne + m];
       }
       dl = warp_sum(dl);
-      if (lane == 0) base[v] = mean + dl;
+      if (lane == 0) {
+        if (BF) {
+          base[v] = 0.0;
+          amean[(size_t)v * npts + p] = (float)((double)xmean[(size_t)v * npts + p] + mean + dl);
+        } else {
+          base[v] = mean + dl;
+        }
+      }
     }
     float acc[8][2];
 #pragma unroll
@@ -451,9 +477,30 @@ __global__ void __launch_bounds__(LKP_NT) lk_update_kernel(int ne, int npts, int
       if (m >= ne) continue;
 #pragma unroll
       for (int v = 0; v < 8; v++)
-        if (v < nv) xa[((size_t)v * npts + p) * ne + m] = (float)(base[v] + (double)acc[v][h]);
+        if (v < nv) {
+          const size_t at = ((size_t)v * npts + p) * ne + m;
+          if (BF)
+            reinterpret_cast<__nv_bfloat16*>(xa_)[at] = __float2bfloat16_rn(acc[v][h]);
+          else
+            reinterpret_cast<float*>(xa_)[at] = (float)(base[v] + (double)acc[v][h]);
+        }
     }
   }
+}
+
+template <bool BF>
+static int launch_lk_update(int ne, int npts, int nv, const void* xb, const float* xmean, const float* trans,
+                            const float* transm, void* xa, float* amean, cudaStream_t stream) {
+  const size_t smem = sizeof(float) * (size_t)lku_base_floats(nv, ne) + sizeof(double) * 8;
+  cudaError_t e = cudaFuncSetAttribute(lk_update_kernel<BF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return cuda_status(e);
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int grid = npts < nsm * 4 ? npts : nsm * 4;
+  lk_update_kernel<BF><<<grid, LKP_NT, smem, stream>>>(ne, npts, nv, xb, xmean, trans, transm, xa, amean);
+  note_launch();
+  return cuda_status(cudaGetLastError());
 }
 
 template <int MODE>
@@ -481,21 +528,28 @@ extern "C" int letkf_update_mixed(int ne, int npts, int nv, const float* xb, con
     return LETKF_ERR_NOGPU;
   }
   if (npts == 0) return LETKF_OK;
-  const size_t smem = sizeof(float) * (size_t)lku_base_floats(nv, ne) + sizeof(double) * 8;
-  cudaError_t e = cudaFuncSetAttribute(lk_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return cuda_status(e);
-  int dev = 0, nsm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const int grid = npts < nsm * 4 ? npts : nsm * 4;
-  lk_update_kernel<<<grid, LKP_NT, smem, (cudaStream_t)stream>>>(ne, npts, nv, xb, trans, transm, xa);
-  note_launch();
-  return cuda_status(cudaGetLastError());
+  return launch_lk_update<false>(ne, npts, nv, xb, nullptr, trans, transm, xa, nullptr, (cudaStream_t)stream);
 }
 
-extern "C" int letkf_core_batch_largek(int ne, int npts, const int64_t* offs, const float* rows, const float* rdiag,
-                                       const float* rloc, const float* dep, double* parm_infl, float* trans,
-                                       float* transm, int rdiag_wloc, double minfl, int* status, void* stream) {
+extern "C" int letkf_update_bf16(int ne, int npts, int nv, const float* xmean, const void* xpert,
+                                 const float* trans, const float* transm, float* amean, void* apert, void* stream) {
+  if (ne < 2 || npts < 0 || nv < 1 || nv > 8 || !xmean || !xpert || !trans || !amean || !apert) return LETKF_ERR_ARG;
+  if (ne > 2 * LKP_NT) return LETKF_ERR_CAPACITY;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return LETKF_ERR_NOGPU;
+  }
+  if (npts == 0) return LETKF_OK;
+  return launch_lk_update<true>(ne, npts, nv, xpert, xmean, trans, transm, apert, amean, (cudaStream_t)stream);
+}
+
+// the large-ensemble core over packed rows (rows, dep per list entry) or over
+// index lists into the observation ensemble (ridx; FP32 rows or BF16 rows16,
+// dep per observation)
+static int largek_core(int ne, int npts, const int64_t* offs, const float* rows, const __nv_bfloat16* rows16,
+                       const int* ridx, const float* rdiag, const float* rloc, const float* dep, double* parm_infl,
+                       float* trans, float* transm, int rdiag_wloc, double minfl, int* status, void* stream) {
   if (ne < 2 || npts < 0 || !offs || !parm_infl || !trans || !status) return LETKF_ERR_ARG;
   if (ne > LETKF_LARGEK_MAX_NE) return LETKF_ERR_CAPACITY;
   int ndev = 0;
@@ -552,17 +606,21 @@ extern "C" int letkf_core_batch_largek(int ne, int npts, const int64_t* offs, co
     // 1. Gram
     g.out = G;
     g.rows = rows;
+    g.rows16 = rows16;
+    g.ridx = ridx;
     g.wts = w;
     g.offs = offs + p0;
     g.ne = ne;
     st = lk_gemm<LK_GRAM>(g, nb, s);
     if (st) break;
     // 2. prep
-    lk_prep_kernel<<<nb, LKP_NT, 0, s>>>(ne, kp, offs + p0, rows, w, dep, rloc, parm_infl + p0, minfl, G, Y, Z, bvec,
-                                         inv_s, pt, active);
+    lk_prep_kernel<<<nb, LKP_NT, 0, s>>>(ne, kp, offs + p0, rows, rows16, ridx, w, dep, rloc, parm_infl + p0, minfl,
+                                         G, Y, Z, bvec, inv_s, pt, active);
     note_launch();
     // 3. coupled Newton-Schulz
     g.rows = nullptr;
+    g.rows16 = nullptr;
+    g.ridx = nullptr;
     g.wts = nullptr;
     g.offs = nullptr;
     g.active = active;
@@ -661,4 +719,22 @@ extern "C" int letkf_core_batch_largek(int ne, int npts, const int64_t* offs, co
   for (void* p : fr)
     if (p) cudaFreeAsync(p, s);
   return st;
+}
+
+extern "C" int letkf_core_batch_largek(int ne, int npts, const int64_t* offs, const float* rows, const float* rdiag,
+                                       const float* rloc, const float* dep, double* parm_infl, float* trans,
+                                       float* transm, int rdiag_wloc, double minfl, int* status, void* stream) {
+  return largek_core(ne, npts, offs, rows, nullptr, nullptr, rdiag, rloc, dep, parm_infl, trans, transm, rdiag_wloc,
+                     minfl, status, stream);
+}
+
+extern "C" int letkf_core_batch_largek_indexed(int ne, int npts, const int64_t* offs, const int* idx,
+                                               const void* ens_obs, int ens_bf16, const float* dep_obs,
+                                               const float* rdiag, const float* rloc, double* parm_infl,
+                                               float* trans, float* transm, int rdiag_wloc, double minfl,
+                                               int* status, void* stream) {
+  if (!ens_obs || !dep_obs || !idx) return LETKF_ERR_ARG;
+  return largek_core(ne, npts, offs, ens_bf16 ? nullptr : (const float*)ens_obs,
+                     ens_bf16 ? (const __nv_bfloat16*)ens_obs : nullptr, idx, rdiag, rloc, dep_obs, parm_infl, trans,
+                     transm, rdiag_wloc, minfl, status, stream);
 }

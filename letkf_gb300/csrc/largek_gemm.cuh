@@ -11,8 +11,10 @@
 // one CTA's MMAs also overlap another's global loads.
 //
 // Modes:
-//   LK_GRAM   out = Ywᵀ Y over the point's local rows (K = its L, rows of the
-//             packed [nrows][ne] array, Yw = w_l y_l)
+//   LK_GRAM   out = Ywᵀ Y over the point's local rows (K = its L, Yw = w_l y_l):
+//             rows of the packed FP32 [nrows][ne] array, or with ridx rows
+//             ridx[l] of the observation ensemble (FP32 rows, or BF16 rows16),
+//             so that no per-point copies are made however long the list
 //   LK_T      out = X Y and e2[b] += ||out - I||²_F   (Newton-Schulz residual)
 //   LK_AXPBY  out = alpha X Y + beta D   (alpha, beta per point when alpha_b,
 //             beta_b are set;
@@ -50,7 +52,9 @@ struct LkGemmArgs {
   float* e2;              // [batch] (LK_T)
   const int* active;      // [batch] or NULL
   // LK_GRAM
-  const float* rows;      // [nrows][ne]
+  const float* rows;      // [nrows][ne], or [nobs][ne] with ridx
+  const __nv_bfloat16* rows16;  // [nobs][ne] BF16 rows (with ridx; rows is then NULL)
+  const int* ridx;        // [nrows] observation of each list entry, or NULL (packed rows)
   const float* wts;       // [nrows] weight of each row (rloc / rdiag)
   const int64_t* offs;    // [batch + 1] rows of point b: offs[b] .. offs[b+1]-1
   int ne;
@@ -138,10 +142,17 @@ __global__ void __launch_bounds__(LK_NT, 3) largek_gemm_kernel(LkGemmArgs a) {
         const int l = k0 + j;
         float ya = 0.f, yb = 0.f;
         if (l < L) {
-          const float* row = a.rows + (size_t)(r0 + l) * a.ne;
+          const size_t ri = a.ridx ? (size_t)a.ridx[r0 + l] : (size_t)(r0 + l);
           const float w = a.wts[r0 + l];
-          if (m0 + r < a.ne) ya = w * row[m0 + r];
-          if (n0 + r < a.ne) yb = row[n0 + r];
+          if (a.rows16) {
+            const __nv_bfloat16* row = a.rows16 + ri * a.ne;
+            if (m0 + r < a.ne) ya = w * __bfloat162float(row[m0 + r]);
+            if (n0 + r < a.ne) yb = __bfloat162float(row[n0 + r]);
+          } else {
+            const float* row = a.rows + ri * a.ne;
+            if (m0 + r < a.ne) ya = w * row[m0 + r];
+            if (n0 + r < a.ne) yb = row[n0 + r];
+          }
         }
         xa[j] = ya;
         xb[j] = yb;

@@ -116,99 +116,156 @@ struct SpeedyCtx {
   // GFS variant (gfs/letkf/letkf_tools.f90:686-925)
   int gfs;
   double dist_zero_rain, dist_zerov_rain, sigma_obs_rain, base_obsv_rain;
+  // FP32 pre-test of the horizontal distance: cos of the cut-off angles
+  // dist_zero / re (-2 where the cut-off reaches the antipode)
+  float cos_cut, cos_cut_rain;
 };
+
+// One warp per grid point: lane l tests candidates ib + l, ib + l + 32, ...;
+// the accepted ones are written in candidate order (ballot prefix), so lists
+// and their order are those of the reference's sequential loop.
+struct WarpList {
+  int* idx;
+  double *rloc, *rdiag;
+  int64_t base;
+  int cnt;
+  __device__ __forceinline__ void push(bool ok, int ob, double r, double rd) {
+    const unsigned bal = __ballot_sync(0xffffffffu, ok);
+    if (ok && idx) {
+      const int64_t at = base + cnt + __popc(bal & ((1u << (threadIdx.x & 31)) - 1u));
+      idx[at] = ob;
+      rloc[at] = r;
+      rdiag[at] = rd;
+    }
+    cnt += __popc(bal);
+  }
+};
+
+// false only where the reference's FP64 test (common/common.f90:401-424:
+// acos of the cosine of the angle, times re, against the cut-off) certainly
+// rejects: the FP32 cosine is below the cut-off's by more than 1e-4 (FP32
+// rounding of these terms is below 1e-6); every other candidate gets the
+// FP64 test
+__device__ __forceinline__ bool maybe_within(const SpeedyCtx& c, int ob, float s1, float c1, double lon1,
+                                             float cos_cut) {
+  constexpr double D2R = 3.1415926535 / 180.0;
+  float s2, c2;
+  sincosf((float)(c.olat[ob] * D2R), &s2, &c2);
+  const float dl = (float)((c.olon[ob] - lon1) * D2R);
+  const float cosd = s1 * s2 + c1 * c2 * cosf(dl);
+  return cosd >= cos_cut - 1.0e-4f;
+}
 
 // GFS candidate test (gfs/letkf/letkf_tools.f90:833-915); logrlev = ln p of
 // the point; var_local (6 classes) may be NULL (nvar = 0)
-__device__ __forceinline__ void gfs_range(const SpeedyCtx& c, int ib, int ie, double lon1, double lat1,
-                                          double logrlev, int* idx, double* rloc, double* rdiag, int64_t base,
-                                          int& cnt) {
-  for (int ip = ib; ip <= ie; ip++) {
-    const int ob = ip - 1;
-    const int elm = (int)llround(c.elm[ob]);
-    double dlev;
-    if (elm == 14593) {
-      dlev = fabs(log(c.odat[ob]) - logrlev);
-      if (dlev > c.dist_zerov) continue;
-    } else if (elm == 19999) {
-      dlev = fabs(log(c.base_obsv_rain) - logrlev);
-      if (dlev > c.dist_zerov_rain) continue;
-    } else if (elm >= 99991) {
-      dlev = 0.0;
-    } else {
-      dlev = fabs(log(c.olev[ob]) - logrlev);
-      if (dlev > c.dist_zerov) continue;
-    }
-    const double dist = distll(c.olon[ob], c.olat[ob], lon1, lat1);
-    if (dist > (elm == 19999 ? c.dist_zero_rain : c.dist_zero)) continue;
-    double vl = 1.0;
-    if (c.var_local) {
-      int iobs;
-      switch (elm) {
-        case 2819: case 2820: iobs = 1; break;
-        case 3073: case 3074: iobs = 2; break;
-        case 3330: case 3331: iobs = 3; break;
-        case 14593: iobs = 4; break;
-        case 19999: iobs = 5; break;
-        case 99991: case 99992: case 99993: iobs = 6; break;
-        default: iobs = 0; break;  // class undefined in the reference: not selected
+__device__ __forceinline__ void gfs_range(const SpeedyCtx& c, int ib, int ie, double lon1, double lat1, float s1,
+                                          float c1, double logrlev, WarpList& out) {
+  const int lane = threadIdx.x & 31;
+  for (int ip0 = ib; ip0 <= ie; ip0 += 32) {
+    const int ip = ip0 + lane;
+    bool ok = false;
+    int ob = ip - 1;
+    double r = 0.0, rd = 0.0;
+    if (ip <= ie) {
+      const int elm = (int)llround(c.elm[ob]);
+      ok = maybe_within(c, ob, s1, c1, lon1, elm == 19999 ? c.cos_cut_rain : c.cos_cut);
+      double dlev = 0.0;
+      if (ok) {
+        if (elm == 14593) {
+          dlev = fabs(log(c.odat[ob]) - logrlev);
+          ok = !(dlev > c.dist_zerov);
+        } else if (elm == 19999) {
+          dlev = fabs(log(c.base_obsv_rain) - logrlev);
+          ok = !(dlev > c.dist_zerov_rain);
+        } else if (elm < 99991) {
+          dlev = fabs(log(c.olev[ob]) - logrlev);
+          ok = !(dlev > c.dist_zerov);
+        }
       }
-      if (iobs == 0) continue;
-      vl = c.var_local[iobs - 1];
-      if (vl < 2.2250738585072014e-308) continue;
+      double dist = 0.0;
+      if (ok) {
+        dist = distll(c.olon[ob], c.olat[ob], lon1, lat1);
+        ok = !(dist > (elm == 19999 ? c.dist_zero_rain : c.dist_zero));
+      }
+      double vl = 1.0;
+      if (ok && c.var_local) {
+        int iobs;
+        switch (elm) {
+          case 2819: case 2820: iobs = 1; break;
+          case 3073: case 3074: iobs = 2; break;
+          case 3330: case 3331: iobs = 3; break;
+          case 14593: iobs = 4; break;
+          case 19999: iobs = 5; break;
+          case 99991: case 99992: case 99993: iobs = 6; break;
+          default: iobs = 0; break;  // class undefined in the reference: not selected
+        }
+        if (iobs == 0) ok = false;
+        else {
+          vl = c.var_local[iobs - 1];
+          if (vl < 2.2250738585072014e-308) ok = false;
+        }
+      }
+      if (ok && out.idx) {
+        const double a = dist / (elm == 19999 ? c.sigma_obs_rain : c.sigma_obs), b = dlev / c.sigma_obsv;
+        r = exp(-0.5 * (a * a + b * b));
+        if (c.var_local) r = r * vl;
+        rd = c.oerr[ob] * c.oerr[ob];
+      }
     }
-    if (idx) {
-      const double a = dist / (elm == 19999 ? c.sigma_obs_rain : c.sigma_obs), b = dlev / c.sigma_obsv;
-      double r = exp(-0.5 * (a * a + b * b));
-      if (c.var_local) r = r * vl;
-      idx[base + cnt] = ob;
-      rdiag[base + cnt] = c.oerr[ob] * c.oerr[ob];
-      rloc[base + cnt] = r;
-    }
-    cnt++;
+    out.push(ok, ob, r, rd);
   }
 }
 
 // Test candidates [ib, ie] (1-based, inclusive) for one point; appends.
-__device__ __forceinline__ void speedy_range(const SpeedyCtx& c, int ib, int ie, double lon1, double lat1, int ilev,
-                                             double logpfm, int* idx, double* rloc, double* rdiag, int64_t base,
-                                             int& cnt) {
-  for (int ip = ib; ip <= ie; ip++) {
-    const int ob = ip - 1;
-    const int elm = (int)llround(c.elm[ob]);
-    double dlev;
-    if (elm == 14593 && ilev > 1) dlev = fabs(log(c.odat[ob]) - logpfm);
-    else if (elm != 14593) dlev = fabs(log(c.olev[ob]) - logpfm);
-    else dlev = 0.0;
-    if (dlev > c.dist_zerov) continue;
-    const double dist = distll(c.olon[ob], c.olat[ob], lon1, lat1);
-    if (dist > c.dist_zero) continue;
-    int iobs;
-    switch (elm) {
-      case 2819: iobs = 1; break;
-      case 2820: iobs = 2; break;
-      case 3073: iobs = 3; break;
-      case 3330: iobs = 4; break;
-      case 3331: iobs = 5; break;
-      case 14593: iobs = 6; break;
-      default: iobs = 7; break;
+__device__ __forceinline__ void speedy_range(const SpeedyCtx& c, int ib, int ie, double lon1, double lat1, float s1,
+                                             float c1, int ilev, double logpfm, WarpList& out) {
+  const int lane = threadIdx.x & 31;
+  for (int ip0 = ib; ip0 <= ie; ip0 += 32) {
+    const int ip = ip0 + lane;
+    bool ok = false;
+    int ob = ip - 1;
+    double r = 0.0, rd = 0.0;
+    if (ip <= ie) {
+      const int elm = (int)llround(c.elm[ob]);
+      ok = maybe_within(c, ob, s1, c1, lon1, c.cos_cut);
+      double dlev = 0.0, dist = 0.0;
+      if (ok) {
+        if (elm == 14593 && ilev > 1) dlev = fabs(log(c.odat[ob]) - logpfm);
+        else if (elm != 14593) dlev = fabs(log(c.olev[ob]) - logpfm);
+        ok = !(dlev > c.dist_zerov);
+      }
+      if (ok) {
+        dist = distll(c.olon[ob], c.olat[ob], lon1, lat1);
+        ok = !(dist > c.dist_zero);
+      }
+      double vl = 0.0;
+      if (ok) {
+        int iobs;
+        switch (elm) {
+          case 2819: iobs = 1; break;
+          case 2820: iobs = 2; break;
+          case 3073: iobs = 3; break;
+          case 3330: iobs = 4; break;
+          case 3331: iobs = 5; break;
+          case 14593: iobs = 6; break;
+          default: iobs = 7; break;
+        }
+        vl = c.var_local[iobs - 1];
+        ok = !(vl < 2.2250738585072014e-308);
+      }
+      if (ok && out.idx) {
+        const double a = dist / c.sigma_obs, b = dlev / c.sigma_obsv;
+        rd = c.oerr[ob] * c.oerr[ob];
+        r = exp(-0.5 * (a * a + b * b)) * vl;
+      }
     }
-    const double vl = c.var_local[iobs - 1];
-    if (vl < 2.2250738585072014e-308) continue;
-    if (idx) {
-      const double a = dist / c.sigma_obs, b = dlev / c.sigma_obsv;
-      idx[base + cnt] = ob;
-      rdiag[base + cnt] = c.oerr[ob] * c.oerr[ob];
-      rloc[base + cnt] = exp(-0.5 * (a * a + b * b)) * vl;
-    }
-    cnt++;
+    out.push(ok, ob, r, rd);
   }
 }
 
 // speedy/letkf/letkf_tools.f90:575-603
 __device__ __forceinline__ void speedy_sub(const SpeedyCtx& c, int imin, int imax, int jmin, int jmax, double lon1,
-                                           double lat1, int ilev, double logpfm, int* idx, double* rloc,
-                                           double* rdiag, int64_t base, int& cnt) {
+                                           double lat1, float s1, float c1, int ilev, double logpfm, WarpList& out) {
   const int nlon = c.nlon;
   for (int j = jmin; j <= jmax; j++) {
     int ib;
@@ -217,8 +274,8 @@ __device__ __forceinline__ void speedy_sub(const SpeedyCtx& c, int imin, int ima
     else ib = 1;
     const int ie = c.G[(size_t)(j - 1) * nlon + imax - 1];
     if (ie - ib + 1 == 0) continue;
-    if (c.gfs) gfs_range(c, ib, ie, lon1, lat1, logpfm, idx, rloc, rdiag, base, cnt);
-    else speedy_range(c, ib, ie, lon1, lat1, ilev, logpfm, idx, rloc, rdiag, base, cnt);
+    if (c.gfs) gfs_range(c, ib, ie, lon1, lat1, s1, c1, logpfm, out);
+    else speedy_range(c, ib, ie, lon1, lat1, s1, c1, ilev, logpfm, out);
   }
 }
 
@@ -227,7 +284,7 @@ __global__ void search_speedy_kernel(SpeedyCtx c, int npts, const double* __rest
                                      const int* __restrict__ pilev, const double* __restrict__ plogp, double dlat_zero,
                                      const int64_t* __restrict__ offs, int* nobsl, int* idx, double* rloc,
                                      double* rdiag) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int p = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);  // one warp per point
   if (p >= npts) return;
   const int nlon = c.nlon, nlat = c.nlat;
   const double lon1 = plon[p], lat1 = plat[p];
@@ -243,9 +300,15 @@ __global__ void search_speedy_kernel(SpeedyCtx c, int npts, const double* __rest
   }
   const int jmin = first_below(minlat, c.lat, nlat - 2);
   const int jmax = first_below(maxlat, c.lat, nlat - 2);
-  const int64_t base = idx ? offs[p] : 0;
-  int cnt = 0, imin, imax;
-#define SUB(a, b) speedy_sub(c, (a), (b), jmin, jmax, lon1, lat1, ilev, logpfm, idx, rloc, rdiag, base, cnt)
+  WarpList out;
+  out.idx = idx;
+  out.rloc = rloc;
+  out.rdiag = rdiag;
+  out.base = idx ? offs[p] : 0;
+  out.cnt = 0;
+  const float s1 = sinf((float)(lat1 * (3.1415926535 / 180.0))), c1 = cosf((float)(lat1 * (3.1415926535 / 180.0)));
+  int imin, imax;
+#define SUB(a, b) speedy_sub(c, (a), (b), jmin, jmax, lon1, lat1, s1, c1, ilev, logpfm, out)
   if (minlon >= 0 && maxlon <= 360.0) {
     imin = first_below(minlon, c.lon, nlon - 1);
     imax = first_below(maxlon, c.lon, nlon - 1);
@@ -293,7 +356,25 @@ __global__ void search_speedy_kernel(SpeedyCtx c, int npts, const double* __rest
     }
   }
 #undef SUB
-  if (!idx) nobsl[p] = cnt;
+  if (!idx && (threadIdx.x & 31) == 0) nobsl[p] = out.cnt;
+}
+
+// cos of the angle dist / re (the FP32 pre-test's threshold)
+static float cos_cut(double dist) {
+  const double ang = dist / 6371.3e3;  // common/common.f90:35
+  return ang >= 3.14159 ? -2.f : (float)cos(ang);
+}
+
+static void launch_speedy_warps(const SpeedyCtx& c, int npts, const double* plon, const double* plat,
+                                const double* pdlon, const int* pilev, const double* plogp, double dlat_zero,
+                                const int64_t* offs, int* nobsl, int* idx, double* rloc, double* rdiag,
+                                cudaStream_t stream) {
+  const int64_t threads = (int64_t)npts * 32;
+  const int bs = 128;
+  search_speedy_kernel<<<(unsigned)((threads + bs - 1) / bs), bs, 0, stream>>>(c, npts, plon, plat, pdlon, pilev,
+                                                                               plogp, dlat_zero, offs, nobsl, idx,
+                                                                               rloc, rdiag);
+  note_launch();
 }
 
 // one thread per point: CTAs small enough that the grid covers the SMs twice
@@ -349,11 +430,10 @@ int launch_search_speedy(int nlon, int nlat, const double* lon, const double* la
   c.sigma_obsv = params[4];
   c.gfs = 0;
   c.dist_zero_rain = c.dist_zerov_rain = c.sigma_obs_rain = c.base_obsv_rain = 0.0;
+  c.cos_cut = cos_cut(c.dist_zero);
+  c.cos_cut_rain = c.cos_cut;
   (void)nobs;
-  const int bs = search_block(npts);
-  search_speedy_kernel<<<(npts + bs - 1) / bs, bs, 0, stream>>>(c, npts, plon, plat, pdlon, pilev, plogp, params[2],
-                                                                  offs, nobsl, idx, rloc, rdiag);
-  note_launch();
+  launch_speedy_warps(c, npts, plon, plat, pdlon, pilev, plogp, params[2], offs, nobsl, idx, rloc, rdiag, stream);
   return cuda_status(cudaGetLastError());
 }
 
@@ -387,10 +467,9 @@ int launch_search_gfs(int nlon, int nlat, const double* lon, const double* lat, 
   c.base_obsv_rain = params[7];
   const double dz = c.dist_zero > c.dist_zero_rain ? c.dist_zero : c.dist_zero_rain;
   const double dlat_zero = dz / 3.1415926535 / 6371.3e3 * 180.0;  // gfs/letkf/letkf_tools.f90:712
-  const int bs = search_block(npts);
-  search_speedy_kernel<<<(npts + bs - 1) / bs, bs, 0, stream>>>(c, npts, plon, plat, nullptr, nullptr, prlev,
-                                                                  dlat_zero, offs, nobsl, idx, rloc, rdiag);
-  note_launch();
+  c.cos_cut = cos_cut(c.dist_zero);
+  c.cos_cut_rain = cos_cut(c.dist_zero_rain);
+  launch_speedy_warps(c, npts, plon, plat, nullptr, nullptr, prlev, dlat_zero, offs, nobsl, idx, rloc, rdiag, stream);
   return cuda_status(cudaGetLastError());
 }
 

@@ -225,7 +225,6 @@ struct letkf_server_s {
   int running = 0;
   bool stop = false;
   uint64_t tick = 0;
-  int grid_cap = 0;
   std::vector<double> latencies;
   double first_submit = -1.0, last_done = 0.0;
   int64_t points_done = 0, failed = 0;
@@ -301,7 +300,7 @@ static int run_job(letkf_server_s* S, const letkf_job_desc& j, Domain* dm, cudaS
     std::vector<double> one((size_t)j.npts, 1.0);
     rc = letkf_sweep_set_inflation(h, one.data(), 0);
   }
-  if (rc == LETKF_OK) rc = letkf_sweep_set_option(h, LETKF_OPT_GRID_CAP, S->grid_cap);
+  if (rc == LETKF_OK) rc = letkf_sweep_set_option(h, LETKF_OPT_GRID_SHARE, S->d.nslots);
   if (rc == LETKF_OK) rc = letkf_sweep_run(h, s);
   if (rc == LETKF_OK) rc = letkf_sweep_get_analysis(h, j.xa, 0);
   std::vector<int> stat((size_t)j.npts);
@@ -463,9 +462,6 @@ int letkf_server_create(letkf_server_t* out, const letkf_server_desc* d) {
     delete S;
     return LETKF_ERR_CUDA;
   }
-  int nsm = 0;
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, d->device);
-  S->grid_cap = std::max(1, nsm * 4 / d->nslots);
   for (int i = 0; i < d->nslots; i++) S->workers.emplace_back(worker_main, S);
   *out = S;
   return LETKF_OK;

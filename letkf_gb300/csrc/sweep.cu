@@ -24,6 +24,8 @@ int launch_sweep_mixed(const SweepArgs& a, cudaStream_t stream, int grid_cap);
 int launch_sweep_tc(const SweepArgs& a, cudaStream_t stream, int grid_cap);
 int prepare_sweep_mixed(int n);
 int prepare_sweep_tc();
+int launch_sweep_tc128(const SweepArgs& a, cudaStream_t stream, int grid_cap);
+int prepare_sweep_tc128();
 int launch_sweep_prep_obs(int, const double*, const double*, const double*, const double*, const double*,
                           const double*, const int*, const int*, const double*, const double*, float4*, float4*, int*,
                           cudaStream_t);
@@ -546,7 +548,14 @@ int letkf_sweep_device_buffers(letkf_sweep_t h, void** xb, void** xa, double** i
 int letkf_sweep_set_option(letkf_sweep_t h, int option, int value) {
   if (!h) return LETKF_ERR_ARG;
   switch (option) {
-    case LETKF_OPT_GRID_CAP: h->grid_cap = value; return LETKF_OK;
+    case LETKF_OPT_GRID_CAP:
+      if (value < 0) return LETKF_ERR_ARG;
+      h->grid_cap = value;
+      return LETKF_OK;
+    case LETKF_OPT_GRID_SHARE:
+      if (value < 1) return LETKF_ERR_ARG;
+      h->grid_cap = value == 1 ? 0 : -value;  // the launchers read a negative cap as a share
+      return LETKF_OK;
     case LETKF_OPT_MAX_SWEEPS:
       if (value < 1 || value > 64) return LETKF_ERR_ARG;
       h->max_sweeps = value;
@@ -772,7 +781,14 @@ static void build_args(letkf_sweep_t h, SweepArgs& a) {
   a.fault_wait_polls = h->fault_wait;
 }
 
-static bool tc_path(letkf_sweep_t h) { return h->use_tc && h->use_ns && h->d.ne <= 64; }
+// tensor-core sweeps: sweep_tc.cu for ne <= 64, sweep_tc128.cu for 64 < ne <= 128
+static bool tc_path(letkf_sweep_t h) { return h->use_tc && h->use_ns && h->d.ne <= 128; }
+
+static int launch_tc(letkf_sweep_t h, const SweepArgs& a, cudaStream_t s) {
+  return h->d.ne <= 64 ? launch_sweep_tc(a, s, h->grid_cap) : launch_sweep_tc128(a, s, h->grid_cap);
+}
+
+static int prepare_tc(letkf_sweep_t h) { return h->d.ne <= 64 ? prepare_sweep_tc() : prepare_sweep_tc128(); }
 
 static int launch_mixed_run(letkf_sweep_t h, const SweepArgs& a, cudaStream_t s) {
   cudaMemsetAsync(h->counter, 0, sizeof(int), s);
@@ -781,7 +797,7 @@ static int launch_mixed_run(letkf_sweep_t h, const SweepArgs& a, cudaStream_t s)
   // Newton-Schulz sweep (tensor-core or SIMT), then the Jacobi pass over the
   // points it deferred
   cudaMemsetAsync(h->defer_count, 0, sizeof(int), s);
-  int st = tc ? launch_sweep_tc(a, s, h->grid_cap) : launch_sweep_mixed(a, s, h->grid_cap);
+  int st = tc ? launch_tc(h, a, s) : launch_sweep_mixed(a, s, h->grid_cap);
   if (st != LETKF_OK) return st;
   SweepArgs b = a;
   if (a.list_offs) {
@@ -887,7 +903,7 @@ static int run_on(letkf_sweep_t h, cudaStream_t s) {
       h->gexec = nullptr;
     }
     // kernel attributes are set before the capture, not inside it
-    int st = tc_path(h) ? prepare_sweep_tc() : LETKF_OK;
+    int st = tc_path(h) ? prepare_tc(h) : LETKF_OK;
     if (st == LETKF_OK) st = prepare_sweep_mixed(h->d.ne);
     if (st != LETKF_OK) return st;
     const int64_t n0 = letkf_launch_count();
@@ -1076,7 +1092,7 @@ int letkf_sweep_autotune(letkf_sweep_t h, int sample_points, int* choice) {
     int tc, ns, scaled;
   };
   std::vector<Cand> cands;
-  if (h->d.ne <= 64) {
+  if (h->d.ne <= 128) {
     cands.push_back({1, 1, 1});
     cands.push_back({1, 1, 0});
   }

@@ -462,6 +462,7 @@ static int launch_sweep_np(const SweepArgs& a, cudaStream_t stream, int grid_cap
   if (per_sm < 1) per_sm = 1;
   int grid = nsm * per_sm;
   if (grid_cap > 0 && grid > grid_cap) grid = grid_cap;
+  if (grid_cap < 0) grid = grid / -grid_cap > 0 ? grid / -grid_cap : 1;  // a 1/v share of the resident CTAs
   if (grid > a.nwork) grid = a.nwork > 0 ? a.nwork : 1;
   kern<<<grid, MixedCfg<NP>::NT, bytes, stream>>>(a);
   note_launch();

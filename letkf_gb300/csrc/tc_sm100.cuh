@@ -10,6 +10,7 @@
 // g*SBO + q*LBO.  We store k groups of one row group contiguously:
 // LBO = 128 bytes, SBO = (K/4) * 128 bytes.
 #pragma once
+#include <cuda_bf16.h>
 #include <stdint.h>
 
 namespace letkf {
@@ -189,4 +190,45 @@ __device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) 
 }
 
 }  // namespace tc
+}  // namespace letkf
+
+namespace letkf {
+
+// ---- operand splits shared by the tensor-core sweeps ----
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+// 8 values -> hi and lo bf16 packs (16 bytes each)
+__device__ __forceinline__ void split8(const float* v, uint4& hi, uint4& lo) {
+  float h[8], l[8];
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    h[j] = __bfloat162float(__float2bfloat16_rn(v[j]));
+    l[j] = v[j] - h[j];
+  }
+  hi = make_uint4(pack_bf16x2(h[0], h[1]), pack_bf16x2(h[2], h[3]), pack_bf16x2(h[4], h[5]), pack_bf16x2(h[6], h[7]));
+  lo = make_uint4(pack_bf16x2(l[0], l[1]), pack_bf16x2(l[2], l[3]), pack_bf16x2(l[4], l[5]), pack_bf16x2(l[6], l[7]));
+}
+
+// 4 values -> tf32 hi (low 13 mantissa bits cleared) and the FP32 remainder
+__device__ __forceinline__ void split4_tf32(const float* v, float4& hi, float4& lo) {
+  float h[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) h[j] = __uint_as_float(__float_as_uint(v[j]) & 0xFFFFE000u);
+  hi = make_float4(h[0], h[1], h[2], h[3]);
+  lo = make_float4(v[0] - h[0], v[1] - h[1], v[2] - h[2], v[3] - h[3]);
+}
+
+__device__ __forceinline__ void unpack8(uint4 p, float* v) {
+  const uint32_t w[4] = {p.x, p.y, p.z, p.w};
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const __nv_bfloat162 b = *reinterpret_cast<const __nv_bfloat162*>(&w[j]);
+    v[2 * j] = __low2float(b);
+    v[2 * j + 1] = __high2float(b);
+  }
+}
+
 }  // namespace letkf

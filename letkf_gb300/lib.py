@@ -68,6 +68,9 @@ _SIGS = {
     "letkf_obs_departure": (_i, [_i, _i, _vp, _vp, _vp, _d, _vp, _vp, _vp, _vp, _vp]),
     "letkf_core_batch_largek": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _d, _vp, _vp]),
     "letkf_update_mixed": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
+    "letkf_core_batch_largek_indexed": (_i, [_i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _d, _vp,
+                                             _vp]),
+    "letkf_update_bf16": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "letkf_obs_analysis": (_i, [_i, _i, _vp, _vp, _vp, _d, _vp, _d, _vp, _vp, _vp]),
     "letkf_efso": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "letkf_grd_decode": (_i, [_i64, _i, _i, _vp, _i, _i, _i, _i, _vp, _i64, _i64, _vp]),

@@ -34,6 +34,7 @@ OPT_POLISH_PROBE = 12
 OPT_NS_COND = 13
 OPT_MAX_NOBS_PER_GRID = 14
 OPT_FAULT_WAIT = 15
+OPT_GRID_SHARE = 16
 
 
 class SweepDesc(C.Structure):

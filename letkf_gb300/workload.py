@@ -189,14 +189,23 @@ class GlobalWorkload:
             dat[s] = y
         return hdxf, dep, dat
 
-    def points(self, idx):
+    def search_params(self, sigma_obs):
+        """(dist_zero, dist_zerov, dlat_zero, sigma_obs, sigma_obsv) for another
+        horizontal localisation scale on the same observations."""
+        dist_zero = sigma_obs * math.sqrt(10.0 / 3.0) * 2.0
+        dist_zerov = self.sigma_obsv * math.sqrt(10.0 / 3.0) * 2.0
+        dlat_zero = dist_zero / 3.1415926535 / 6371.3e3 * 180.0   # speedy/letkf/letkf_obs.f90:82-88
+        return (dist_zero, dist_zerov, dlat_zero, sigma_obs, self.sigma_obsv)
+
+    def points(self, idx, params=None):
         """lon, lat, dlon_zero, ilev (1-based), log p of the points idx."""
+        params = self.params if params is None else params
         idx = np.asarray(idx)
         nij = self.nlon * self.nlat
         lev, ij = idx // nij, idx % nij
         j, i = ij // self.nlon, ij % self.nlon
         lat = self.lat[j]
-        dlon = self.params[2] / np.maximum(np.cos(3.1415926535 * lat / 180.0), 1e-12)
+        dlon = params[2] / np.maximum(np.cos(3.1415926535 * lat / 180.0), 1e-12)
         return self.lon[i], lat, dlon, (lev + 1).astype(np.int32), np.log(self.plev[lev])
 
     def background_torch(self, device, idx):

@@ -115,3 +115,111 @@ def test_largek_ill_conditioned_points_are_certified_or_flagged(cuda, rd_scale):
         assert np.isfinite(tr[p]).all(), p
         scale = np.abs(ref["trans"][p]).max()
         assert np.abs(tr[p] - ref["trans"][p]).max() <= 1e-3 * scale, (p, Ls[p])
+
+
+@pytest.mark.parametrize("ne", [256, 512])
+def test_indexed_bf16_lists_equal_the_packed_rows(cuda, ne):
+    """The core over index lists into a BF16 observation ensemble (no packed
+    copies) gives the same transforms, bit for bit, as the packed FP32 rows of
+    the same values (BF16 values are exact in FP32); and it meets the oracle
+    bar.  Lists repeat observations and run long (L up to 3000)."""
+    import torch
+
+    from letkf_gb300.core import core_batch_largek, core_batch_largek_indexed
+
+    rng = np.random.default_rng(ne + 1)
+    nobs = 5000
+    ens = rng.standard_normal((nobs, ne))
+    ens -= ens.mean(1, keepdims=True)
+    ens16 = torch.as_tensor(ens, dtype=torch.bfloat16, device=cuda)
+    ens64 = ens16.double().cpu().numpy()
+    dep_obs = rng.standard_normal(nobs).astype(np.float32)
+    Ls = [0, 3, 3000, 700, 128, 1]
+    offs = np.concatenate([[0], np.cumsum(Ls)]).astype(np.int64)
+    idx = rng.integers(0, nobs, int(offs[-1])).astype(np.int32)
+    rd = rng.uniform(0.3, 3.0, idx.size).astype(np.float32)
+    rl = rng.uniform(0.01, 1.0, idx.size).astype(np.float32)
+    infl = rng.uniform(0.95, 1.3, len(Ls))
+    t = lambda a, dt=torch.float32: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=cuda)
+    pa, pb = t(infl, torch.float64), t(infl, torch.float64)
+    a = core_batch_largek_indexed(ne, t(offs, torch.int64), t(idx, torch.int32), ens16, t(dep_obs), t(rd), t(rl), pa,
+                                  want_transm=True)
+    rows = ens64[idx]
+    b = core_batch_largek(ne, t(offs, torch.int64), t(rows), t(rd), t(rl), t(dep_obs[idx]), pb, want_transm=True)
+    torch.cuda.synchronize()
+    for k in ("trans", "transm", "status"):
+        assert torch.equal(a[k], b[k]), k
+    assert torch.equal(pa, pb)
+    ref = O.letkf_core_batch(ne, offs, rows, rd.astype(np.float64), rl.astype(np.float64),
+                             dep_obs[idx].astype(np.float64), infl, want_transm=True)
+    tr = a["trans"].cpu().numpy().astype(np.float64)
+    for p in range(len(Ls)):
+        scale = np.abs(ref["trans"][p]).max()
+        assert np.abs(tr[p] - ref["trans"][p]).max() <= 1e-4 * scale, (p, Ls[p])
+
+
+def test_update_bf16_storage(cuda):
+    """letkf_update_bf16: FP32 mean + BF16 perturbations in and out.  The
+    analysis mean within 1e-6 relative of the FP64 result on the same stored
+    inputs; the perturbations within BF16 rounding (2^-8 relative)."""
+    import torch
+
+    from letkf_gb300.core import update_bf16
+
+    rng = np.random.default_rng(7)
+    nv, npts, ne = 3, 17, 320
+    xmean = (rng.standard_normal((nv, npts)) * 10 + 280).astype(np.float32)
+    xp = torch.as_tensor(rng.standard_normal((nv, npts, ne)), dtype=torch.bfloat16, device=cuda)
+    a = rng.standard_normal((npts, ne, ne)) * 0.05
+    tr = (np.eye(ne)[None] + (a + a.transpose(0, 2, 1))).astype(np.float32)  # column-major == symmetric
+    tm = (rng.standard_normal((npts, ne)) * 0.01).astype(np.float32)
+    t = lambda x: torch.as_tensor(np.ascontiguousarray(x), device=cuda)
+    am, ap = update_bf16(t(xmean), xp, t(tr), t(tm))
+    x64 = xp.double().cpu().numpy()
+    m = x64.mean(-1, keepdims=True)
+    xd = x64 - m
+    want_mean = xmean.astype(np.float64) + m[..., 0] + np.einsum("vpk,pk->vp", xd, tm.astype(np.float64))
+    want_pert = np.einsum("vpk,pmk->vpm", xd, tr.astype(np.float64))
+    assert np.abs(am.cpu().numpy() - want_mean).max() <= 1e-6 * np.abs(want_mean).max()
+    got = ap.double().cpu().numpy()
+    assert np.abs(got - want_pert).max() <= 2.0 ** -8 * np.abs(want_pert).max()
+    assert np.sqrt(np.mean((got - want_pert) ** 2)) <= 2.0 ** -8 * np.sqrt(np.mean(want_pert ** 2))
+
+
+def test_largek_long_lists_against_oracle(cuda):
+    """k = 512 with local lists of 12,000 observations (the Gram over K = L in
+    400 stages) through the indexed BF16 path, against the FP64 oracle."""
+    import torch
+
+    from letkf_gb300.core import core_batch_largek_indexed
+
+    ne = 512
+    rng = np.random.default_rng(12)
+    nobs = 20000
+    ens = rng.standard_normal((nobs, ne))
+    ens -= ens.mean(1, keepdims=True)
+    ens16 = torch.as_tensor(ens, dtype=torch.bfloat16, device=cuda)
+    ens64 = ens16.double().cpu().numpy()
+    dep_obs = rng.standard_normal(nobs).astype(np.float32)
+    Ls = [12000, 10000]
+    offs = np.concatenate([[0], np.cumsum(Ls)]).astype(np.int64)
+    idx = np.concatenate([rng.choice(nobs, L, replace=False) for L in Ls]).astype(np.int32)
+    # error variances large enough that A stays well conditioned with this many observations
+    rd = rng.uniform(50.0, 200.0, idx.size).astype(np.float32)
+    rl = rng.uniform(0.01, 1.0, idx.size).astype(np.float32)
+    infl = np.array([1.05, 1.2])
+    t = lambda a, dt=torch.float32: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=cuda)
+    pinf = t(infl, torch.float64)
+    out = core_batch_largek_indexed(ne, t(offs, torch.int64), t(idx, torch.int32), ens16, t(dep_obs), t(rd), t(rl),
+                                    pinf, want_transm=True)
+    torch.cuda.synchronize()
+    assert (out["status"].cpu().numpy() == 0).all()
+    ref = O.letkf_core_batch(ne, offs, ens64[idx], rd.astype(np.float64), rl.astype(np.float64),
+                             dep_obs[idx].astype(np.float64), infl, want_transm=True, nthreads=2)
+    tr = out["trans"].cpu().numpy().astype(np.float64)
+    tm = out["transm"].cpu().numpy().astype(np.float64)
+    for p in range(len(Ls)):
+        scale = np.abs(ref["trans"][p]).max()
+        assert np.abs(tr[p] - ref["trans"][p]).max() <= 1e-4 * scale, p
+        assert np.abs(tm[p] - ref["transm"][p]).max() <= 1e-4 * scale, p
+    np.testing.assert_allclose(pinf.cpu().numpy(), ref["parm_infl"], rtol=1e-5)

@@ -69,11 +69,14 @@ def test_tc_polish_against_oracle(cuda, ne):
 @pytest.mark.parametrize("ne,var_local,eig,tc,scaled", [(40, None, 0, 1, 1), (64, [1.0, 0.5, 0.0], 0, 1, 1),
                                                       (20, None, 0, 1, 1), (50, None, 0, 1, 1), (64, None, 0, 1, 0),
                                                       (64, None, 0, 0, 1),
-                                                      (100, None, 0, 1, 1), (64, None, 1, 1, 1)])
+                                                      (100, None, 0, 1, 1), (64, None, 1, 1, 1),
+                                                      (128, None, 0, 1, 1), (128, [1.0, 0.5, 0.0], 0, 1, 0),
+                                                      (72, None, 0, 1, 1), (128, None, 0, 0, 1)])
 def test_mixed_sweep_against_oracle(cuda, ne, var_local, eig, tc, scaled):
-    """tc=1, eig=0 and ne <= 64 runs the tcgen05 sweep (spectrum-scaled or
-    plain Newton-Schulz steps; background rows by TMA bulk copy when ne is a
-    multiple of 4, by plain loads for ne = 50); otherwise the SIMT sweep."""
+    """tc=1 and eig=0 run the tcgen05 sweeps (ne <= 64: sweep_tc; 64 < ne <=
+    128: sweep_tc128; spectrum-scaled or plain Newton-Schulz steps; background
+    rows by TMA bulk copy when ne is a multiple of 4, by plain loads for
+    ne = 50); otherwise the SIMT sweep."""
     from letkf_gb300.sweep import OPT_EIGENSOLVER, OPT_TC_NS_SCALING, OPT_TENSOR_CORES, PREC_MIXED, Sweep
 
     case, prm, perm, grd, so, varloc, hdxf, dep = _setup(ne=ne, f32=True, var_local=var_local)
@@ -273,7 +276,7 @@ def test_autotune_keeps_inflation_and_picks_a_valid_variant(cuda, ne):
     sw.set_inflation(infl0)
     choice = sw.autotune(sample_points=npts // 2)
     assert choice["us_per_1000_points"] > 0
-    if ne > 64:
+    if ne > 128:
         assert not choice["tensor_cores"]
     np.testing.assert_array_equal(sw.diagnostics()["infl"], infl0)
     sw.run()

@@ -308,7 +308,8 @@ def test_sweep_max_nobs_needs_groups(cuda):
 
 
 # ---------------------------------------------------------------- bounded waits
-def test_bounded_wait_gives_up_then_the_handle_recovers(cuda):
+@pytest.mark.parametrize("ne", [40, 128])
+def test_bounded_wait_gives_up_then_the_handle_recovers(cuda, ne):
     """A wait that runs out (injected: a barrier nothing arrives at) ends the
     tensor-core sweep with LETKF_ERR_TIMEOUT instead of hanging; the context
     stays usable and the next normal run on the same handle gives the same
@@ -317,9 +318,9 @@ def test_bounded_wait_gives_up_then_the_handle_recovers(cuda):
     from letkf_gb300.lib import LETKF_ERR_TIMEOUT, LetkfError
     from letkf_gb300.sweep import OPT_FAULT_WAIT
 
-    case, prm, perm, grd = _case(ne=40)
+    case, prm, perm, grd = _case(ne=ne)
     npts = case["pri"].size
-    sw = _sweep(case, prm, 40)
+    sw = _sweep(case, prm, ne)
     sw.run()
     xa0 = sw.analysis()
     for polls in (1, 64):
