@@ -83,7 +83,7 @@ def parse():
                     help="sampled points of the large-ensemble sweep at 60 km")
     ap.add_argument("--largek-700-points", type=int, default=256,
                     help="sampled points of the large-ensemble sweep at the stated 700 km")
-    ap.add_argument("--serve-requests", type=int, default=48, help="requests of the serving measurement")
+    ap.add_argument("--serve-requests", type=int, default=500, help="requests of the serving measurement")
     ap.add_argument("--serve-slots", type=int, default=3, help="jobs on the device at once")
     ap.add_argument("--serve-load", type=float, default=0.7,
                     help="offered load: arrival rate x mean single-job service time")
@@ -259,9 +259,13 @@ def run_serving(args, dev):
     mixed precision) and three Lorenz-96 rings (N = 40, 1e4, 1e5; k = 20, 32,
     64; mixed core with the FP64 update).  The arrival rate is the offered load over the mean service
     time of a request alone.  Latency = submit -> analysis on the host."""
-    from letkf_gb300.serve import PREC_MIXED, Server
+    import torch
+
+    from letkf_gb300.serve import LETKF_PENDING, PREC_MIXED, Server
     from letkf_gb300.workload import RegionalWorkload
 
+    # every host buffer a job reads or writes is page-locked
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
     specs = []
     for i, ne in enumerate((20, 32, 64, 128)):
         wl = RegionalWorkload(100 + i, 128, 128, 20, ne, 250_000, 2)
@@ -269,60 +273,135 @@ def run_serving(args, dev):
         xb = wl.background_torch(dev)
         ri, rj, plev = wl.points()
         specs.append(dict(kind="sweep", name=f"regional 128x128x20 k={ne}", domain=i, pts=(ri, rj, plev),
-                          params=wl.params, obs=dict(ri=wl.ri, rj=wl.rj, lev=wl.lev, dat=dat, err=wl.err,
-                                                     cls=wl.cls),
-                          hdxf=hdxf, dep=dep, xb=xb.cpu().numpy(), npts=wl.npts))
-        del hdxf, dep, dat, xb
+                          params=wl.params, obs=dict(ri=pin(wl.ri), rj=pin(wl.rj), lev=pin(wl.lev), dat=pin(dat),
+                                                     err=pin(wl.err), cls=pin(wl.cls.astype(np.int32))),
+                          hdxf=pin(hdxf), dep=pin(dep), xb=pin(xb.cpu().numpy()), npts=wl.npts, wl=wl,
+                          obs_np=(hdxf, dep, dat)))
+        del xb
     for j, (nx, ne) in enumerate(((40, 20), (10_000, 32), (100_000, 64))):
         rng = np.random.default_rng(200 + j)
         xf = 8.0 + rng.standard_normal((nx, ne))
         m = xf.sum(1) / ne
         y = m + rng.standard_normal(nx)
-        specs.append(dict(kind="l96", name=f"lorenz96 N={nx} k={ne}", domain=10 + j, xf=xf, hdxf=xf - m[:, None],
-                          dep=y - m, cell=np.arange(1, nx + 1, dtype=np.int32), npts=nx))
+        specs.append(dict(kind="l96", name=f"lorenz96 N={nx} k={ne}", domain=10 + j, xf=pin(xf),
+                          hdxf=pin(xf - m[:, None]), dep=pin(y - m), cell=pin(np.arange(1, nx + 1, dtype=np.int32)),
+                          npts=nx))
 
-    def submit(srv, sp):
+    pools = {}  # page-locked output buffers per domain, reused once a job's result has been collected
+
+    def out_buf(sp):
+        free = pools.setdefault(sp["name"], [])
+        if free:
+            return free.pop()
+        like = sp["xf"] if sp["kind"] == "l96" else sp["xb"]
+        return torch.empty(like.shape, dtype=torch.from_numpy(like[:0]).dtype, pin_memory=True).numpy()
+
+    def submit(srv, sp, precision=PREC_MIXED, domain=None, xa=None):
+        dom = sp["domain"] if domain is None else domain
         if sp["kind"] == "l96":
-            return srv.submit_l96(sp["xf"], sp["hdxf"], sp["dep"], sp["cell"], precision=PREC_MIXED,
-                                  domain=sp["domain"])
+            return srv.submit_l96(sp["xf"], sp["hdxf"], sp["dep"], sp["cell"], precision=precision, domain=dom,
+                                  xa=xa)
         ri, rj, plev = sp["pts"]
         return srv.submit_sweep(ri, rj, plev, sp["params"], 128, 128, sp["obs"], sp["hdxf"], sp["dep"], sp["xb"],
-                                precision=PREC_MIXED, domain=sp["domain"])
+                                precision=PREC_MIXED, domain=dom, xa=xa)
 
     with Server(nslots=args.serve_slots) as srv:
-        alone = []
+        alone, first = [], []
         for sp in specs:  # each domain once, alone: service time, and the domain becomes resident
             t0 = time.perf_counter()
-            srv.wait(submit(srv, sp))
+            j = submit(srv, sp, xa=out_buf(sp))
+            srv.wait(j)
             alone.append(time.perf_counter() - t0)
+            first.append(j.xa)
         mean_service = statistics.mean(alone)
         rate = args.serve_load / mean_service
         rng = np.random.default_rng(7)
         gaps = rng.exponential(1.0 / rate, args.serve_requests)
         picks = rng.integers(0, len(specs), args.serve_requests)
-        jobs = []
+        jobs, pending = [], []
+
+        def collect(block):
+            # results collected (the latency is the server's submit -> done);
+            # their output buffers return to the domain's pool
+            keep = []
+            for k, j in pending:
+                r = srv.wait(j, timeout=None if block else 0.0)
+                if r["status"] == LETKF_PENDING:
+                    keep.append((k, j))
+                else:
+                    pools[specs[k]["name"]].append(j.xa)
+                    j.xa = None
+            pending[:] = keep
+
         t0 = time.perf_counter()
         t_next = 0.0
         for g, k in zip(gaps, picks):
             t_next += g
+            collect(False)
             dt = t0 + t_next - time.perf_counter()
             if dt > 0:
                 time.sleep(dt)
-            jobs.append((k, submit(srv, specs[k])))
-        for _, j in jobs:
-            srv.wait(j)
-            j.xa = None
+            j = submit(srv, specs[k], xa=out_buf(specs[k]))
+            jobs.append((k, j))
+            pending.append((k, j))
+        collect(True)
         st = srv.stats()
     lat = np.array([j.result["latency_s"] for _, j in jobs])
     span = max(j.result["t_done"] for _, j in jobs) - min(j.result["t_submit"] for _, j in jobs)
     points = sum(specs[k]["npts"] for k, _ in jobs)
+    errors = serving_errors(specs, first, submit)
+    per = {}
+    for k, j in jobs:
+        per.setdefault(specs[k]["name"], []).append(j.result["latency_s"])
+    per_domain = {n: {"requests": len(v), "p50_ms": round(float(np.percentile(v, 50)) * 1e3, 1),
+                      "p99_ms": round(float(np.percentile(v, 99)) * 1e3, 1)} for n, v in per.items()}
     return {"requests": int(args.serve_requests), "slots": int(args.serve_slots), "offered_load": args.serve_load,
             "arrival_rate_hz": rate, "p50_latency_ms": float(np.percentile(lat, 50) * 1e3),
             "p99_latency_ms": float(np.percentile(lat, 99) * 1e3), "points_per_s": points / span,
             "jobs_per_s": len(jobs) / span,
             "service_alone_ms": {sp["name"]: round(a * 1e3, 2) for sp, a in zip(specs, alone)},
             "resident_domains": int(st["resident_domains"]), "peak_device_bytes": int(st["peak_bytes"]),
-            "host_buffers": "pageable numpy arrays (copied in the timed latency)"}
+            "per_domain": per_domain, "error_vs_fp64_oracle": errors,
+            "host_buffers": "page-locked (copied in the timed latency)"}
+
+
+def serving_errors(specs, first, submit):
+    """Analysis-mean and perturbation RMS error, over the background spread,
+    of each domain's first served analysis: regional domains against the
+    oracle's SCALE grid loop on 512 sampled points; Lorenz-96 rings against
+    the same job in the FP64 plain form (within 1e-10 of the oracle by the
+    tests)."""
+    from letkf_gb300.serve import PREC_F64, Server
+
+    out = {}
+    nthreads = os.cpu_count() or 1
+    for sp, xa in zip(specs, first):
+        if sp["kind"] == "sweep":
+            wl = sp["wl"]
+            so, hd, dp = cpu_oracle_setup(wl, sp["obs_np"])
+            idx = sample_points(wl, 512, seed=3)
+            _, xb_s, xa_ref, _, _ = cpu_oracle_run(wl, so, hd, dp, idx, nthreads)
+            got = xa[:, idx, :].astype(np.float64)
+            xp = xb_s - xb_s.mean(-1, keepdims=True)
+            points = int(idx.size)
+            ref_name = "oracle"
+        else:
+            with Server(nslots=1) as s64:
+                j = submit(s64, sp, precision=PREC_F64, domain=-1)
+                s64.wait(j)
+                xa_ref = j.xa[None]
+            got = xa.astype(np.float64)[None]
+            xb = np.asarray(sp["xf"], dtype=np.float64)[None]
+            xp = xb - xb.mean(-1, keepdims=True)
+            points = int(sp["npts"])
+            ref_name = "FP64 plain form"
+        spread = np.sqrt((xp ** 2).sum(-1) / (xp.shape[-1] - 1)).mean()
+        pert = lambda x: x - x.mean(-1, keepdims=True)
+        em = float(np.sqrt(np.mean((got.mean(-1) - xa_ref.mean(-1)) ** 2)) / spread)
+        ep = float(np.sqrt(np.mean((pert(got) - pert(xa_ref)) ** 2)) / spread)
+        out[sp["name"]] = {"analysis_mean_rms_over_spread": em, "perturbation_rms_over_spread": ep,
+                           "points": points, "reference": ref_name}
+    return out
 
 
 # --------------------------------------------------------------- large k
@@ -629,7 +708,10 @@ def run_gpu(args, rank, world, dist):
     tc_on = bool(args.tc and args.ne <= 64 and args.eig == "newton-schulz")
     if tuned is not None:
         tc_on = tuned["tensor_cores"]
-    kernel = "sweep_tc_kernel" if tc_on else f"sweep_mixed_kernel<{64 if args.ne <= 64 else 128}>"
+    if tc_on:
+        kernel = "sweep_tc_kernel" if args.ne <= 64 else "sweep_tc128_kernel"
+    else:
+        kernel = f"sweep_mixed_kernel<{32 if args.ne <= 32 else 64 if args.ne <= 64 else 128}>"
     peaks, src = measured_peaks()
     flops = algorithmic_flops(nobsl, args.ne, args.nv)
     ach = flops / (t / args.steps) / 1e12
@@ -651,7 +733,7 @@ def run_gpu(args, rank, world, dist):
     nl = nobsl.astype(np.float64)
     out["local_obs"] = {"min": int(nl.min()), "mean": float(nl.mean()), "p50": float(np.median(nl)),
                         "p99": float(np.percentile(nl, 99)), "max": int(nl.max()), "zero_frac": float((nl == 0).mean())}
-    out["transform"] = {"method": args.eig, "tensor_cores": bool(args.tc and args.ne <= 64 and args.eig == "newton-schulz"),
+    out["transform"] = {"method": args.eig, "tensor_cores": tc_on,
                         "scaled_steps": bool(args.tc_scaling), "autotune": tuned,
                         "deferred_to_jacobi": sw.deferred(),
                         "iterations_mean": float(dg["sweeps"][nobsl > 0].mean()) if (nobsl > 0).any() else 0.0,

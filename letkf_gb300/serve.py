@@ -75,6 +75,14 @@ def _f64(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 
 
+def _out_like(x, out):
+    if out is None:
+        return np.empty_like(x)
+    if out.shape != x.shape or out.dtype != x.dtype or not out.flags.c_contiguous:
+        raise ValueError("xa must be a contiguous array of the input's shape and type")
+    return out
+
+
 class Job:
     """A submitted job: its id, descriptor and the arrays it references."""
 
@@ -100,11 +108,12 @@ class Server:
         return job
 
     def submit_sweep(self, pri, prj, prlev, params, nlon, nlat, obs, hdxf, dep, xb, infl=None, precision=PREC_MIXED,
-                     domain=-1, minfl=0.0):
+                     domain=-1, minfl=0.0, xa=None):
         """A regional sweep job (letkf_sweep_* semantics).  obs: dict ri, rj,
         lev, dat, err (float64) and cls (int32), unsorted; hdxf [nobs, ne];
         xb [nv, npts, ne] (float32 for PREC_MIXED, else float64); params: dict
-        with the SCALE search parameters."""
+        with the SCALE search parameters.  xa: the output array (like xb; a
+        new array when None), for instance page-locked memory."""
         dt = np.float32 if precision == PREC_MIXED else np.float64
         xb = np.ascontiguousarray(xb, dtype=dt)
         nv, npts, ne = xb.shape
@@ -113,7 +122,7 @@ class Server:
                 "cls": np.ascontiguousarray(obs["cls"], dtype=np.int32)}
         for k in ("ri", "rj", "lev", "dat", "err"):
             keep["o" + k] = _f64(obs[k])
-        xa = np.empty_like(xb)
+        xa = _out_like(xb, xa)
         inf = None if infl is None else _f64(infl).copy()
         d = JobDesc()
         d.kind, d.domain, d.precision, d.ne, d.nv = JOB_SCALE_SWEEP, int(domain), int(precision), ne, nv
@@ -132,7 +141,7 @@ class Server:
         return self._submit(Job(d, keep, xa, inf, npts))
 
     def submit_l96(self, xf, hdxf, dep, obs_cell, obserr=1.0, xlocal=3.0, msw_infl=1.05, infl=None,
-                   precision=PREC_F64, domain=-1):
+                   precision=PREC_F64, domain=-1, xa=None):
         """A Lorenz-96 analysis job (lorenz96/letkf/letkf.f90:180-265): xf
         [nx, ne] float64 members, hdxf [ny, ne] and dep [ny] from
         core.obs_departure semantics, obs_cell [ny] 1-based grid indices."""
@@ -140,7 +149,7 @@ class Server:
         nx, ne = xf.shape
         keep = {"xb": xf, "hdxf": _f64(hdxf), "dep": _f64(dep),
                 "cell": np.ascontiguousarray(obs_cell, dtype=np.int32)}
-        xa = np.empty_like(xf)
+        xa = _out_like(xf, xa)
         inf = None if infl is None else _f64(infl).copy()
         d = JobDesc()
         d.kind, d.domain, d.precision, d.ne, d.nv = JOB_L96, int(domain), int(precision), ne, 1

@@ -39,7 +39,7 @@ def _spread(xb):
 def test_tc_polish_against_oracle(cuda, ne):
     """The anchored polish step on the tensor cores (LETKF_OPT_TC_POLISH)
     meets the mixed-form bar against the oracle."""
-    from letkf_gb300.sweep import OPT_TC_POLISH, PREC_MIXED, Sweep
+    from letkf_gb300.sweep import OPT_TC_POLISH, OPT_TENSOR_CORES, PREC_MIXED, Sweep
 
     case, prm, perm, grd, so, varloc, hdxf, dep = _setup(ne=ne, f32=True)
     xb = case["xb"].astype(np.float64)
@@ -50,6 +50,7 @@ def test_tc_polish_against_oracle(cuda, ne):
     sw.set_points(case["pri"], case["prj"], case["prlev"])
     sw.set_obs(case["ri"], case["rj"], case["lev"], case["dat"], case["err"], dep, case["cls"],
                hdxf.astype(np.float32))
+    sw.set_option(OPT_TENSOR_CORES, 1)
     sw.set_option(OPT_TC_POLISH, 1)
     sw.set_background(case["xb"])
     sw.set_inflation(infl0)
