@@ -405,10 +405,9 @@ int letkf_l96_obs_cell(int nx, int ny, const double* h, int* cell, void* stream)
 #define LETKF_OPT_EIGENSOLVER 3 /* transform of the mixed form: */
 #define LETKF_EIG_NEWTON_SCHULZ 0 /*   W = sqrt((k-1)) A^(-1/2) by Newton-Schulz (default) */
 #define LETKF_EIG_JACOBI 1        /*   eigen-decomposition by parallel Jacobi */
-#define LETKF_OPT_TENSOR_CORES 4  /* 1: Gram and Newton-Schulz on tcgen05 for ne <= 128 (ne <= 64: four CTAs per
-                                     SM; 64 < ne <= 128: one CTA of 256 threads per SM); 0: the FP32 SIMT sweep;
-                                     2 (default): tcgen05 for 32 < ne <= 128, SIMT for ne <= 32 (measured faster
-                                     there: 39.5 against 44 ms on a 128x128x20 regional sweep at ne = 20) */
+#define LETKF_OPT_TENSOR_CORES 4  /* 1 (default): Gram and Newton-Schulz on tcgen05 for ne <= 128 (ne <= 64: four
+                                     CTAs per SM; 64 < ne <= 128: one CTA of 256 threads per SM); 0: the FP32 SIMT
+                                     sweep */
 #define LETKF_OPT_TC_NS_ITERS 5   /* tensor-core Newton-Schulz iterations before the FP32 ones (default 14) */
 #define LETKF_OPT_TC_NS_SCALING 6 /* 1 (default): spectrum-scaled tensor-core Newton-Schulz steps; 0: plain */
 #define LETKF_OPT_TC_NS_TOL 7     /* v: the tensor-core phase ends once ||ZY - I||_F^2 < 10^-v (1..7, default 3) */

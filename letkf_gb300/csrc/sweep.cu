@@ -228,7 +228,7 @@ struct letkf_sweep_s {
   int grid_cap = 0;
   int max_sweeps = 12;
   int use_ns = 1;
-  int use_tc = 2;  // 0 SIMT, 1 tensor cores for ne <= 128, 2 tensor cores for 32 < ne <= 128
+  int use_tc = 1;
   int tc_ns_max = 14;
   int tc_ns_scaled = 1;
   int tc_ns_tol_exp = 3;
@@ -561,7 +561,7 @@ int letkf_sweep_set_option(letkf_sweep_t h, int option, int value) {
       h->max_sweeps = value;
       return LETKF_OK;
     case LETKF_OPT_TENSOR_CORES:
-      if (value < 0 || value > 2) return LETKF_ERR_ARG;
+      if (value != 0 && value != 1) return LETKF_ERR_ARG;
       h->use_tc = value;
       return LETKF_OK;
     case LETKF_OPT_TC_NS_ITERS:
@@ -782,10 +782,7 @@ static void build_args(letkf_sweep_t h, SweepArgs& a) {
 }
 
 // tensor-core sweeps: sweep_tc.cu for ne <= 64, sweep_tc128.cu for 64 < ne <= 128
-static bool tc_path(letkf_sweep_t h) {
-  const bool tc = h->use_tc == 1 || (h->use_tc == 2 && h->d.ne > 32);
-  return tc && h->use_ns && h->d.ne <= 128;
-}
+static bool tc_path(letkf_sweep_t h) { return h->use_tc && h->use_ns && h->d.ne <= 128; }
 
 static int launch_tc(letkf_sweep_t h, const SweepArgs& a, cudaStream_t s) {
   return h->d.ne <= 64 ? launch_sweep_tc(a, s, h->grid_cap) : launch_sweep_tc128(a, s, h->grid_cap);

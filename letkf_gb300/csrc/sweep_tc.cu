@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
       if (tid == 0) reinterpret_cast<float*>(ctrl)[1] = (float)((double)(n - 1) / infl);
       // G = D0[r] + D0[r+64] + D1[r] + D1[r+64]: warps 2-3 first, then warps 0-1 add
       if (wid >= 2) {
-#pragma unroll
+#pragma unroll 1
         for (int c0 = 0; c0 < 64; c0 += 16) {
           float v0[16], v1[16];
           tc::tmem_ld16(D0 + lane_off + c0, v0);
@@ -330,7 +330,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
       __syncthreads();
       const float cdiag = reinterpret_cast<const float*>(ctrl)[1];
       if (wid < 2) {
-#pragma unroll
+#pragma unroll 1
         for (int c0 = 0; c0 < 64; c0 += 16) {
           float v0[16], v1[16];
           tc::tmem_ld16(D0 + lane_off + c0, v0);
@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
         // keep the exact FP32 A in the Gram's second accumulator (lanes 0..63 of
         // columns 64..127); the Newton-Schulz products only use columns 0..63
         if (wid < 2) {
-#pragma unroll
+#pragma unroll 1
           for (int c0 = 0; c0 < 64; c0 += 16) {
             float v[16];
 #pragma unroll
@@ -449,7 +449,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
         const float s = a.tc_scale_bound ? fminf(fro, gmax) : fmaxf(1.05f * lam, 0.5f * gmax);
         const float inv_s = 1.f / s;
         // S = [A/s ; I] split into bf16 hi / lo (row r per thread)
-#pragma unroll
+#pragma unroll 1
         for (int c0 = 0; c0 < 64; c0 += 8) {
           float v[8];
           if (r < 64) {
@@ -509,7 +509,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
           tc::fence_after_sync();
           float e2 = 0.f;
           if (wid >= 2) {
-#pragma unroll
+#pragma unroll 1
             for (int c0 = 0; c0 < 64; c0 += 16) {
               float v[16];
               tc::tmem_ld16(D0 + lane_off + c0, v);
@@ -561,7 +561,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
           } else {
             lo = f_ns(lo);
           }
-#pragma unroll
+#pragma unroll 1
           for (int c0 = 0; c0 < 64; c0 += 16) {
             float v[16];
             tc::tmem_ld16(D0 + lane_off + c0, v);
@@ -600,7 +600,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
           for (bool last = false; !last && !tmo;) {
             // B <- A / s (row r of A from TMEM lanes 0..63)
             if (wid < 2) {
-#pragma unroll
+#pragma unroll 1
               for (int c0 = 0; c0 < 64; c0 += 16) {
                 float v[16];
                 tc::tmem_ld16(D1 + lane_off + c0, v);
@@ -628,7 +628,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
             tc::fence_after_sync();
             // S rows 0..63 <- P (from rows 64..127 of D); B <- Z
             if (wid >= 2) {
-#pragma unroll
+#pragma unroll 1
               for (int c0 = 0; c0 < 64; c0 += 16) {
                 float v[16];
                 tc::tmem_ld16(D0 + lane_off + c0, v);
@@ -659,7 +659,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
             // B <- R = Q - I (rows 0..63 of D); ||R||_F^2
             float e2 = 0.f;
             if (wid < 2) {
-#pragma unroll
+#pragma unroll 1
               for (int c0 = 0; c0 < 64; c0 += 16) {
                 float v[16];
                 tc::tmem_ld16(D0 + lane_off + c0, v);
@@ -697,7 +697,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
             }
             // Z <- Z - Z R / 2 (rows 64..127); the last step writes W = coef Z
             if (wid >= 2) {
-#pragma unroll
+#pragma unroll 1
               for (int c0 = 0; c0 < 64; c0 += 16) {
                 float v[16];
                 tc::tmem_ld16(D0 + lane_off + c0, v);
@@ -753,7 +753,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
           float* Pf = reinterpret_cast<float*>(sm + L::ZF);  // A Z, then Q; the probe vectors
           if (r >= 64) {
             float* dst = Zf + (r - 64) * 64;
-  #pragma unroll
+  #pragma unroll 1
             for (int c0 = 0; c0 < 64; c0 += 8) {
               const uint32_t off = tc::kmajor_off_bf16(r, c0, 64);
               float sh[8], sl[8];
@@ -766,7 +766,7 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
           }
           __syncthreads();
           if (r < 64) {
-  #pragma unroll
+  #pragma unroll 1
             for (int c0 = 0; c0 < 64; c0 += 16) {
               float v[16];
               tc::tmem_ld16(D1 + lane_off + c0, v);
