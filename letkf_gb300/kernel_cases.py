@@ -8,6 +8,9 @@ where the kernel streams the ensemble):
                 points, k = 64, 6 variables, 140,625 clustered obs) and its
                 deferred-point pass
   sweep_simt    the same sweep on the SIMT kernel
+  sweep_tc128   the tensor-core sweep of the same domain with k = 128
+  search_700km  SPEEDY lat/lon search (count and fill) of 64 points of the
+                360x181x32 global grid with 3e6 observations at 700 km
   f64           FP64 plain form of 8,192 of those points: search (count,
                 fill), gather, core_f64, update_f64
   l96           Lorenz-96 ring of 100,000 variables, k = 32: departures,
@@ -33,22 +36,22 @@ import time
 import numpy as np
 
 
-def _regional():
+def _regional(ne=64):
     from .workload import RegionalWorkload
 
-    return RegionalWorkload(5, 96, 96, 16, 64, 140_625, 6)
+    return RegionalWorkload(5, 96, 96, 16, ne, 140_625, 6)
 
 
-def case_sweep(dev, tc):
+def case_sweep(dev, tc, ne=64):
     import torch
 
     from .sweep import OPT_TENSOR_CORES, PREC_MIXED, Sweep
 
-    wl = _regional()
+    wl = _regional(ne)
     hdxf, dep, dat = wl.obs_torch(dev)
     xb = wl.background_torch(dev)
     ri, rj, plev = wl.points()
-    sw = Sweep(64, wl.nvar, wl.nlon, wl.nlat, wl.npts, wl.params, precision=PREC_MIXED)
+    sw = Sweep(ne, wl.nvar, wl.nlon, wl.nlat, wl.npts, wl.params, precision=PREC_MIXED)
     sw.set_points(ri, rj, plev, tile=4)
     sw.set_obs(wl.ri, wl.rj, wl.lev, dat, wl.err, dep, wl.cls, hdxf)
     sw.set_option(OPT_TENSOR_CORES, int(tc))
@@ -152,6 +155,30 @@ def case_largek(dev):
     return f"{npts} points (k = {ne}, mean L = {Ls.mean():.0f}), {dt * 1e3:.1f} ms, {npts / dt:.0f} points/s, {ok} ok"
 
 
+def case_search_700km(dev):
+    import torch
+
+    from .core import search_speedy
+    from .workload import GlobalWorkload
+
+    wl = GlobalWorkload(21)
+    params = wl.search_params(700.0e3)
+    idx = np.sort(np.random.default_rng(5).choice(wl.npts, 64, replace=False))
+    lon, lat, dlon, ilev, lnp = wl.points(idx, params)
+    f = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
+    grid = {"lon": f(wl.lon), "lat": f(wl.lat), "nobsgrd": torch.as_tensor(wl.nobsgrd, dtype=torch.int32, device=dev)}
+    obs = {"elm": f(wl.elm), "lon": f(wl.olon), "lat": f(wl.olat), "lev": f(wl.olev), "dat": f(wl.olev),
+           "err": f(wl.err)}
+    pts = {"lon": f(lon), "lat": f(lat), "dlon_zero": f(dlon), "ilev": torch.as_tensor(ilev, device=dev),
+           "logpfm": f(lnp)}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    offs, oi, rl, rd = search_speedy(grid, obs, pts, params, np.ones(7))
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    return f"64 points of the 360x181x32 grid, 3e6 obs, 700 km: {int(offs[-1])} local obs, {dt * 1e3:.1f} ms"
+
+
 def _speedy_members(dev, ne=80, nlon=192, nlat=96, nlev=7):
     import torch
 
@@ -233,6 +260,7 @@ def case_obs_space(dev):
 
 
 CASES = {"sweep_tc": lambda d: case_sweep(d, True), "sweep_simt": lambda d: case_sweep(d, False),
+         "sweep_tc128": lambda dev: case_sweep(dev, True, ne=128), "search_700km": case_search_700km,
          "f64": case_f64, "l96": case_l96, "relax": case_relax, "largek": case_largek,
          "speedy_io": case_speedy_io, "obsope": case_obsope, "obs_space": case_obs_space}
 
