@@ -21,6 +21,12 @@ struct ScaleParams {
       sigma_obs_radar, sigma_obs_radar_noref, sigma_obsz_radar, radar_ref_thres_dbz, sigma_obs_tc, sigma_obsv_tc;
 };
 
+// One warp per grid point: lane l tests candidates ib + l, ib + l + 32, ...
+// of each row range; accepted ones are written in candidate order through a
+// ballot prefix.  A candidate is first tested in FP32 and rejected there only
+// where its normalised distance exceeds the cut-off by more than 1e-3
+// (FP32 rounding of these terms is below 1e-5); every other candidate takes
+// the reference's FP64 test.
 __global__ void search_scale_kernel(int nlon, int nlat, const int* __restrict__ G, int nobs,
                                     const double* __restrict__ ori, const double* __restrict__ orj,
                                     const double* __restrict__ olev, const double* __restrict__ odat,
@@ -30,8 +36,9 @@ __global__ void search_scale_kernel(int nlon, int nlat, const int* __restrict__ 
                                     const double* __restrict__ prz, const double* __restrict__ var_local,
                                     ScaleParams P, const int64_t* __restrict__ offs, int* nobsl, int* idx,
                                     double* rloc, double* rdiag) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int p = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   if (p >= npts) return;
+  const int lane = threadIdx.x & 31;
   const int ld = nlon + 1;
   const double ri = pri[p], rj = prj[p], rlev = prlev[p], rz = prz ? prz[p] : 0.0;
   const double logr = log(rlev);
@@ -44,50 +51,83 @@ __global__ void search_scale_kernel(int nlon, int nlat, const int* __restrict__ 
   int jmax = (int)ceil(rj + P.dlat_zero);
   if (jmax > nlat) jmax = nlat;
   const double dzf2 = scale_dzf2();
+  const float cut32 = (float)dzf2 * 1.001f;
+  const float logr32 = (float)logr, rz32 = (float)rz;
   int cnt = 0;
   const int64_t base = idx ? offs[p] : 0;
   if (nobs > 0 && G[(size_t)(nlat - 1) * ld + nlon] > 0 && imin <= imax && jmin <= jmax) {
     for (int j = jmin; j <= jmax; j++) {
       const int ib = G[(size_t)(j - 1) * ld + imin - 1], ie = G[(size_t)(j - 1) * ld + imax];
-      for (int ob = ib; ob < ie; ob++) {
-        const int vl = ovarloc[ob];
-        if (var_local && var_local[vl] < 2.2250738585072014e-308) continue;
-        const double rdx = (ri - ori[ob]) * P.dx, rdy = (rj - orj[ob]) * P.dy;
-        double nd_h = sqrt(sumsq_rn(rdx, rdy)), nd_v;
-        const int cls = ocls[ob];
-        if (cls == 1) {
-          nd_h = nd_h / P.sigma_obs;
-          nd_v = fabs(log(odat[ob]) - logr) / P.sigma_obsv;
-        } else if (cls == 2) {
-          nd_h = nd_h / P.sigma_obs_rain;
-          nd_v = fabs(log(P.base_obsv_rain) - logr) / P.sigma_obsv_rain;
-        } else if (cls >= 3 && cls <= 5) {
-          if (cls == 3 && odat[ob] <= P.radar_ref_thres_dbz + 1.0e-6)
-            nd_h = nd_h / P.sigma_obs_radar_noref;
-          else
-            nd_h = nd_h / P.sigma_obs_radar;
-          nd_v = fabs(olev[ob] - rz) / P.sigma_obsz_radar;
-        } else if (cls == 6) {
-          nd_h = nd_h / P.sigma_obs_tc;
-          nd_v = fabs(log(olev[ob]) - logr) / P.sigma_obsv_tc;
-        } else {
-          nd_h = nd_h / P.sigma_obs;
-          nd_v = fabs(log(olev[ob]) - logr) / P.sigma_obsv;
+      for (int ob0 = ib; ob0 < ie; ob0 += 32) {
+        const int ob = ob0 + lane;
+        bool ok = ob < ie;
+        double ndist = 0.0;
+        int vl = 0;
+        if (ok) {
+          vl = ovarloc[ob];
+          if (var_local && var_local[vl] < 2.2250738585072014e-308) ok = false;
         }
-        const double ndist = sumsq_rn(nd_h, nd_v);
-        if (ndist > dzf2) continue;
-        if (idx) {
+        const int cls = ok ? ocls[ob] : 0;
+        if (ok) {
+          // FP32 pre-test (certain rejections only)
+          const float hx = (float)((ri - ori[ob]) * P.dx), hy = (float)((rj - orj[ob]) * P.dy);
+          float sh, vz;
+          if (cls == 2) {
+            sh = (float)P.sigma_obs_rain;
+            vz = fabsf(__logf((float)P.base_obsv_rain) - logr32) / (float)P.sigma_obsv_rain;
+          } else if (cls >= 3 && cls <= 5) {
+            sh = (float)((cls == 3 && odat[ob] <= P.radar_ref_thres_dbz + 1.0e-6) ? P.sigma_obs_radar_noref
+                                                                                 : P.sigma_obs_radar);
+            vz = fabsf((float)olev[ob] - rz32) / (float)P.sigma_obsz_radar;
+          } else if (cls == 6) {
+            sh = (float)P.sigma_obs_tc;
+            vz = fabsf(__logf((float)olev[ob]) - logr32) / (float)P.sigma_obsv_tc;
+          } else {
+            sh = (float)P.sigma_obs;
+            vz = fabsf(__logf((float)(cls == 1 ? odat[ob] : olev[ob])) - logr32) / (float)P.sigma_obsv;
+          }
+          const float hh = (hx * hx + hy * hy) / (sh * sh);
+          ok = !(hh + vz * vz > cut32);
+        }
+        if (ok) {
+          const double rdx = (ri - ori[ob]) * P.dx, rdy = (rj - orj[ob]) * P.dy;
+          double nd_h = sqrt(sumsq_rn(rdx, rdy)), nd_v;
+          if (cls == 1) {
+            nd_h = nd_h / P.sigma_obs;
+            nd_v = fabs(log(odat[ob]) - logr) / P.sigma_obsv;
+          } else if (cls == 2) {
+            nd_h = nd_h / P.sigma_obs_rain;
+            nd_v = fabs(log(P.base_obsv_rain) - logr) / P.sigma_obsv_rain;
+          } else if (cls >= 3 && cls <= 5) {
+            if (cls == 3 && odat[ob] <= P.radar_ref_thres_dbz + 1.0e-6)
+              nd_h = nd_h / P.sigma_obs_radar_noref;
+            else
+              nd_h = nd_h / P.sigma_obs_radar;
+            nd_v = fabs(olev[ob] - rz) / P.sigma_obsz_radar;
+          } else if (cls == 6) {
+            nd_h = nd_h / P.sigma_obs_tc;
+            nd_v = fabs(log(olev[ob]) - logr) / P.sigma_obsv_tc;
+          } else {
+            nd_h = nd_h / P.sigma_obs;
+            nd_v = fabs(log(olev[ob]) - logr) / P.sigma_obsv;
+          }
+          ndist = sumsq_rn(nd_h, nd_v);
+          ok = !(ndist > dzf2);
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, ok);
+        if (ok && idx) {
+          const int64_t at = base + cnt + __popc(bal & ((1u << lane) - 1u));
           double nrloc = exp(-0.5 * ndist);
           if (var_local) nrloc = nrloc * var_local[vl];
-          idx[base + cnt] = ob;
-          rloc[base + cnt] = nrloc;
-          rdiag[base + cnt] = oerr[ob] * oerr[ob] / nrloc;
+          idx[at] = ob;
+          rloc[at] = nrloc;
+          rdiag[at] = oerr[ob] * oerr[ob] / nrloc;
         }
-        cnt++;
+        cnt += __popc(bal);
       }
     }
   }
-  if (!idx) nobsl[p] = cnt;
+  if (!idx && lane == 0) nobsl[p] = cnt;
 }
 
 // common/common.f90:401-424 (pi and re of common/common.f90:28,35)
@@ -377,16 +417,6 @@ static void launch_speedy_warps(const SpeedyCtx& c, int npts, const double* plon
   note_launch();
 }
 
-// one thread per point: CTAs small enough that the grid covers the SMs twice
-static int search_block(int npts) {
-  int dev = 0, nsm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  if (npts >= 2 * nsm * 128) return 128;
-  if (npts >= 2 * nsm * 64) return 64;
-  return 32;
-}
-
 int launch_search_scale(int nlon, int nlat, const int* G, int nobs, const double* ori, const double* orj,
                         const double* olev, const double* odat, const double* oerr, const int* ocls,
                         const int* ovarloc, int npts, const double* pri, const double* prj, const double* prlev,
@@ -396,10 +426,11 @@ int launch_search_scale(int nlon, int nlat, const int* G, int nobs, const double
   ScaleParams P;
   double* f = &P.dx;
   for (int i = 0; i < 15; i++) f[i] = params[i];
-  const int bs = search_block(npts);
-  search_scale_kernel<<<(npts + bs - 1) / bs, bs, 0, stream>>>(nlon, nlat, G, nobs, ori, orj, olev, odat, oerr,
-                                                                 ocls, ovarloc, npts, pri, prj, prlev, prz,
-                                                                 var_local, P, offs, nobsl, idx, rloc, rdiag);
+  const int64_t threads = (int64_t)npts * 32;  // one warp per point
+  const int bs = 128;
+  search_scale_kernel<<<(unsigned)((threads + bs - 1) / bs), bs, 0, stream>>>(
+      nlon, nlat, G, nobs, ori, orj, olev, odat, oerr, ocls, ovarloc, npts, pri, prj, prlev, prz, var_local, P, offs,
+      nobsl, idx, rloc, rdiag);
   note_launch();
   return cuda_status(cudaGetLastError());
 }
