@@ -81,7 +81,7 @@ def parse():
     ap.add_argument("--no-configs", action="store_true", help="skip the Lorenz-96 and SPEEDY-grid parity lines")
     ap.add_argument("--largek-points", type=int, default=4096,
                     help="sampled points of the large-ensemble sweep at 60 km")
-    ap.add_argument("--largek-700-points", type=int, default=256,
+    ap.add_argument("--largek-700-points", type=int, default=64,
                     help="sampled points of the large-ensemble sweep at the stated 700 km")
     ap.add_argument("--serve-requests", type=int, default=500, help="requests of the serving measurement")
     ap.add_argument("--serve-slots", type=int, default=3, help="jobs on the device at once")
@@ -530,6 +530,7 @@ def run_largek(args, dev):
            "workload": f"global {wl.nlon}x{wl.nlat}x{wl.nlev}, {wl.nvar} vars, k={wl.ne}, {wl.nobs} obs, "
                        f"sigma_v={wl.sigma_obsv} ln p (SPEEDY lat/lon search)"}
     for sigma, npts_s, nerr in ((700.0e3, args.largek_700_points, 8), (60.0e3, args.largek_points, 256)):
+        # (at 700 km the mixed-precision transform does not certify and the core's FP64 pass answers)
         params = wl.search_params(sigma)
         rng = np.random.default_rng(5)
         idx = np.sort(rng.choice(wl.npts, npts_s, replace=False))
@@ -591,8 +592,8 @@ def run_largek(args, dev):
         key = f"sigma_{sigma / 1e3:.0f}km"
         out[key] = {"sigma_h_m": sigma, "sample_points": int(idx.size), "value": idx.size / t, "unit": UNIT,
                     "ms_per_sample": t * 1e3,
-                    "step": "search + large-k core over the index lists (tensor-core Gram and Newton-Schulz) + "
-                            "BF16-storage update, CUDA events",
+                    "step": "search + large-k core over the index lists (tensor-core Gram and Newton-Schulz; FP64 "
+                            "pass for points that do not certify) + BF16-storage update, CUDA events",
                     "local_obs": {"min": int(nl.min()), "mean": float(nl.mean()), "p50": float(np.median(nl)),
                                   "max": int(nl.max())},
                     "status_ok": int((status == 0).sum()),

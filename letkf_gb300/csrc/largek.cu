@@ -544,6 +544,12 @@ extern "C" int letkf_update_bf16(int ne, int npts, int nv, const float* xmean, c
   return launch_lk_update<true>(ne, npts, nv, xpert, xmean, trans, transm, apert, amean, (cudaStream_t)stream);
 }
 
+namespace letkf {
+int largek_fp64_pass(int ne, int npts, const int64_t* offs, const float* rows, const __nv_bfloat16* rows16,
+                     const int* ridx, const float* rdiag, const float* rloc, const float* dep, double* parm_infl,
+                     float* trans, float* transm, int rdiag_wloc, double minfl, int* status, cudaStream_t s);
+}  // namespace letkf
+
 // the large-ensemble core over packed rows (rows, dep per list entry) or over
 // index lists into the observation ensemble (ridx; FP32 rows or BF16 rows16,
 // dep per observation)
@@ -718,6 +724,10 @@ static int largek_core(int ne, int npts, const int64_t* offs, const float* rows,
   void* fr[] = {w, G, Y, Z, Yn, Zn, T, bvec, e2, inv_s, alphas, betas, active, count, err, pt, restart};
   for (void* p : fr)
     if (p) cudaFreeAsync(p, s);
+  // points whose mixed-precision transform did not certify: the FP64 pass
+  if (st == LETKF_OK)
+    st = largek_fp64_pass(ne, npts, offs, rows, rows16, ridx, rdiag, rloc, dep, parm_infl, trans, transm, rdiag_wloc,
+                          minfl, status, s);
   return st;
 }
 

@@ -223,3 +223,34 @@ def test_largek_long_lists_against_oracle(cuda):
         assert np.abs(tr[p] - ref["trans"][p]).max() <= 1e-4 * scale, p
         assert np.abs(tm[p] - ref["transm"][p]).max() <= 1e-4 * scale, p
     np.testing.assert_allclose(pinf.cpu().numpy(), ref["parm_infl"], rtol=1e-5)
+
+
+def test_fp64_pass_answers_ill_conditioned_points(cuda):
+    """Points the mixed-precision transform cannot certify (observation-error
+    variances x1e-4: lambda_max / c up to ~1e5, tr(G) above the core's 1e6 c
+    truncation guard) are redone in FP64 (Gram and Newton-Schulz): every point
+    comes back LETKF_OK with its transform within 1e-5 of the oracle's largest
+    entry and the inflation within 1e-8."""
+    import torch
+
+    from letkf_gb300.core import core_batch_largek
+    from letkf_gb300.lib import LETKF_OK
+
+    ne = 256
+    rng = np.random.default_rng(10_000)
+    Ls = [300, 700, 150, 512, 90, 1000, 33, 400]
+    offs, rows, rd, rl, d, infl = _batch(rng, ne, Ls)
+    rd = (rd * 1e-4).astype(np.float32).astype(np.float64)
+    ref = O.letkf_core_batch(ne, offs, rows, rd, rl, d, infl, want_transm=True)
+    t = lambda a, dt=torch.float32: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=cuda)
+    pinf = t(infl, torch.float64)
+    out = core_batch_largek(ne, t(offs, torch.int64), t(rows), t(rd), t(rl), t(d), pinf, want_transm=True)
+    torch.cuda.synchronize()
+    assert (out["status"].cpu().numpy() == LETKF_OK).all()
+    tr = out["trans"].cpu().numpy().astype(np.float64)
+    tm = out["transm"].cpu().numpy().astype(np.float64)
+    for p in range(len(Ls)):
+        scale = np.abs(ref["trans"][p]).max()
+        assert np.abs(tr[p] - ref["trans"][p]).max() <= 1e-5 * scale, (p, Ls[p])
+        assert np.abs(tm[p] - ref["transm"][p]).max() <= 1e-5 * scale, (p, Ls[p])
+    np.testing.assert_allclose(pinf.cpu().numpy(), ref["parm_infl"], rtol=1e-8)
