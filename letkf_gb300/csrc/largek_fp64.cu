@@ -7,9 +7,10 @@
 // lists, small observation errors), the smallest eigen-directions of W are
 // then not resolved and the core reports LETKF_ERR_EIG.  This pass redoes those
 // points in FP64, the reference's precision (common/common_letkf.f90:101-239):
-//   1. rows of the point gathered in FP64 (Y and Yw = w Y, w = rloc / rdiag or
-//      1 / rdiag with rdiag_wloc), G = Ywᵀ Y and b = Ywᵀ dep by cuBLAS DGEMM /
-//      DGEMV (plain library products);
+//   1. rows of the point gathered in FP64 and scaled, B = sqrt(w) Y with
+//      w = rloc / rdiag (1 / rdiag with rdiag_wloc), G = Bᵀ B by cuBLAS DGEMM
+//      (measured 2.4x faster than DSYRK's triangle here, which computes half
+//      the products) and b = Bᵀ (sqrt(w) dep) by DGEMV;
 //   2. A = G + cI, s = Gershgorin bound, Y0 = A / s, Z0 = I;
 //   3. coupled Newton-Schulz in FP64, batched over the points (cuBLAS
 //      strided-batched DGEMM), spectrum-scaled steps from the lower bound
@@ -42,36 +43,31 @@ struct L64Point {
   int done, skip;
 };
 
-// Yc, Ywc [L][ne] (column-major ne x L): the point's rows in FP64, and the
-// departures per list entry
+// Bc [L][ne] (column-major ne x L): the point's rows in FP64 times sqrt(w),
+// and sqrt(w) dep per list entry
 __global__ void l64_gather_kernel(int ne, int L, int64_t r0, const float* __restrict__ rows,
                                   const __nv_bfloat16* __restrict__ rows16, const int* __restrict__ ridx,
                                   const float* __restrict__ rdiag, const float* __restrict__ rloc,
-                                  const float* __restrict__ dep, int wloc, double* Yc, double* Ywc, double* d64,
-                                  double* w64) {
+                                  const float* __restrict__ dep, int wloc, double* Bc, double* e64) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (int64_t)L * ne) return;
   const int64_t l = t / ne;
   const int m = (int)(t - l * ne);
   const int64_t e = r0 + l;
   const size_t ri = ridx ? (size_t)ridx[e] : (size_t)e;
-  const double w = wloc ? 1.0 / (double)rdiag[e] : (double)rloc[e] / (double)rdiag[e];
+  const double sw = sqrt(wloc ? 1.0 / (double)rdiag[e] : (double)rloc[e] / (double)rdiag[e]);
   const double y = rows16 ? (double)__bfloat162float(rows16[ri * ne + m]) : (double)rows[ri * ne + m];
-  Yc[t] = y;
-  Ywc[t] = w * y;
-  if (m == 0) {
-    d64[l] = (double)dep[ri];
-    w64[l] = w;
-  }
+  Bc[t] = sw * y;
+  if (m == 0) e64[l] = sw * (double)dep[ri];
 }
 
 // p1 = sum dep^2 w, p3 = sum rloc over the point's entries
-__global__ void l64_sums_kernel(int L, int64_t r0, const float* __restrict__ rloc, const double* __restrict__ d64,
-                                const double* __restrict__ w64, double* out) {
+__global__ void l64_sums_kernel(int L, int64_t r0, const float* __restrict__ rloc, const double* __restrict__ e64,
+                                double* out) {
   __shared__ double red[L64_NT / 32];
   double p1 = 0.0, p3 = 0.0;
   for (int l = threadIdx.x; l < L; l += L64_NT) {
-    p1 += d64[l] * d64[l] * w64[l];
+    p1 += e64[l] * e64[l];
     p3 += (double)rloc[r0 + l];
   }
   p1 = block_sum<double, L64_NT>(p1, red);
@@ -82,7 +78,8 @@ __global__ void l64_sums_kernel(int L, int64_t r0, const float* __restrict__ rlo
   }
 }
 
-// A = G + cI (in place), s, Y0 = A / s, Z0 = I, the point's scalars
+// G's upper triangle from its lower one (exactly symmetric), A = G + cI (in place), s,
+// Y0 = A / s, Z0 = I, the point's scalars
 __global__ void l64_prep_kernel(int ne, double* G, double* Y, double* Z, const double* __restrict__ sums,
                                 const double* __restrict__ infl_in, double minfl, L64Point* pt) {
   __shared__ double red[L64_NT / 32];
@@ -90,6 +87,11 @@ __global__ void l64_prep_kernel(int ne, double* G, double* Y, double* Z, const d
   const int b = blockIdx.x, tid = threadIdx.x;
   const size_t mo = (size_t)b * ne * ne;
   double* A = G + mo;
+  for (size_t idx = tid; idx < (size_t)ne * ne; idx += L64_NT) {
+    const int j = (int)(idx / ne), m = (int)(idx - (size_t)j * ne);  // row m, column j
+    if (m < j) A[idx] = A[(size_t)m * ne + j];
+  }
+  __syncthreads();
   double tr = 0.0;
   for (int m = tid; m < ne; m += L64_NT) tr += A[(size_t)m * ne + m];
   tr = block_sum<double, L64_NT>(tr, red);
@@ -245,16 +247,14 @@ int largek_fp64_pass(int ne, int npts, const int64_t* offs, const float* rows, c
   cublasSetStream(hb, s);
   const size_t mat = (size_t)ne * ne;
   const int R = (int)std::min<size_t>(todo.size(), 32);  // points per group
-  double *Yc = nullptr, *Ywc = nullptr, *d64 = nullptr, *w64 = nullptr, *G = nullptr, *Y = nullptr, *Z = nullptr;
+  double *Bc = nullptr, *e64 = nullptr, *G = nullptr, *Y = nullptr, *Z = nullptr;
   double *T = nullptr, *M = nullptr, *Yn = nullptr, *Zn = nullptr, *bvec = nullptr, *sums = nullptr, *pinf = nullptr;
   int *active = nullptr, *which = nullptr;
   L64Point* pt = nullptr;
   bool okm = true;
   auto A = [&](auto** p, size_t bytes) { okm = okm && cudaMallocAsync((void**)p, bytes, s) == cudaSuccess; };
-  A(&Yc, sizeof(double) * (size_t)lmax * ne);
-  A(&Ywc, sizeof(double) * (size_t)lmax * ne);
-  A(&d64, sizeof(double) * (size_t)lmax);
-  A(&w64, sizeof(double) * (size_t)lmax);
+  A(&Bc, sizeof(double) * (size_t)lmax * ne);
+  A(&e64, sizeof(double) * (size_t)lmax);
   for (double** p : {&G, &Y, &Z, &T, &M, &Yn, &Zn}) A(p, sizeof(double) * mat * R);
   A(&bvec, sizeof(double) * (size_t)ne * R);
   A(&sums, sizeof(double) * 2 * R);
@@ -274,15 +274,15 @@ int largek_fp64_pass(int ne, int npts, const int64_t* offs, const float* rows, c
       const int L = (int)(ho[p + 1] - r0);
       const int64_t tot = (int64_t)L * ne;
       l64_gather_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(ne, L, r0, rows, rows16, ridx, rdiag, rloc,
-                                                                       dep, rdiag_wloc, Yc, Ywc, d64, w64);
-      l64_sums_kernel<<<1, L64_NT, 0, s>>>(L, r0, rloc, d64, w64, sums + 2 * j);
+                                                                       dep, rdiag_wloc, Bc, e64);
+      l64_sums_kernel<<<1, L64_NT, 0, s>>>(L, r0, rloc, e64, sums + 2 * j);
       note_launch();
       note_launch();
       cudaMemcpyAsync(pinf + j, parm_infl + p, sizeof(double), cudaMemcpyDeviceToDevice, s);
-      rc = cublas_status(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_T, ne, ne, L, &one, Ywc, ne, Yc, ne, &zero,
+      rc = cublas_status(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_T, ne, ne, L, &one, Bc, ne, Bc, ne, &zero,
                                      G + (size_t)j * mat, ne));
       if (rc == LETKF_OK)
-        rc = cublas_status(cublasDgemv(hb, CUBLAS_OP_N, ne, L, &one, Ywc, ne, d64, 1, &zero, bvec + (size_t)j * ne, 1));
+        rc = cublas_status(cublasDgemv(hb, CUBLAS_OP_N, ne, L, &one, Bc, ne, e64, 1, &zero, bvec + (size_t)j * ne, 1));
     }
     if (rc != LETKF_OK) break;
     // 2. A, s, Y0, Z0
@@ -322,7 +322,7 @@ int largek_fp64_pass(int ne, int npts, const int64_t* offs, const float* rows, c
     rc = cuda_status(cudaGetLastError());
   }
   const int rc2 = cuda_status(cudaStreamSynchronize(s));
-  void* fr[] = {Yc, Ywc, d64, w64, G, Y, Z, T, M, Yn, Zn, bvec, sums, pinf, active, which, pt};
+  void* fr[] = {Bc, e64, G, Y, Z, T, M, Yn, Zn, bvec, sums, pinf, active, which, pt};
   for (void* p : fr)
     if (p) cudaFreeAsync(p, s);
   cublasDestroy(hb);
