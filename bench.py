@@ -74,6 +74,8 @@ def parse():
                     help="skip the FP32 polish where the anchored probe residual is below 10^-v (0: always polish)")
     ap.add_argument("--ns-cond", type=int, default=None,
                     help="Newton-Schulz only where the spectrum bound s/c < 10^v (0: no bound)")
+    ap.add_argument("--col-unit", type=int, default=None,
+                    help="order positions a tensor-core CTA takes at a time with the column cache (0: off)")
     ap.add_argument("--tune-points", type=int, default=32768,
                     help="run the autotuner on this many points before timing (0: the options given)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
@@ -645,8 +647,9 @@ def run_gpu(args, rank, world, dist):
     import torch
 
     from letkf_gb300 import lib as L
-    from letkf_gb300.sweep import (OPT_EIGENSOLVER, OPT_NS_COND, OPT_POLISH_PROBE, OPT_POLISH_TOL, OPT_TC_NS_ITERS,
-                                   OPT_TC_NS_SCALING, OPT_TC_NS_TOL, OPT_TENSOR_CORES, PREC_F64, PREC_MIXED, Sweep)
+    from letkf_gb300.sweep import (OPT_COLUMN_UNIT, OPT_EIGENSOLVER, OPT_NS_COND, OPT_POLISH_PROBE, OPT_POLISH_TOL,
+                                   OPT_TC_NS_ITERS, OPT_TC_NS_SCALING, OPT_TC_NS_TOL, OPT_TENSOR_CORES, PREC_F64,
+                                   PREC_MIXED, Sweep)
     from letkf_gb300.workload import RegionalWorkload
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
@@ -671,6 +674,8 @@ def run_gpu(args, rank, world, dist):
         sw.set_option(OPT_POLISH_PROBE, args.polish_probe)
     if args.ns_cond is not None:
         sw.set_option(OPT_NS_COND, args.ns_cond)
+    if args.col_unit is not None:
+        sw.set_option(OPT_COLUMN_UNIT, args.col_unit)
     sw.set_background_device(xb.data_ptr())
     infl0 = np.ones(wl.npts)
     sw.set_inflation(infl0)

@@ -427,6 +427,11 @@ int letkf_l96_obs_cell(int nx, int ny, const double* h, int* cell, void* stream)
                                       the lists (no CUDA graph); 0 (default): no limit */
 #define LETKF_OPT_GRID_SHARE 16    /* v >= 1: each persistent sweep launch takes 1/v of the CTAs its kernel can keep
                                       resident (the server's slots share the SMs this way); replaces a grid cap */
+#define LETKF_OPT_COLUMN_UNIT 17   /* where the points come in columns (equal ri, rj; the levels of a grid column), a
+                                      tensor-core CTA (ne <= 64) takes v consecutive order positions at a time and keeps
+                                      the search's horizontal candidates of its column for the next levels, which apply
+                                      only the vertical test (same lists, order and weights); v >= 1, or -1 (default):
+                                      the mean column length of the points; 0: off */
 #define LETKF_OPT_FAULT_WAIT 15    /* failure injection, v > 0: the next mixed-form runs on the tensor-core sweep
                                       wait on a barrier that nothing arrives at and give up after v polls, so the
                                       run reports LETKF_ERR_TIMEOUT and analyses nothing; 0 (default): off */

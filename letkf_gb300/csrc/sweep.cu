@@ -20,6 +20,11 @@ namespace letkf {
 
 struct SweepScaleParams;
 struct SweepArgs;
+// column cache: entries per CTA slot (32 bytes each) and slots per SM (the
+// tensor-core sweep keeps at most four CTAs on an SM)
+constexpr int LETKF_COL_CAP = 8192;
+constexpr int LETKF_COL_SLOTS_PER_SM = 4;
+
 int launch_sweep_mixed(const SweepArgs& a, cudaStream_t stream, int grid_cap);
 int launch_sweep_tc(const SweepArgs& a, cudaStream_t stream, int grid_cap);
 int prepare_sweep_mixed(int n);
@@ -213,6 +218,13 @@ struct letkf_sweep_s {
   bool groups_set = false;
   size_t obs_cap = 0;  // observations the resident buffers hold (kept across set_obs calls)
   int max_nobs = 0;    // MAX_NOBS_PER_GRID (0: no limit)
+  // column cache of the tensor-core search: enabled where most points of the
+  // processing order share (ri, rj) with the point before them
+  int4* col_ent = nullptr;
+  int col_slots = 0;
+  int col_unit = -1;  // order positions a CTA takes at a time (0: no cache; -1: the mean column length)
+  int col_len = 1;     // mean length of the runs of equal (ri, rj) in the processing order
+  bool columns = false;
   uint32_t fault_wait = 0;
   // selection probe
   int nprobe = 0, probe_cap = 0;
@@ -333,7 +345,8 @@ int letkf_sweep_destroy(letkf_sweep_t h) {
                   h->odat, h->oerr,  h->odep,  h->ocls,  h->ovarloc, h->G,     h->var_local, h->obsF,
                   h->obsA, h->meta,  h->ens32, h->ens64, h->xb,    h->xa,      h->infl,   h->status,
                   h->nobsl, h->sweeps, h->counter, h->defer_list, h->defer_count, h->defer_total, h->err_flag,
-                  h->operm, h->ogrp, h->probe_slot, h->probe_idx, h->probe_count, h->probe_rloc};
+                  h->operm, h->ogrp, h->probe_slot, h->probe_idx, h->probe_count, h->probe_rloc,
+                  h->col_ent};
   if (h->stream) {
     for (void* p : ptrs) dfree(p, h->stream);
     cudaStreamSynchronize(h->stream);
@@ -357,7 +370,8 @@ int letkf_sweep_set_points(letkf_sweep_t h, const double* ri, const double* rj, 
   const int np = h->d.npts;
   for (int p = 0; p < np; p++)
     if (!(rlev[p] > 0.0)) return LETKF_ERR_ARG;
-  // processing order: column tiles of tile x tile cells, input order inside a tile
+  // processing order: column tiles of tile x tile cells; inside a tile the
+  // points of one column (equal ri, rj) follow each other in input order
   std::vector<int> order(np);
   std::iota(order.begin(), order.end(), 0);
   std::vector<int64_t> band(np);
@@ -369,7 +383,11 @@ int letkf_sweep_set_points(letkf_sweep_t h, const double* ri, const double* rj, 
       const int64_t ti = (int64_t)std::floor((ri[p] - 0.5) / tile), tj = (int64_t)std::floor((rj[p] - 0.5) / tile);
       key[p] = (tj + 1) * (ntx + 1) + (ti + 1);
     }
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key[a] < key[b]; });
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+      if (key[a] != key[b]) return key[a] < key[b];
+      if (rj[a] != rj[b]) return rj[a] < rj[b];
+      return ri[a] < ri[b];
+    });
     for (int o = 0; o < np; o++) band[o] = key[order[o]] / (ntx + 1);
   }
   std::vector<double> lg(np);
@@ -381,6 +399,21 @@ int letkf_sweep_set_points(letkf_sweep_t h, const double* ri, const double* rj, 
   cudaMemcpyAsync(h->prlev, rlev, sizeof(double) * np, cudaMemcpyHostToDevice, s);
   if (rz) cudaMemcpyAsync(h->prz, rz, sizeof(double) * np, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(h->order, order.data(), sizeof(int) * np, cudaMemcpyHostToDevice, s);
+  // columns: most positions share (ri, rj) with the one before them
+  int64_t same = 0;
+  for (int o = 1; o < np; o++) same += ri[order[o]] == ri[order[o - 1]] && rj[order[o]] == rj[order[o - 1]];
+  h->columns = np > 1 && 2 * same >= (int64_t)np;
+  h->col_len = np > 0 ? (int)std::min<int64_t>(4096, (np + (np - same) - 1) / (np - same)) : 1;
+  if (h->columns && !h->col_ent) {
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    h->col_slots = nsm * LETKF_COL_SLOTS_PER_SM;
+    if (dalloc(&h->col_ent, (size_t)h->col_slots * LETKF_COL_CAP * 2, s) != LETKF_OK) {
+      h->col_ent = nullptr;
+      h->col_slots = 0;
+    }
+  }
   const int st = cuda_status(cudaStreamSynchronize(s));
   h->horder.swap(order);
   h->hband.swap(band);
@@ -609,6 +642,10 @@ int letkf_sweep_set_option(letkf_sweep_t h, int option, int value) {
       if (value < 0) return LETKF_ERR_ARG;
       h->fault_wait = (uint32_t)value;
       return LETKF_OK;
+    case LETKF_OPT_COLUMN_UNIT:
+      if (value < -1 || value > 4096) return LETKF_ERR_ARG;
+      h->col_unit = value;
+      return LETKF_OK;
     case LETKF_OPT_EIGENSOLVER:
       if (value != LETKF_EIG_NEWTON_SCHULZ && value != LETKF_EIG_JACOBI) return LETKF_ERR_ARG;
       h->use_ns = value == LETKF_EIG_NEWTON_SCHULZ;
@@ -779,6 +816,15 @@ static void build_args(letkf_sweep_t h, SweepArgs& a) {
   a.probe_rloc = h->probe_rloc;
   a.probe_count = h->probe_count;
   a.fault_wait_polls = h->fault_wait;
+  // the column cache serves the tensor-core sweep for ne <= 64
+  if (h->columns && h->col_ent && h->col_unit != 0 && h->d.ne <= 64) {
+    a.col_ent = h->col_ent;
+    a.col_cap = LETKF_COL_CAP;
+    a.col_slots = h->col_slots;
+    a.col_unit = h->col_unit > 0 ? h->col_unit : h->col_len;
+  } else {
+    a.col_unit = 1;
+  }
 }
 
 // tensor-core sweeps: sweep_tc.cu for ne <= 64, sweep_tc128.cu for 64 < ne <= 128

@@ -65,6 +65,14 @@ struct SweepArgs {
   const int* qmap;           // if set, work item q analyses order position qmap[q] (the deferred pass of list mode)
   const int* list_idx;
   const double* list_rloc;
+  // column cache of the search (sweep_search.cuh SwCache): CTA b keeps the
+  // horizontal survivors of its current column in col_ent[2 b col_cap ...]
+  // (b < col_slots); a CTA takes col_unit consecutive order positions at a
+  // time, so the levels of a column (consecutive in the order) meet in one CTA
+  int4* col_ent;  // NULL: no cache
+  int col_cap;
+  int col_slots;
+  int col_unit;  // >= 1
   // failure injection: > 0 makes the tensor-core sweep wait, before its first
   // point, on a barrier that nothing arrives at, giving up after this many
   // polls (LETKF_ERR_TIMEOUT through err_flag); 0 in normal runs

@@ -54,22 +54,177 @@ struct SearchSmem {
   float* pr;    // rloc
   int* rowib;   // [SW_MAXROWS]
   int* rowpre;  // [SW_MAXROWS + 1]
-  int* wcnt;    // [CPT*NT/32 + 1]
+  int* wcnt;    // [2 * (CPT*NT/32 + 1)]: accepted, then column-cache survivors
 };
+
+// The FP32 filter's terms, written with explicit roundings so that the direct
+// scan and the column cache below give the same bits: the horizontal term
+// h2 = (di^2 dx^2 + dj^2 dy^2) / sigma_h^2 and nd = h2 + vv^2 / sigma_v^2.
+__device__ __forceinline__ float sw_h2(float rif, float rjf, float dx2, float dy2, const float4& f) {
+  const float di = rif - f.x, dj = rjf - f.y;
+  return __fmul_rn(__fmaf_rn(__fmul_rn(di, di), dx2, __fmul_rn(__fmul_rn(dj, dj), dy2)), f.w);
+}
+__device__ __forceinline__ float sw_nd(float h2, float vv, float qx) { return __fmaf_rn(__fmul_rn(vv, vv), qx, h2); }
+
+// One candidate's outcome: accepted (ok) with its pending-list entry, and for
+// the column cache whether it survives the horizontal test (sv) with its
+// 32-byte entry (e0, e1)
+struct SwCand {
+  int ob;
+  bool ok, sv;
+  float w, d, r;
+  int4 e0, e1;
+};
+
+// Column cache.  The horizontal part of the test depends on (ri, rj) only, so
+// the points of one column (the levels of a grid column, consecutive in the
+// processing order) share it.  The first point of a column scans the
+// candidate ranges as usual and also keeps, in candidate order, every
+// candidate whose horizontal term alone does not exceed the band's upper edge
+// as two int4: (ob | vertical-coordinate bit << 31, h2, vertical coordinate,
+// 1/sigma_v^2) and (rloc factor, 1/err^2, departure, 0), so that a cached
+// level reads nothing else; any other candidate has nd >= h2 > band_hi at every level
+// (nd = h2 + a non-negative term, rounded monotonically) and is rejected.  The
+// next points of the column read only that list and apply the vertical test,
+// with the same FP32 terms and the same FP64 re-test of the band, so the
+// accepted lists, their order and the FP32 weights are the direct scan's.
+struct SwCache {
+  int4* ent;  // [2 * cap] or NULL (no cache)
+  int cap;    // entries
+};
+
+// Compaction of one batch of CPT*NT evaluated candidates: accepted ones go to
+// the pending list (and the probe) in candidate order, survivors to the
+// column cache; flush(CH) consumes the pending list in stages of CH.
+template <int NT, int CH, int CPT, bool BUILD, typename Flush>
+__device__ __forceinline__ void sw_compact(const SweepArgs& a, const SearchSmem& s, int probe, const SwCand (&cg)[CPT],
+                                           int& pend, int& L, const SwCache& cache, int& nsurv, Flush& flush) {
+  constexpr int NW = NT / 32;
+  constexpr int SV = CPT * NW + 1;  // survivors' counts follow the accepted ones
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const unsigned below = (1u << lane) - 1u;
+  int before[CPT], sbefore[CPT];
+#pragma unroll
+  for (int g = 0; g < CPT; g++) {
+    const unsigned bal = __ballot_sync(0xffffffffu, cg[g].ok);
+    before[g] = __popc(bal & below);
+    if (lane == 0) s.wcnt[g * NW + wid] = __popc(bal);
+    if (BUILD) {
+      const unsigned sb = __ballot_sync(0xffffffffu, cg[g].sv);
+      sbefore[g] = __popc(sb & below);
+      if (lane == 0) s.wcnt[SV + g * NW + wid] = __popc(sb);
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    int t = 0;
+    for (int k = 0; k < CPT * NW; k++) {
+      const int v = s.wcnt[k];
+      s.wcnt[k] = t;
+      t += v;
+    }
+    s.wcnt[CPT * NW] = t;
+    if (BUILD) {
+      t = 0;
+      for (int k = 0; k < CPT * NW; k++) {
+        const int v = s.wcnt[SV + k];
+        s.wcnt[SV + k] = t;
+        t += v;
+      }
+      s.wcnt[SV + CPT * NW] = t;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int g = 0; g < CPT; g++) {
+    if (cg[g].ok) {
+      const int rel = s.wcnt[g * NW + wid] + before[g];
+      const int slot = pend + rel;
+      s.pidx[slot] = cg[g].ob;
+      s.pw[slot] = cg[g].w;
+      s.pd[slot] = cg[g].d;
+      s.pr[slot] = cg[g].r;
+      if (probe >= 0 && L + rel < a.probe_cap) {
+        const size_t at = (size_t)probe * a.probe_cap + (L + rel);
+        a.probe_idx[at] = cg[g].ob;
+        a.probe_rloc[at] = cg[g].r;
+      }
+    }
+    if (BUILD && cg[g].sv) {
+      const int at = nsurv + s.wcnt[SV + g * NW + wid] + sbefore[g];
+      if (at < cache.cap) {
+        cache.ent[2 * at] = cg[g].e0;
+        cache.ent[2 * at + 1] = cg[g].e1;
+      }
+    }
+  }
+  pend += s.wcnt[CPT * NW];
+  L += s.wcnt[CPT * NW];
+  if (BUILD) nsurv += s.wcnt[SV + CPT * NW];
+  __syncthreads();
+  while (pend >= CH) {
+    flush(CH);
+    __syncthreads();
+    // move the tail (fewer than CPT*NT entries) to the front
+    const int rest = pend - CH;
+    int i0[CPT];
+    float w0[CPT], d0[CPT], r0[CPT];
+#pragma unroll
+    for (int g = 0; g < CPT; g++) {
+      const int t = g * NT + tid;
+      if (t < rest) {
+        i0[g] = s.pidx[CH + t];
+        w0[g] = s.pw[CH + t];
+        d0[g] = s.pd[CH + t];
+        r0[g] = s.pr[CH + t];
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int g = 0; g < CPT; g++) {
+      const int t = g * NT + tid;
+      if (t < rest) {
+        s.pidx[t] = i0[g];
+        s.pw[t] = w0[g];
+        s.pd[t] = d0[g];
+        s.pr[t] = r0[g];
+      }
+    }
+    pend = rest;
+    __syncthreads();
+  }
+}
+
+// The FP32 filter with the FP64 re-test of the band |nd - cutoff| < 1e-3
+// cutoff: whether the candidate is accepted, and in nd_out the nd its rloc is
+// computed from (the FP64 value rounded to FP32 where the re-test ran)
+__device__ __forceinline__ bool sw_accept(const SweepArgs& a, int ob, float nd, double ri, double rj, double logr,
+                                          double rz, float& nd_out) {
+  const float dzf2 = 13.33333333f;  // scale/letkf/letkf_obs.f90:30 (default-real literal)
+  const float band_lo = dzf2 * (1.f - SW_BAND), band_hi = dzf2 * (1.f + SW_BAND);
+  bool ok = nd <= band_lo;
+  if (!ok && nd <= band_hi) {
+    const double ndd = scale_ndist_exact(a, ob, ri, rj, logr, rz);
+    ok = !(ndd > (double)dzf2);
+    nd = (float)ndd;
+  }
+  nd_out = nd;
+  return ok;
+}
 
 // One pass over the candidates of a grid point.  Each batch tests CPT*NT
 // candidates (CPT per thread, candidate base + g*NT + tid in group g), so the
 // batches and their barriers are CPT times fewer; accepted observations are
 // compacted group by group, which keeps the reference's candidate order.
-template <int NT, int CH, int CPT = 1, typename Flush>
+// BUILD: the column cache of this point's (ri, rj) is written on the way;
+// *nsurv receives its length (above cache.cap: not usable).
+template <int NT, int CH, int CPT, bool BUILD, typename Flush>
 __device__ int sweep_search(const SweepArgs& a, double ri, double rj, double logr, double rz, const SearchSmem& s,
-                            int probe, Flush&& flush) {
-  constexpr int NW = NT / 32;
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+                            int probe, Flush&& flush, const SwCache& cache = SwCache{nullptr, 0},
+                            int* nsurv_out = nullptr) {
+  const int tid = threadIdx.x;
   const int ld = a.nlon + 1;
-  const float dzf2 = 13.33333333f;  // scale/letkf/letkf_obs.f90:30 (default-real literal)
-  const double dzf2d = (double)13.33333333f;
-  const float band_lo = dzf2 * (1.f - SW_BAND), band_hi = dzf2 * (1.f + SW_BAND);
+  const float band_hi = 13.33333333f * (1.f + SW_BAND);
   const float dx2 = (float)(a.P.dx * a.P.dx), dy2 = (float)(a.P.dy * a.P.dy);
   const float rif = (float)ri, rjf = (float)rj, logrf = (float)logr, rzf = (float)rz;
   int imin = (int)floor(ri - a.P.dlon_zero), imax = (int)ceil(ri + a.P.dlon_zero);
@@ -78,7 +233,7 @@ __device__ int sweep_search(const SweepArgs& a, double ri, double rj, double log
   imax = min(imax, a.nlon);
   jmin = max(jmin, 1);
   jmax = min(jmax, a.nlat);
-  int pend = 0, L = 0;
+  int pend = 0, L = 0, nsurv = 0;
   const bool any = a.nobs > 0 && a.G[(size_t)(a.nlat - 1) * ld + a.nlon] > 0 && imin <= imax && jmin <= jmax;
   for (int jb = jmin; any && jb <= jmax; jb += SW_MAXROWS) {
     const int nrow = min(SW_MAXROWS, jmax - jb + 1);
@@ -97,15 +252,14 @@ __device__ int sweep_search(const SweepArgs& a, double ri, double rj, double log
     __syncthreads();
     const int ncand = s.rowpre[nrow];
     for (int base = 0; base < ncand; base += CPT * NT) {
-      int obg[CPT], before[CPT];
-      bool okg[CPT];
-      float wg[CPT], dg[CPT], rg[CPT];
+      SwCand cg[CPT];
 #pragma unroll
       for (int g = 0; g < CPT; g++) {
         const int c = base + g * NT + tid;
-        int ob = -1;
-        bool ok_acc = false;
-        float w = 0.f, dv = 0.f, rl = 0.f;
+        SwCand& o = cg[g];
+        o.ob = -1;
+        o.ok = o.sv = false;
+        o.w = o.d = o.r = 0.f;
         if (c < ncand) {
           int lo = 0, hi = nrow - 1;  // rowpre[lo] <= c < rowpre[lo+1]
           while (lo < hi) {
@@ -113,99 +267,84 @@ __device__ int sweep_search(const SweepArgs& a, double ri, double rj, double log
             if (s.rowpre[mid] <= c) lo = mid;
             else hi = mid - 1;
           }
-          ob = s.rowib[lo] + (c - s.rowpre[lo]);
+          const int ob = s.rowib[lo] + (c - s.rowpre[lo]);
+          o.ob = ob;
           const int meta = a.obsMeta[ob];
           if (!(meta & 2)) {
             const float4 f = a.obsF[ob];
-            const float di = rif - f.x, dj = rjf - f.y;
-            const float h2 = (di * di * dx2 + dj * dj * dy2) * f.w;
+            const float h2 = sw_h2(rif, rjf, dx2, dy2, f);
             const float4 q = a.obsA[ob];
             const float vv = ((meta & 1) ? rzf : logrf) - f.z;
-            float nd = h2 + vv * vv * q.x;
-            bool ok = nd <= band_lo;
-            if (!ok && nd <= band_hi) {
-              const double ndd = scale_ndist_exact(a, ob, ri, rj, logr, rz);
-              ok = !(ndd > dzf2d);
-              nd = (float)ndd;
+            float nd;
+            if (sw_accept(a, ob, sw_nd(h2, vv, q.x), ri, rj, logr, rz, nd)) {
+              o.ok = true;
+              o.r = __expf(-0.5f * nd) * q.w;
+              o.w = o.r * q.y;
+              o.d = q.z;
             }
-            if (ok) {
-              ok_acc = true;
-              rl = __expf(-0.5f * nd) * q.w;
-              w = rl * q.y;
-              dv = q.z;
+            if (BUILD) {
+              o.sv = h2 <= band_hi;
+              o.e0 = make_int4((int)((unsigned)ob | ((unsigned)(meta & 1) << 31)), __float_as_int(h2),
+                               __float_as_int(f.z), __float_as_int(q.x));
+              o.e1 = make_int4(__float_as_int(q.w), __float_as_int(q.y), __float_as_int(q.z), 0);
             }
           }
         }
-        const unsigned bal = __ballot_sync(0xffffffffu, ok_acc);
-        before[g] = __popc(bal & ((1u << lane) - 1u));
-        if (lane == 0) s.wcnt[g * NW + wid] = __popc(bal);
-        obg[g] = ob;
-        okg[g] = ok_acc;
-        wg[g] = w;
-        dg[g] = dv;
-        rg[g] = rl;
       }
-      __syncthreads();
-      if (tid == 0) {
-        int t = 0;
-        for (int k = 0; k < CPT * NW; k++) {
-          const int v = s.wcnt[k];
-          s.wcnt[k] = t;
-          t += v;
-        }
-        s.wcnt[CPT * NW] = t;
-      }
-      __syncthreads();
-#pragma unroll
-      for (int g = 0; g < CPT; g++)
-        if (okg[g]) {
-          const int rel = s.wcnt[g * NW + wid] + before[g];
-          const int slot = pend + rel;
-          s.pidx[slot] = obg[g];
-          s.pw[slot] = wg[g];
-          s.pd[slot] = dg[g];
-          s.pr[slot] = rg[g];
-          if (probe >= 0 && L + rel < a.probe_cap) {
-            const size_t at = (size_t)probe * a.probe_cap + (L + rel);
-            a.probe_idx[at] = obg[g];
-            a.probe_rloc[at] = rg[g];
-          }
-        }
-      pend += s.wcnt[CPT * NW];
-      L += s.wcnt[CPT * NW];
-      __syncthreads();
-      while (pend >= CH) {
-        flush(CH);
-        __syncthreads();
-        // move the tail (fewer than CPT*NT entries) to the front
-        const int rest = pend - CH;
-        int i0[CPT];
-        float w0[CPT], d0[CPT], r0[CPT];
-#pragma unroll
-        for (int g = 0; g < CPT; g++) {
-          const int t = g * NT + tid;
-          if (t < rest) {
-            i0[g] = s.pidx[CH + t];
-            w0[g] = s.pw[CH + t];
-            d0[g] = s.pd[CH + t];
-            r0[g] = s.pr[CH + t];
-          }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int g = 0; g < CPT; g++) {
-          const int t = g * NT + tid;
-          if (t < rest) {
-            s.pidx[t] = i0[g];
-            s.pw[t] = w0[g];
-            s.pd[t] = d0[g];
-            s.pr[t] = r0[g];
-          }
-        }
-        pend = rest;
-        __syncthreads();
+      sw_compact<NT, CH, CPT, BUILD>(a, s, probe, cg, pend, L, cache, nsurv, flush);
+    }
+  }
+  if (pend > 0) {
+    flush(pend);
+    __syncthreads();
+  }
+  if (probe >= 0 && threadIdx.x == 0) a.probe_count[probe] = L;
+  if (nsurv_out) *nsurv_out = nsurv;
+  return L;
+}
+
+// A point whose column cache holds n entries (see SwCache): the vertical
+// test over the cached horizontal survivors, in their (candidate) order.  The
+// next batch's entries are loaded before this batch's compaction barriers.
+template <int NT, int CH, typename Flush>
+__device__ int sweep_search_cached(const SweepArgs& a, const int4* __restrict__ ent, int n, double ri, double rj,
+                                   double logr, double rz, const SearchSmem& s, int probe, Flush&& flush) {
+  const int tid = threadIdx.x;
+  const float logrf = (float)logr, rzf = (float)rz;
+  int pend = 0, L = 0, nsurv = 0;
+  const SwCache none{nullptr, 0};
+  int4 e0 = make_int4(0, 0, 0, 0), e1 = e0;
+  if (tid < n) {
+    e0 = ent[2 * tid];
+    e1 = ent[2 * tid + 1];
+  }
+  for (int base = 0; base < n; base += NT) {
+    SwCand cg[1];
+    SwCand& o = cg[0];
+    const int c = base + tid;
+    int4 f0 = make_int4(0, 0, 0, 0), f1 = f0;
+    if (c + NT < n) {
+      f0 = ent[2 * (c + NT)];
+      f1 = ent[2 * (c + NT) + 1];
+    }
+    o.ob = -1;
+    o.ok = o.sv = false;
+    o.w = o.d = o.r = 0.f;
+    if (c < n) {
+      const int ob = e0.x & 0x7fffffff;
+      o.ob = ob;
+      const float vv = ((e0.x < 0) ? rzf : logrf) - __int_as_float(e0.z);
+      float nd;
+      if (sw_accept(a, ob, sw_nd(__int_as_float(e0.y), vv, __int_as_float(e0.w)), ri, rj, logr, rz, nd)) {
+        o.ok = true;
+        o.r = __expf(-0.5f * nd) * __int_as_float(e1.x);
+        o.w = o.r * __int_as_float(e1.y);
+        o.d = __int_as_float(e1.z);
       }
     }
+    sw_compact<NT, CH, 1, false>(a, s, probe, cg, pend, L, none, nsurv, flush);
+    e0 = f0;
+    e1 = f1;
   }
   if (pend > 0) {
     flush(pend);

@@ -72,11 +72,13 @@ struct TcLayout {
   static constexpr int ROWIB = PR + 4 * PCAP;
   static constexpr int ROWPRE = ROWIB + 4 * SW_MAXROWS;
   static constexpr int WCNT = ROWPRE + 4 * (SW_MAXROWS + 1);
-  static constexpr int MEAN = ((WCNT + 4 * (TC_CPT * TC_NT / 32 + 2)) + 7) & ~7;  // double[16]
+  static constexpr int MEAN = ((WCNT + 4 * 2 * (TC_CPT * TC_NT / 32 + 1)) + 7) & ~7;  // double[16]
   static constexpr int MBAR = MEAN + 128;        // uint64[5]: Gram stages 0/1, products, background rows, drain
   static constexpr int TMEMH = MBAR + 40;        // uint32
-  static constexpr int CTRL = TMEMH + 8;         // int[4]
-  static constexpr int TOTAL = CTRL + 16;
+  static constexpr int CTRL = TMEMH + 8;         // int[4]: position, scratch
+  static constexpr int CKEY = CTRL + 16;         // double[2]: the column-cache point (ri, rj)
+  static constexpr int RUN = CKEY + 16;          // int[4]: run of positions [next, end), column-cache length
+  static constexpr int TOTAL = RUN + 16;
 };
 
 // sum_j M[j][c] x[j] for a 64 x 64 row-major matrix in shared memory (column
@@ -165,6 +167,11 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
     tc::mbar_init(&mbar[3], 1);
     tc::mbar_init(&mbar[4], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    int* rn = reinterpret_cast<int*>(sm + L::RUN);
+    rn[0] = rn[1] = 0;
+    rn[2] = -2;
+    double* ck = reinterpret_cast<double*>(sm + L::CKEY);
+    ck[0] = ck[1] = __longlong_as_double(0x7ff8000000000000ll);  // NaN: equal to no point
   }
   if (wid == 0) tc::tmem_alloc(tmem_holder, TC_TMEM_COLS);
   tc::fence_before_sync();
@@ -203,9 +210,24 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
   const bool skip_all = __syncthreads_or(tmo);  // uniform over the CTA
   if (skip_all) tmo = 1;
 
+  // The CTA takes runs of col_unit consecutive order positions [run[0],
+  // run[1]).  Column cache of the search (state in shared memory, uniform over
+  // the CTA): run[2] entries for the point column ckey = (ri, rj); -1: it did
+  // not fit, -2: none.
+  const bool col = a.col_ent != nullptr && !a.list_offs && (int)blockIdx.x < a.col_slots;
+  double* ckey = reinterpret_cast<double*>(sm + L::CKEY);
+  int* run = reinterpret_cast<int*>(sm + L::RUN);
   for (; !skip_all;) {
     __syncthreads();
-    if (tid == 0) ctrl[0] = atomicAdd(a.counter, 1);
+    if (tid == 0) {
+      if (run[0] >= run[1]) {
+        const int unit = a.col_unit > 1 ? a.col_unit : 1;
+        const int64_t u0 = (int64_t)atomicAdd(a.counter, 1) * unit;
+        run[0] = (int)min(u0, (int64_t)npts_work);
+        run[1] = (int)min(u0 + unit, (int64_t)npts_work);
+      }
+      ctrl[0] = run[0]++;
+    }
     __syncthreads();
     const int q = ctrl[0];
     if (q >= npts_work) break;
@@ -280,8 +302,26 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
       chunk++;
     };
     const int probe = a.probe_slot ? a.probe_slot[pt] : -1;
-    const int Lp = a.list_offs ? sweep_list<TC_NT, TC_CH>(a, qq, ss, flush)
-                               : sweep_search<TC_NT, TC_CH, TC_CPT>(a, ri, rj, logr, rz, ss, probe, flush);
+    int Lp;
+    const bool same_col = col && ri == ckey[0] && rj == ckey[1];
+    const int cn = run[2];
+    if (a.list_offs) {
+      Lp = sweep_list<TC_NT, TC_CH>(a, qq, ss, flush);
+    } else if (same_col && cn >= 0) {
+      Lp = sweep_search_cached<TC_NT, TC_CH>(a, a.col_ent + (size_t)blockIdx.x * a.col_cap * 2, cn, ri, rj, logr,
+                                             rz, ss, probe, flush);
+    } else if (col && !same_col) {
+      int nsv = 0;
+      const SwCache cache{a.col_ent + (size_t)blockIdx.x * a.col_cap * 2, a.col_cap};
+      Lp = sweep_search<TC_NT, TC_CH, TC_CPT, true>(a, ri, rj, logr, rz, ss, probe, flush, cache, &nsv);
+      if (tid == 0) {  // read by the next point, after the barriers in between
+        ckey[0] = ri;
+        ckey[1] = rj;
+        run[2] = nsv <= a.col_cap ? nsv : -1;
+      }
+    } else {  // no cache, or this column's did not fit
+      Lp = sweep_search<TC_NT, TC_CH, TC_CPT, false>(a, ri, rj, logr, rz, ss, probe, flush);
+    }
     for (int b = 0; b < 2; b++)
       if ((outst >> b) & 1u) {
         wait_bar(b);

@@ -66,7 +66,7 @@ struct T8Layout {
   static constexpr int ROWIB = PR + 4 * PCAP;
   static constexpr int ROWPRE = ROWIB + 4 * SW_MAXROWS;
   static constexpr int WCNT = ROWPRE + 4 * (SW_MAXROWS + 1);
-  static constexpr int MEAN = ((WCNT + 4 * (T8_NT / 32 + 2)) + 7) & ~7;  // double[16]
+  static constexpr int MEAN = ((WCNT + 4 * 2 * (T8_NT / 32 + 1)) + 7) & ~7;  // double[16]
   static constexpr int MBAR = MEAN + 128;             // uint64[5]: Gram stages 0/1, products, rows, drain
   static constexpr int TMEMH = MBAR + 40;
   static constexpr int CTRL = TMEMH + 8;              // int[4]
@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(T8_NT, 1) sweep_tc128_kernel(SweepArgs a) {
     };
     const int probe = a.probe_slot ? a.probe_slot[pt] : -1;
     const int Lp = a.list_offs ? sweep_list<T8_NT, T8_CH>(a, qq, ss, flush)
-                               : sweep_search<T8_NT, T8_CH, 1>(a, ri, rj, logr, rz, ss, probe, flush);
+                               : sweep_search<T8_NT, T8_CH, 1, false>(a, ri, rj, logr, rz, ss, probe, flush);
     for (int b = 0; b < 2; b++)
       if ((outst >> b) & 1u) {
         wait_bar(b);

@@ -35,6 +35,7 @@ OPT_NS_COND = 13
 OPT_MAX_NOBS_PER_GRID = 14
 OPT_FAULT_WAIT = 15
 OPT_GRID_SHARE = 16
+OPT_COLUMN_UNIT = 17
 
 
 class SweepDesc(C.Structure):

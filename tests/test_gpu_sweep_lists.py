@@ -83,9 +83,23 @@ def test_fused_search_lists_equal_oracle(cuda, ne, tc, with_varloc):
     sw.run()
     dg = sw.diagnostics()
     _check_lists(sw, so, perm, case, points, cap)
-    cnt, _, _ = sw.probe()
+    cnt, obs, rl = sw.probe()
     np.testing.assert_array_equal(cnt, dg["nobsl"])
     assert dg["nobsl"].max() > 100
+    if tc == 1 and ne <= 64:
+        # the tensor-core sweep keeps each column's horizontal candidates for
+        # its next levels: without that cache, the same bits throughout
+        from letkf_gb300.sweep import OPT_COLUMN_UNIT
+
+        xa = sw.analysis()
+        sw.set_option(OPT_COLUMN_UNIT, 0)
+        sw.set_inflation(np.full(npts, 1.05))
+        sw.run()
+        cnt0, obs0, rl0 = sw.probe()
+        np.testing.assert_array_equal(cnt0, cnt)
+        np.testing.assert_array_equal(obs0, obs)
+        np.testing.assert_array_equal(rl0, rl)
+        np.testing.assert_array_equal(sw.analysis(), xa)
     sw.close()
 
 
@@ -169,6 +183,51 @@ def test_fused_search_on_the_cutoff(cuda, tc, ne):
     n_line = case["ri"].size // 2
     assert 0 < cnt[0] < n_line
     sw.close()
+
+
+@pytest.mark.parametrize("unit", [3, 2, 16])
+def test_column_cache_on_the_cutoff(cuda, unit):
+    """The cut-off case with each point in a column of three levels, the
+    on-the-line level second or third, so that its list comes from the column
+    cache (the horizontal survivors kept by the column's first level): lists
+    equal the oracle's, and equal, bit for bit with rloc, those of the run
+    without the cache.  unit 2 splits a column over two runs of positions."""
+    from letkf_gb300.sweep import OPT_COLUMN_UNIT
+
+    case, rz = _cutoff_case(40)
+    prm = S.scale_params(case)
+    perm, grd = O.scale_sort_obs(case["nlon"], case["nlat"], case["ri"], case["rj"])
+    so = _oracle(case, prm, perm, grd)
+    pi, pj, pl = case["pri"], case["prj"], case["prlev"]
+    # per column: another level first, then the cut-off level (point 0) or
+    # two others then the cut-off level (point 1)
+    levs = [(pl[0] * 0.8, pl[0], pl[0] * 1.1), (pl[1] * 1.05, pl[1] * 0.9, pl[1])]
+    zs = [(rz[0] + 500.0, rz[0], rz[0] - 300.0), (rz[1] - 200.0, rz[1] + 100.0, rz[1])]
+    case["pri"] = np.repeat(pi, 3)
+    case["prj"] = np.repeat(pj, 3)
+    case["prlev"] = np.array([v for c in levs for v in c])
+    rzc = np.array([v for c in zs for v in c])
+    case["xb"] = np.repeat(case["xb"], 3, axis=1)
+    sw = _sweep(case, prm, 40, 1, rz=rzc)
+    sw.set_option(OPT_COLUMN_UNIT, unit)
+    points = np.arange(case["pri"].size, dtype=np.int32)
+    sw.set_probe(points, 2048)
+    sw.run()
+    _check_lists(sw, so, perm, case, points, 2048, rz=rzc)
+    cnt, obs, rl = sw.probe()
+    n_line = case["ri"].size // 2
+    assert 0 < cnt[1] < n_line and cnt[5] > 0
+    xa = sw.analysis()
+    sw.set_option(OPT_COLUMN_UNIT, 0)
+    sw.set_inflation(np.full(points.size, 1.05))
+    sw.run()
+    cnt0, obs0, rl0 = sw.probe()
+    xa0 = sw.analysis()
+    sw.close()
+    np.testing.assert_array_equal(cnt0, cnt)
+    np.testing.assert_array_equal(obs0, obs)
+    np.testing.assert_array_equal(rl0, rl)
+    np.testing.assert_array_equal(xa0, xa)
 
 
 def test_fused_search_matches_golden_fixture(cuda):
