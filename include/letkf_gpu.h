@@ -463,7 +463,10 @@ int letkf_sweep_set_obs(letkf_sweep_t h, int nobs, const double* ri, const doubl
                         const int* varloc, const double* var_local_row, int nvarloc, const void* hdxf,
                         int hdxf_f32);
 /* background members xb[nv][npts][ne] (float64 for LETKF_PREC_F64, float32
- * for LETKF_PREC_MIXED); host or device pointer */
+ * for LETKF_PREC_MIXED); host or device pointer.  A device source is copied
+ * after the work queued on the legacy default stream (and on the streams that
+ * synchronise with it) has finished, so data written there need no extra
+ * synchronisation; data written on a non-blocking stream must be complete. */
 int letkf_sweep_set_background(letkf_sweep_t h, const void* xb, int on_device);
 int letkf_sweep_set_inflation(letkf_sweep_t h, const double* infl, int on_device);
 int letkf_sweep_set_option(letkf_sweep_t h, int option, int value);

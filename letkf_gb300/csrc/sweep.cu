@@ -555,18 +555,29 @@ int letkf_sweep_set_obs(letkf_sweep_t h, int nobs, const double* ri, const doubl
   return cuda_status(cudaStreamSynchronize(s));
 }
 
+// An input copied into the handle.  The handle's streams do not wait for the
+// legacy default stream, so a device source (written there, or on any stream
+// that synchronises with it) is copied on the legacy default stream, after the
+// handle's own work has drained; a host source is copied on the handle's stream.
+static int copy_in(letkf_sweep_t h, void* dst, const void* src, size_t bytes, int on_device) {
+  int st = cuda_status(cudaStreamSynchronize(h->stream));
+  if (st != LETKF_OK) return st;
+  if (on_device) {
+    cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, cudaStreamLegacy);
+    return cuda_status(cudaStreamSynchronize(cudaStreamLegacy));
+  }
+  cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream);
+  return cuda_status(cudaStreamSynchronize(h->stream));
+}
+
 int letkf_sweep_set_background(letkf_sweep_t h, const void* xb, int on_device) {
   if (!h || !xb) return LETKF_ERR_ARG;
-  const size_t bytes = (size_t)h->d.npts * h->d.nv * h->d.ne * elem(h);
-  cudaMemcpyAsync(h->xb, xb, bytes, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream);
-  return cuda_status(cudaStreamSynchronize(h->stream));
+  return copy_in(h, h->xb, xb, (size_t)h->d.npts * h->d.nv * h->d.ne * elem(h), on_device);
 }
 
 int letkf_sweep_set_inflation(letkf_sweep_t h, const double* infl, int on_device) {
   if (!h || !infl) return LETKF_ERR_ARG;
-  cudaMemcpyAsync(h->infl, infl, sizeof(double) * h->d.npts,
-                  on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream);
-  return cuda_status(cudaStreamSynchronize(h->stream));
+  return copy_in(h, h->infl, infl, sizeof(double) * h->d.npts, on_device);
 }
 
 int letkf_sweep_device_buffers(letkf_sweep_t h, void** xb, void** xa, double** infl, int** nobsl) {
