@@ -74,6 +74,10 @@ def parse():
                     help="skip the FP32 polish where the anchored probe residual is below 10^-v (0: always polish)")
     ap.add_argument("--ns-cond", type=int, default=None,
                     help="Newton-Schulz only where the spectrum bound s/c < 10^v (0: no bound)")
+    ap.add_argument("--decompose", action="store_true",
+                    help="one regional domain split into 2-D tiles (one per rank, or --tiles on one GPU in turn), "
+                         "each tile's halo observations exchanged once before the timed region")
+    ap.add_argument("--tiles", type=int, default=None, help="tiles of --decompose on one GPU (default: the ranks)")
     ap.add_argument("--col-unit", type=int, default=None,
                     help="order positions a tensor-core CTA takes at a time with the column cache (0: off)")
     ap.add_argument("--tune-points", type=int, default=32768,
@@ -844,6 +848,115 @@ def run_gpu(args, rank, world, dist):
     return out, sw
 
 
+# ------------------------------------------------------- domain decomposition
+def run_decompose(args, rank, world, dist):
+    """One regional domain split into 2-D process tiles (shard.tile_of), as
+    the reference's SCALE decomposition (scale/letkf/letkf_obs.f90:886-985).
+    With N ranks each rank owns every N-th observation, one exchange_obs
+    all-gather before the timed region gives each tile its halo, and each
+    rank times its tile's sweep (max over ranks).  On one GPU, --tiles K runs
+    the K tiles in turn as one step and compares the reassembled analysis
+    with the single-domain sweep's, bit for bit.  value = the domain's points
+    per step / step time."""
+    import torch
+
+    from letkf_gb300 import lib as L
+    from letkf_gb300.shard import exchange_obs, rank_grid, tile_of, tile_sweep
+    from letkf_gb300.sweep import PREC_MIXED, Sweep
+    from letkf_gb300.workload import RegionalWorkload
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    wl = RegionalWorkload(args.seed, args.nlon, args.nlat, args.nlev, args.ne, args.nobs, args.nv)
+    hdxf, dep, dat = wl.obs_torch(dev)
+    xb = wl.background_torch(dev)
+    pts = wl.points()
+    obs = {"ri": wl.ri, "rj": wl.rj, "lev": wl.lev, "dat": dat, "err": wl.err, "dep": dep, "cls": wl.cls,
+           "hdxf": hdxf}
+    ntiles = world if world > 1 else (args.tiles or 1)
+    px, py = rank_grid(ntiles)
+    mine = [rank] if world > 1 else list(range(ntiles))
+    t0 = time.perf_counter()
+    parts = []
+    for k in mine:
+        tile = tile_of(k, ntiles, args.nlon, args.nlat)
+        if world > 1:
+            own = np.arange(wl.nobs) % world == rank
+            local = {key: np.asarray(v)[own] for key, v in obs.items()}
+            local["uid"] = np.nonzero(own)[0]
+            halo = exchange_obs(local, tile, args.nlon, args.nlat, wl.params["dlon_zero"], wl.params["dlat_zero"])
+            points, sw, nobs_t = tile_sweep(tile, args.nlon, args.nlat, args.nlev, pts, halo, wl.params, args.ne,
+                                            args.nv, PREC_MIXED, halo=False)
+        else:
+            points, sw, nobs_t = tile_sweep(tile, args.nlon, args.nlat, args.nlev, pts, obs, wl.params, args.ne,
+                                            args.nv, PREC_MIXED)
+        xbt = xb[:, torch.as_tensor(points, device=dev), :].contiguous()
+        torch.cuda.current_stream().synchronize()
+        sw.set_background_device(xbt.data_ptr())
+        sw.set_inflation(np.ones(points.size))
+        parts.append({"tile": tile, "points": points, "sw": sw, "xb": xbt, "obs": nobs_t})
+    t_setup = time.perf_counter() - t0
+    stream = torch.cuda.Stream(device=dev)
+    for _ in range(args.warmup):
+        for pt in parts:
+            pt["sw"].run(stream.cuda_stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n0 = L.launch_count()
+    with ClockSampler(dev.index) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            for pt in parts:
+                pt["sw"].run(stream.cuda_stream)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    launches = L.launch_count() - n0
+    t = ev0.elapsed_time(ev1) / 1e3
+    if dist:
+        tt = torch.tensor([t], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    cfg = config_block(args, wl)
+    cfg["parallelism"] = (f"{ntiles} tiles ({px} x {py}) over {world} rank(s), halo exchange before the timed "
+                          f"region" + ("" if world > 1 else ", tiles in turn on one GPU"))
+    out = {"metric": METRIC, "value": wl.npts * args.steps / t, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+           "scaling": "strong", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded smooth random fields, clustered obs)", "config": cfg,
+           "gpu_launches": int(launches), "clocks": clk.summary(),
+           "decompose": {"tiles": ntiles, "grid": [px, py], "setup_s": round(t_setup, 1),
+                         "tiles_here": [{"tile": list(map(int, pt["tile"])), "points": int(pt["points"].size),
+                                         "halo_obs": pt["obs"]} for pt in parts]}}
+    if world == 1:
+        # the reassembled analysis against the single-domain sweep's
+        xa = np.zeros((args.nv, wl.npts, args.ne), np.float32)
+        for pt in parts:
+            pt["sw"].set_inflation(np.ones(pt["points"].size))
+            pt["sw"].run(stream.cuda_stream)
+            xa[:, pt["points"]] = pt["sw"].analysis()
+        one = Sweep(args.ne, args.nv, args.nlon, args.nlat, wl.npts, wl.params, precision=PREC_MIXED)
+        one.set_points(*pts, tile=4)
+        one.set_obs(wl.ri, wl.rj, wl.lev, dat, wl.err, dep, wl.cls, hdxf)
+        one.set_background_device(xb.data_ptr())
+        one.set_inflation(np.ones(wl.npts))
+        one.run(stream.cuda_stream)
+        xa1 = one.analysis()
+        one.close()
+        out["decompose"]["equal_to_single_domain"] = bool(np.array_equal(xa, xa1))
+        out["decompose"]["max_abs_diff"] = float(np.abs(xa - xa1).max())
+        out["decompose"]["nonfinite"] = [int((~np.isfinite(xa)).sum()), int((~np.isfinite(xa1)).sum())]
+        bad = np.nonzero(~np.isfinite(xa1).all(axis=(0, 2)))[0]
+        out["decompose"]["nonfinite_points_single"] = bad[:20].tolist()
+        bad = np.nonzero(~np.isfinite(xa).all(axis=(0, 2)))[0]
+        out["decompose"]["nonfinite_points_tiles"] = bad[:20].tolist()
+    for pt in parts:
+        pt["sw"].close()
+    return out
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -861,6 +974,8 @@ def main():
         dist = tdist
     if args.impl == "reference":
         line = run_reference(args, rank, world)
+    elif args.decompose:
+        line = run_decompose(args, rank, world, dist)
     else:
         line, sw = run_gpu(args, rank, world, dist)
         sw.close()

@@ -121,6 +121,28 @@ def gather_points(values, points, npts_total, group=None):
     return out
 
 
+OBS_KEYS = ("ri", "rj", "lev", "dat", "err", "dep", "cls")
+
+
+def tile_sweep(tile, nlon, nlat, nlev, pts, obs, params, ne, nv, precision, halo=True):
+    """The analysis handle of one tile: its grid points (every level, global
+    coordinates) and the observations of its halo.
+
+    pts: (ri, rj, rlev) of all nlon * nlat * nlev points in global numbering;
+    obs: dict with OBS_KEYS and "hdxf" [nobs, ne] in global observation order
+    (halo=True keeps the tile's halo; False: obs is that halo already, e.g. from
+    exchange_obs).  Returns (points, handle, observations kept)."""
+    from .sweep import Sweep
+
+    points = tile_points(tile, nlon, nlat, nlev)
+    keep = (halo_mask(obs["ri"], obs["rj"], tile, nlon, nlat, params["dlon_zero"], params["dlat_zero"]) if halo
+            else np.ones(len(obs["ri"]), dtype=bool))
+    sw = Sweep(ne, nv, nlon, nlat, points.size, params, precision=precision)
+    sw.set_points(pts[0][points], pts[1][points], pts[2][points], tile=4)
+    sw.set_obs(*(np.asarray(obs[k])[keep] for k in OBS_KEYS), np.asarray(obs["hdxf"])[keep])
+    return points, sw, int(keep.sum())
+
+
 class RankLost(RuntimeError):
     """A rank of the decomposition left or did not arrive for a cycle."""
 
