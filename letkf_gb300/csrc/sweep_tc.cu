@@ -210,8 +210,8 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
   const bool skip_all = __syncthreads_or(tmo);  // uniform over the CTA
   if (skip_all) tmo = 1;
 
-  // The CTA takes runs of col_unit consecutive order positions [run[0],
-  // run[1]).  Column cache of the search (state in shared memory, uniform over
+  // The CTA takes runs of consecutive order positions [run[0], run[1]), of
+  // col_unit positions until the end of the work nears.  Column cache of the search (state in shared memory, uniform over
   // the CTA): run[2] entries for the point column ckey = (ri, rj); -1: it did
   // not fit, -2: none.
   const bool col = a.col_ent != nullptr && !a.list_offs && (int)blockIdx.x < a.col_slots;
@@ -221,10 +221,15 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
     __syncthreads();
     if (tid == 0) {
       if (run[0] >= run[1]) {
-        const int unit = a.col_unit > 1 ? a.col_unit : 1;
-        const int64_t u0 = (int64_t)atomicAdd(a.counter, 1) * unit;
-        run[0] = (int)min(u0, (int64_t)npts_work);
-        run[1] = (int)min(u0 + unit, (int64_t)npts_work);
+        // guided self-scheduling over the positions: runs of col_unit while
+        // more than four runs per CTA remain, shorter ones towards the end
+        int len = a.col_unit > 1 ? a.col_unit : 1;
+        const int left = npts_work - *reinterpret_cast<volatile int*>(a.counter);
+        const int share = left / (4 * (int)gridDim.x);
+        if (share < len) len = share > 1 ? share : 1;
+        const int s0 = atomicAdd(a.counter, len);
+        run[0] = min(s0, npts_work);
+        run[1] = (int)min((int64_t)s0 + len, (int64_t)npts_work);
       }
       ctrl[0] = run[0]++;
     }
