@@ -96,9 +96,10 @@ struct SwCache {
 // Compaction of one batch of CPT*NT evaluated candidates: accepted ones go to
 // the pending list (and the probe) in candidate order, survivors to the
 // column cache; flush(CH) consumes the pending list in stages of CH.
-template <int NT, int CH, int CPT, bool BUILD, typename Flush>
+template <int NT, int CH, int CPT, typename Flush>
 __device__ __forceinline__ void sw_compact(const SweepArgs& a, const SearchSmem& s, int probe, const SwCand (&cg)[CPT],
                                            int& pend, int& L, const SwCache& cache, int& nsurv, Flush& flush) {
+  const bool BUILD = cache.ent != nullptr;  // uniform
   constexpr int NW = NT / 32;
   constexpr int SV = CPT * NW + 1;  // survivors' counts follow the accepted ones
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -216,12 +217,13 @@ __device__ __forceinline__ bool sw_accept(const SweepArgs& a, int ob, float nd, 
 // candidates (CPT per thread, candidate base + g*NT + tid in group g), so the
 // batches and their barriers are CPT times fewer; accepted observations are
 // compacted group by group, which keeps the reference's candidate order.
-// BUILD: the column cache of this point's (ri, rj) is written on the way;
-// *nsurv receives its length (above cache.cap: not usable).
-template <int NT, int CH, int CPT, bool BUILD, typename Flush>
+// With cache.ent set, the column cache of this point's (ri, rj) is written
+// on the way; *nsurv receives its length (above cache.cap: not usable).
+template <int NT, int CH, int CPT, typename Flush>
 __device__ int sweep_search(const SweepArgs& a, double ri, double rj, double logr, double rz, const SearchSmem& s,
                             int probe, Flush&& flush, const SwCache& cache = SwCache{nullptr, 0},
                             int* nsurv_out = nullptr) {
+  const bool BUILD = cache.ent != nullptr;  // uniform
   const int tid = threadIdx.x;
   const int ld = a.nlon + 1;
   const float band_hi = 13.33333333f * (1.f + SW_BAND);
@@ -291,7 +293,7 @@ __device__ int sweep_search(const SweepArgs& a, double ri, double rj, double log
           }
         }
       }
-      sw_compact<NT, CH, CPT, BUILD>(a, s, probe, cg, pend, L, cache, nsurv, flush);
+      sw_compact<NT, CH, CPT>(a, s, probe, cg, pend, L, cache, nsurv, flush);
     }
   }
   if (pend > 0) {
@@ -342,7 +344,7 @@ __device__ int sweep_search_cached(const SweepArgs& a, const int4* __restrict__ 
         o.d = __int_as_float(e1.z);
       }
     }
-    sw_compact<NT, CH, 1, false>(a, s, probe, cg, pend, L, none, nsurv, flush);
+    sw_compact<NT, CH, 1>(a, s, probe, cg, pend, L, none, nsurv, flush);
     e0 = f0;
     e1 = f1;
   }

@@ -318,14 +318,14 @@ __global__ void __launch_bounds__(TC_NT, 4) sweep_tc_kernel(SweepArgs a) {
     } else if (col && !same_col) {
       int nsv = 0;
       const SwCache cache{a.col_ent + (size_t)blockIdx.x * a.col_cap * 2, a.col_cap};
-      Lp = sweep_search<TC_NT, TC_CH, TC_CPT, true>(a, ri, rj, logr, rz, ss, probe, flush, cache, &nsv);
+      Lp = sweep_search<TC_NT, TC_CH, TC_CPT>(a, ri, rj, logr, rz, ss, probe, flush, cache, &nsv);
       if (tid == 0) {  // read by the next point, after the barriers in between
         ckey[0] = ri;
         ckey[1] = rj;
         run[2] = nsv <= a.col_cap ? nsv : -1;
       }
     } else {  // no cache, or this column's did not fit
-      Lp = sweep_search<TC_NT, TC_CH, TC_CPT, false>(a, ri, rj, logr, rz, ss, probe, flush);
+      Lp = sweep_search<TC_NT, TC_CH, TC_CPT>(a, ri, rj, logr, rz, ss, probe, flush);
     }
     for (int b = 0; b < 2; b++)
       if ((outst >> b) & 1u) {

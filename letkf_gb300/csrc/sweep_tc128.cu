@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(T8_NT, 1) sweep_tc128_kernel(SweepArgs a) {
     };
     const int probe = a.probe_slot ? a.probe_slot[pt] : -1;
     const int Lp = a.list_offs ? sweep_list<T8_NT, T8_CH>(a, qq, ss, flush)
-                               : sweep_search<T8_NT, T8_CH, 1, false>(a, ri, rj, logr, rz, ss, probe, flush);
+                               : sweep_search<T8_NT, T8_CH, 1>(a, ri, rj, logr, rz, ss, probe, flush);
     for (int b = 0; b < 2; b++)
       if ((outst >> b) & 1u) {
         wait_bar(b);
