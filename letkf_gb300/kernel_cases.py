@@ -7,6 +7,9 @@ where the kernel streams the ensemble):
   sweep_tc      tensor-core sweep of a 96x96x16 regional domain (147,456
                 points, k = 64, 6 variables, 140,625 clustered obs) and its
                 deferred-point pass
+  sweep_tc40    tensor-core sweep of a 64x64x40 regional domain (163,840
+                points in columns of 40 levels as the benchmark's, k = 64, 6
+                variables, 62,500 clustered obs: the benchmark's density)
   sweep_simt    the same sweep on the SIMT kernel
   sweep_tc128   the tensor-core sweep of the same domain with k = 128
   search_700km  SPEEDY lat/lon search (count and fill) of 64 points of the
@@ -36,18 +39,18 @@ import time
 import numpy as np
 
 
-def _regional(ne=64):
+def _regional(ne=64, shape=(96, 96, 16), nobs=140_625):
     from .workload import RegionalWorkload
 
-    return RegionalWorkload(5, 96, 96, 16, ne, 140_625, 6)
+    return RegionalWorkload(5, *shape, ne, nobs, 6)
 
 
-def case_sweep(dev, tc, ne=64):
+def case_sweep(dev, tc, ne=64, shape=(96, 96, 16), nobs=140_625):
     import torch
 
     from .sweep import OPT_TENSOR_CORES, PREC_MIXED, Sweep
 
-    wl = _regional(ne)
+    wl = _regional(ne, shape, nobs)
     hdxf, dep, dat = wl.obs_torch(dev)
     xb = wl.background_torch(dev)
     ri, rj, plev = wl.points()
@@ -260,6 +263,7 @@ def case_obs_space(dev):
 
 
 CASES = {"sweep_tc": lambda d: case_sweep(d, True), "sweep_simt": lambda d: case_sweep(d, False),
+         "sweep_tc40": lambda d: case_sweep(d, True, shape=(64, 64, 40), nobs=62_500),
          "sweep_tc128": lambda dev: case_sweep(dev, True, ne=128), "search_700km": case_search_700km,
          "f64": case_f64, "l96": case_l96, "relax": case_relax, "largek": case_largek,
          "speedy_io": case_speedy_io, "obsope": case_obsope, "obs_space": case_obs_space}
