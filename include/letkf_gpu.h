@@ -317,6 +317,36 @@ int letkf_speedy_obsope(int nlon, int nlat, int nlev, int ne, const double* lat,
                         const int* elem, const double* rlon, const double* rlat, const double* rlev,
                         const double* odat, double* hx, int* qc_member, int* qc, void* stream);
 
+/* SCALE observation operator H(x) for conventional observations, every
+ * member (scale/obs/obsope_tools.f90:340-380, the OBS_IN_FORMAT 1 path):
+ * phys2ijk (scale/common/common_obs_scale.f90:969-1075) then Trans_XtoY
+ * (:262-334) for u 2819, v 2820, t 3073, tv 3074, q 3330, rh 3331 and ps
+ * 14593 (prsadj to the observation height, :583-599).  Fields (device, FP64),
+ * each member's local domain with halos, k fastest as the reference's
+ * v3dg(nlevh, nlonh, nlath, nv3dd): v3d element (k, i, j, n) of member m at
+ * v3d[m*v3d_mem_stride + n*v3d_var_stride + (j*nlonh + i)*nlevh + k] (0-based;
+ * n = 0 u, 1 v, 2 t, 3 q, 4 rh, 5 full pressure p; nlevh = nlev + 2*khalo),
+ * v2d (i, j, n) at v2d[m*v2d_mem_stride + n*v2d_var_stride + j*nlonh + i]
+ * (n = 0 ps, 1 t2m, 2 q2m, 3 topo).  khalo >= 2 (KHALO).  Observations
+ * (device): elem[nobs], ri / rj (1-based grid coordinates of the halo domain,
+ * as obsope's ri / rj), rlev (Pa; the height in m for surface elements >
+ * 9999), rotc[nobs][2] (the map projection's rotation coefficients at the
+ * observation, MPRJ_rotcoef of SCALE-RM; NULL: (1, 0)); stggrd 1: u / v on
+ * the staggered grid; ps_adjust_thres: PS_ADJUST_THRES (100 m by default).
+ * Outputs: hx[nobs][ne] (0 where phys2ijk rejects, -9.99e33 with qc 90 for
+ * another element), qc_member[nobs][ne] (may be NULL), qc[nobs] = the maximum
+ * over members (obsope_tools.f90:602-608; may be NULL); qc codes 0 good, 10
+ * ps height adjustment beyond the threshold, 20 too high, 21 too low, 22
+ * outside the domain, 90 other element.  An interpolation stencil keeps its
+ * upper index in [2, n] (the reference's value wherever its stencil stays in
+ * its arrays; the staggered u / v at ri - 0.5 < 1 extrapolate from the edge
+ * columns, where the reference reads outside its array). */
+int letkf_scale_obsope(int nlonh, int nlath, int nlev, int khalo, int ne, const double* v3d,
+                       int64_t v3d_mem_stride, int64_t v3d_var_stride, const double* v2d, int64_t v2d_mem_stride,
+                       int64_t v2d_var_stride, int nobs, const int* elem, const double* ri, const double* rj,
+                       const double* rlev, const double* rotc, int stggrd, double ps_adjust_thres, double* hx,
+                       int* qc_member, int* qc, void* stream);
+
 /* SPEEDY grid-file records (speedy/common/common_speedy.f90:163-287): a file
  * is nrec records of nij = nlon*nlat REAL(4) (u levels, v, t, q, ps, rain),
  * big-endian as the reference's -byteswapio build writes them.  raw holds ne

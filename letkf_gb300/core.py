@@ -266,6 +266,38 @@ def efso(ne, offs, idx, rdiag, rloc, hdxa, fcst, fcer, term, obsdep, stream=None
 
 
 SPEEDY_ELEM = {"u": 2819, "v": 2820, "t": 3073, "q": 3330, "rh": 3331, "ps": 14593, "rain": 9999}
+SCALE_ELEM = {"u": 2819, "v": 2820, "t": 3073, "tv": 3074, "q": 3330, "rh": 3331, "ps": 14593}
+
+
+def scale_obsope(v3d, v2d, khalo, elem, ri, rj, rlev, rotc=None, stggrd=0, ps_adjust_thres=100.0,
+                 want_member_qc=False, stream=None):
+    """SCALE observation operator for conventional observations, all members
+    (scale/obs/obsope_tools.f90:340-380: phys2ijk and Trans_XtoY of
+    scale/common/common_obs_scale.f90).  v3d: float64 [ne, 6, nlath, nlonh,
+    nlevh] (u, v, t, q, rh, full pressure; levels fastest as the reference's
+    v3dg; nlevh = nlev + 2 khalo), v2d: float64 [ne, 4, nlath, nlonh] (ps,
+    t2m, q2m, topo), each contiguous per variable; observations elem (int32) /
+    ri / rj (halo-domain grid coordinates) / rlev [nobs], rotc [nobs, 2] or
+    None, all on the device.  Returns (hx [nobs, ne], qc [nobs] int32, the
+    maximum over members) and, with want_member_qc, qc per member."""
+    import torch
+
+    ne, nv3, nlath, nlonh, nlevh = v3d.shape
+    nlev = nlevh - 2 * khalo
+    if nv3 != 6 or tuple(v2d.shape) != (ne, 4, nlath, nlonh):
+        raise ValueError("scale_obsope: v3d [ne, 6, nlath, nlonh, nlevh] and v2d [ne, 4, nlath, nlonh] expected")
+    for t in (v3d, v2d):
+        if t.dtype != torch.float64 or not t[0, 0].is_contiguous():
+            raise ValueError("scale_obsope: float64 fields, each variable contiguous, expected")
+    nobs = elem.numel()
+    hx = torch.empty((nobs, ne), dtype=torch.float64, device=v3d.device)
+    qc = torch.empty(nobs, dtype=torch.int32, device=v3d.device)
+    qcm = torch.empty((nobs, ne), dtype=torch.int32, device=v3d.device) if want_member_qc else None
+    check(lib().letkf_scale_obsope(nlonh, nlath, nlev, int(khalo), ne, _viewptr(v3d), v3d.stride(0), v3d.stride(1),
+                                   _viewptr(v2d), v2d.stride(0), v2d.stride(1), nobs, _dptr(elem), _dptr(ri),
+                                   _dptr(rj), _dptr(rlev), _dptr(rotc), int(stggrd), float(ps_adjust_thres),
+                                   _dptr(hx), _dptr(qcm), _dptr(qc), _stream(stream)), "letkf_scale_obsope")
+    return (hx, qc, qcm) if want_member_qc else (hx, qc)
 
 
 def speedy_obsope(lat, sig, v3d, v2d, elem, rlon, rlat, rlev, odat, want_member_qc=False, stream=None):

@@ -78,6 +78,8 @@ _SIGS = {
     "letkf_ens_mean_spread": (_i, [_i64, _i, _i, _vp, _i64, _i64, _vp, _vp, _vp]),
     "letkf_speedy_obsope": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _i64, _i64, _vp, _i64, _i64, _i, _vp, _vp, _vp, _vp,
                                  _vp, _vp, _vp, _vp, _vp]),
+    "letkf_scale_obsope": (_i, [_i, _i, _i, _i, _i, _vp, _i64, _i64, _vp, _i64, _i64, _i, _vp, _vp, _vp, _vp, _vp,
+                                _i, _d, _vp, _vp, _vp, _vp]),
     "letkf_update_relax_f64": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "letkf_relax_beta": (_i, [_i, _i, _vp, _vp, _vp, _i, _i, _d, _d, _d, _d, _i, _i, _i, _i, _vp, _vp]),
 }

@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
 LIB_TIMED = os.path.join(BUILD, "liboracle_timed.so")
-SOURCES = ["letkf_core.c", "obs_local.c", "sweep.c", "obs_operator.c"]
+SOURCES = ["letkf_core.c", "obs_local.c", "sweep.c", "obs_operator.c", "obs_operator_scale.c"]
 # parity build: every multiply and add rounded on its own
 FLAGS = ["-std=c99", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fno-fast-math"]
 # the build the CPU baseline is timed with: -O3 and FMA contraction, as the

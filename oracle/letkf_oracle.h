@@ -177,6 +177,16 @@ void oracle_efso(int ne, int npts, int nv, int nterm, const int64_t* offs, const
                  int nobs, const double* obsdep, double* djdy, double* obsense);
 
 
+/* SCALE observation operator for conventional observations
+ * (scale/obs/obsope_tools.f90:340-380, scale/common/common_obs_scale.f90:
+ * 262-334, 969-1075): per (observation, member) phys2ijk then Trans_XtoY;
+ * hx[n][m], qc_member[n][m] (may be NULL), qc[n] = the maximum over members
+ * (may be NULL).  Layout in obs_operator_scale.c. */
+int oracle_scale_obsope(int nlonh, int nlath, int nlev, int khalo, int ne, const double* v3d, int64_t v3d_mem,
+                        int64_t v3d_var, const double* v2d, int64_t v2d_mem, int64_t v2d_var, int nobs,
+                        const int* elem, const double* ri, const double* rj, const double* rlev, const double* rotc,
+                        int stggrd, double ps_thres, double* hx, int* qc_member, int* qc);
+
 /* SPEEDY observation operator (speedy/letkf/obsope.f90:53-104 with phys2ijk,
  * Trans_XtoY, calc_rh, itpl_2d/3d of speedy/common/common_obs_speedy.f90) */
 double oracle_speedy_calc_rh(double t, double q, double p);

@@ -74,6 +74,9 @@ def lib(timed=False):
         i64 = C.c_int64
         _lib.oracle_speedy_calc_rh.restype = d
         _lib.oracle_speedy_calc_rh.argtypes = [d, d, d]
+        _lib.oracle_scale_obsope.restype = C.c_int
+        _lib.oracle_scale_obsope.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, pd, i64, i64, pd, i64,
+                                             i64, C.c_int, pi, pd, pd, pd, pd, C.c_int, d, pd, pi, pi]
         _lib.oracle_speedy_obsope.restype = C.c_int
         _lib.oracle_speedy_obsope.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, pd, pd, pd, i64, i64, pd, i64, i64,
                                               C.c_int, pi, pd, pd, pd, pd, pd, pi, pi]
@@ -426,6 +429,29 @@ def efso(ne, offs, idx, rdiag, rloc, hdxa, fcst, fcer, term, obsdep):
                       _pi(np.ascontiguousarray(idx, dtype=np.int32)), _pd(_f64(rdiag)), _pd(_f64(rloc)), _pd(hdxa),
                       _pd(fcst), _pd(_f64(fcer)), _pi(term), nobs, _pd(_f64(obsdep)), _pd(djdy), _pd(obsense))
     return djdy, obsense
+
+
+def scale_obsope(v3d, v2d, khalo, elem, ri, rj, rlev, rotc=None, stggrd=0, ps_adjust_thres=100.0):
+    """SCALE conventional H(x) for every member (scale/obs/obsope_tools.f90:
+    340-380).  v3d [ne, 6, nlath, nlonh, nlevh] (u, v, t, q, rh, p; C order,
+    levels fastest), v2d [ne, 4, nlath, nlonh] (ps, t2m, q2m, topo).  Returns
+    (hx [nobs, ne], qc [nobs], qc_member [nobs, ne])."""
+    v3d = _f64(v3d)
+    v2d = _f64(v2d)
+    ne, _, nlath, nlonh, nlevh = v3d.shape
+    elem = np.ascontiguousarray(elem, dtype=np.int32)
+    nobs = elem.size
+    hx = np.zeros((nobs, ne))
+    qcm = np.zeros((nobs, ne), dtype=np.int32)
+    qc = np.zeros(nobs, dtype=np.int32)
+    rc = None if rotc is None else _f64(rotc)
+    st = lib().oracle_scale_obsope(nlonh, nlath, nlevh - 2 * khalo, khalo, ne, _pd(v3d), 6 * nlath * nlonh * nlevh,
+                                   nlath * nlonh * nlevh, _pd(v2d), 4 * nlath * nlonh, nlath * nlonh, nobs, _pi(elem),
+                                   _pd(_f64(ri)), _pd(_f64(rj)), _pd(_f64(rlev)), _pd(rc), int(stggrd),
+                                   float(ps_adjust_thres), _pd(hx), _pi(qcm), _pi(qc))
+    if st:
+        raise ValueError("oracle_scale_obsope: khalo >= 2 and nlev >= 2 expected")
+    return hx, qc, qcm
 
 
 def speedy_calc_rh(t, q, p):

@@ -119,3 +119,26 @@ def test_new_entry_points_check_arguments_before_the_device():
     # slot out of range
     assert ad(8, 1, 4, cell, 2, pix, 1, 3.0, 2.0, 1.0, 0, 1.0, 1.0, 20, None, None, None, None, None, None, None,
               None) == L.LETKF_ERR_ARG
+
+
+def test_scale_obsope_checks_arguments_before_the_device():
+    """letkf_scale_obsope refuses khalo < 2 (the reference's level search can
+    reach two halo levels above the top), short variable strides and missing
+    observation arrays with LETKF_ERR_ARG, before any device call."""
+    from letkf_gb300 import lib as L
+
+    f = L.lib().letkf_scale_obsope
+    plane3, plane2 = 36 * 30 * 24, 36 * 30
+    args = lambda kh, var3, nobs: (36, 30, 24 - 2 * kh, kh, 4, None, 0, var3, None, 0, plane2, nobs, None, None, None,
+                                   None, None, 0, 100.0, None, None, None, None)
+    assert f(*args(1, plane3, 0)) == L.LETKF_ERR_ARG
+    assert f(*args(2, plane3, 0)) == L.LETKF_ERR_ARG        # NULL fields
+    import ctypes as C
+
+    buf = (C.c_double * 1)()
+    a = list(args(2, plane3 - 1, 0))
+    a[5] = a[8] = C.cast(buf, C.c_void_p)
+    assert f(*a) == L.LETKF_ERR_ARG                        # variable stride below one domain
+    a = list(args(2, plane3, 5))
+    a[5] = a[8] = C.cast(buf, C.c_void_p)
+    assert f(*a) == L.LETKF_ERR_ARG                        # observations missing
