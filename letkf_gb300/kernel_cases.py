@@ -14,6 +14,12 @@ where the kernel streams the ensemble):
   sweep_tc128   the tensor-core sweep of the same domain with k = 128
   search_700km  SPEEDY lat/lon search (count and fill) of 64 points of the
                 360x181x32 global grid with 3e6 observations at 700 km
+  largek_700km  the large-k step of 16 of those points (k = 512, BF16
+                observation ensemble): search, the mixed-precision core and
+                its FP64 pass (every point at 700 km), BF16-storage update
+  scale_obsope  SCALE observation operator, 40 members of a 128x128x30
+                domain (KHALO 2, 1.07 GB of FP64 fields), 100,000
+                conventional observations of every element
   f64           FP64 plain form of 8,192 of those points: search (count,
                 fill), gather, core_f64, update_f64
   l96           Lorenz-96 ring of 100,000 variables, k = 32: departures,
@@ -182,6 +188,75 @@ def case_search_700km(dev):
     return f"64 points of the 360x181x32 grid, 3e6 obs, 700 km: {int(offs[-1])} local obs, {dt * 1e3:.1f} ms"
 
 
+def case_largek_700km(dev):
+    import torch
+
+    from .core import core_batch_largek_indexed, search_speedy, update_bf16
+    from .workload import GlobalWorkload
+
+    wl = GlobalWorkload(21)
+    hdxf, dep, dat = wl.obs_torch(dev)
+    hdxf16 = hdxf.to(torch.bfloat16)
+    del hdxf
+    dep32 = dep.to(torch.float32)
+    params = wl.search_params(700.0e3)
+    idx = np.sort(np.random.default_rng(5).choice(wl.npts, 16, replace=False))
+    lon, lat, dlon, ilev, lnp = wl.points(idx, params)
+    f = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
+    grid = {"lon": f(wl.lon), "lat": f(wl.lat), "nobsgrd": torch.as_tensor(wl.nobsgrd, dtype=torch.int32, device=dev)}
+    obs = {"elm": f(wl.elm), "lon": f(wl.olon), "lat": f(wl.olat), "lev": f(wl.olev), "dat": dat, "err": f(wl.err)}
+    pts = {"lon": f(lon), "lat": f(lat), "dlon_zero": f(dlon), "ilev": torch.as_tensor(ilev, device=dev),
+           "logpfm": f(lnp)}
+    xb = wl.background_torch(dev, idx)
+    xmean = xb.double().mean(-1).to(torch.float32)
+    xpert16 = (xb - xmean[..., None]).to(torch.bfloat16)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    offs, oi, rl, rd = search_speedy(grid, obs, pts, params, np.ones(7))
+    infl = torch.full((idx.size,), 1.05, dtype=torch.float64, device=dev)
+    core = core_batch_largek_indexed(wl.ne, offs, oi, hdxf16, dep32, rd.to(torch.float32), rl.to(torch.float32),
+                                     infl, want_transm=True)
+    update_bf16(xmean, xpert16, core["trans"], core["transm"])
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    ok = int((core["status"] == 0).sum())
+    return f"16 points, k = {wl.ne}, 700 km: {int(offs[-1])} local obs, {ok} LETKF_OK, {dt * 1e3:.1f} ms"
+
+
+def case_scale_obsope(dev):
+    import torch
+
+    from .core import SCALE_ELEM, scale_obsope
+
+    ne, nlonh, nlath, nlev, kh, nobs = 40, 128, 128, 30, 2, 100_000
+    g = torch.Generator(device=dev).manual_seed(6)
+    nlevh = nlev + 2 * kh
+    sig = torch.exp(-torch.linspace(-0.2, 4.2, nlevh, dtype=torch.float64, device=dev))
+    ps = 1.0e5 * (1 + 0.02 * torch.randn((ne, 1, nlath, nlonh, 1), generator=g, device=dev, dtype=torch.float64))
+    v3d = torch.randn((ne, 6, nlath, nlonh, nlevh), generator=g, device=dev, dtype=torch.float64)
+    v3d[:, 2] = 260 + 10 * v3d[:, 2]
+    v3d[:, 3] = 0.005 + 0.002 * v3d[:, 3]
+    v3d[:, 5] = (ps * sig)[:, 0]
+    v2d = torch.randn((ne, 4, nlath, nlonh), generator=g, device=dev, dtype=torch.float64)
+    v2d[:, 0] = ps[:, 0, :, :, 0]
+    v2d[:, 1] = 285 + v2d[:, 1]
+    v2d[:, 2] = 0.008 + 0.001 * v2d[:, 2]
+    v2d[:, 3] = 200 + 100 * v2d[:, 3]
+    codes = torch.tensor(list(SCALE_ELEM.values()), dtype=torch.int32, device=dev)
+    elem = codes[torch.randint(0, codes.numel(), (nobs,), generator=g, device=dev)]
+    ri = 1 + (nlonh - 1) * torch.rand(nobs, generator=g, device=dev, dtype=torch.float64)
+    rj = 1 + (nlath - 1) * torch.rand(nobs, generator=g, device=dev, dtype=torch.float64)
+    rlev = torch.exp(np.log(3e3) + (np.log(1e5) - np.log(3e3)) *
+                     torch.rand(nobs, generator=g, device=dev, dtype=torch.float64))
+    rlev = torch.where(elem == SCALE_ELEM["ps"], 300.0 * torch.rand_like(rlev), rlev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hx, qc = scale_obsope(v3d, v2d, kh, elem, ri, rj, rlev)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    return f"{nobs} obs x {ne} members, {int((qc == 0).sum())} good, {dt * 1e3:.2f} ms"
+
+
 def _speedy_members(dev, ne=80, nlon=192, nlat=96, nlev=7):
     import torch
 
@@ -266,7 +341,8 @@ CASES = {"sweep_tc": lambda d: case_sweep(d, True), "sweep_simt": lambda d: case
          "sweep_tc40": lambda d: case_sweep(d, True, shape=(64, 64, 40), nobs=62_500),
          "sweep_tc128": lambda dev: case_sweep(dev, True, ne=128), "search_700km": case_search_700km,
          "f64": case_f64, "l96": case_l96, "relax": case_relax, "largek": case_largek,
-         "speedy_io": case_speedy_io, "obsope": case_obsope, "obs_space": case_obs_space}
+         "speedy_io": case_speedy_io, "obsope": case_obsope, "obs_space": case_obs_space,
+         "largek_700km": case_largek_700km, "scale_obsope": case_scale_obsope}
 
 
 def main():
