@@ -18,9 +18,13 @@
 //
 // One warp per observation, members over the lanes; products and sums use the
 // _rn intrinsics in the reference's expression order, so only log and pow
-// differ (by an ulp) from a host build.  Interpolation stencils keep their
-// upper index in [2, n]: the value of the reference wherever its own stencil
-// stays inside the arrays.
+// differ (by an ulp) from a host build.  phys2ijk takes log of the full
+// pressure at the four columns of each level it visits; where the
+// observations would take more of those logs than the members' grids hold, a
+// first kernel writes ln p for every grid point and member (the same device
+// log of the same values, so the same bits) and phys2ijk reads it instead.
+// Interpolation stencils keep their upper index in [2, n]: the value of the
+// reference wherever its own stencil stays inside the arrays.
 #include "letkf_common.cuh"
 
 namespace letkf {
@@ -32,6 +36,7 @@ constexpr double SC_UNDEF = -9.99e33;  // common/common.f90:38
 
 struct ScaleFields {
   int nlonh, nlath, nlevh, nlev, khalo, ne;
+  const double* lnp;  // [ne][nlath][nlonh][nlevh] ln p of every grid point, or NULL (computed on the way)
   const double* v3d;  // (k, i, j, n) of member m at v3d[m*mem3 + n*var3 + ((j-1)*nlonh + (i-1))*nlevh + (k-1)]
   int64_t mem3, var3;  // n = 0 u, 1 v, 2 t, 3 q, 4 rh, 5 p (full pressure)
   const double* v2d;  // (i, j, n) of member m at v2d[m*mem2 + n*var2 + (j-1)*nlonh + (i-1)]
@@ -89,14 +94,30 @@ __device__ double sc_itpl3(const ScaleFields& f, int m, int n, double rk, double
   return sadd(s, smul(smul(smul(sf3(f, m, n, a, b, c), aa), ab), ac));
 }
 
+// LOG(p_full) at (k, i, j) of member m
+__device__ __forceinline__ double sc_logp(const ScaleFields& f, int m, long long k, long long i, long long j) {
+  if (f.lnp) return f.lnp[(((int64_t)m * f.nlath + (j - 1)) * f.nlonh + (i - 1)) * f.nlevh + (k - 1)];
+  return log(sf3(f, m, 5, k, i, j));
+}
+
 // log p of level k bilinear in (ri, rj): itpl_2d_column of LOG(p_full) (:1019-1020)
 __device__ __forceinline__ double sc_lnp(const ScaleFields& f, int m, long long k, long long i, long long j, double ai,
                                          double aj) {
   const double bi = ssub(1.0, ai), bj = ssub(1.0, aj);
-  double s = smul(smul(log(sf3(f, m, 5, k, i - 1, j - 1)), bi), bj);
-  s = sadd(s, smul(smul(log(sf3(f, m, 5, k, i, j - 1)), ai), bj));
-  s = sadd(s, smul(smul(log(sf3(f, m, 5, k, i - 1, j)), bi), aj));
-  return sadd(s, smul(smul(log(sf3(f, m, 5, k, i, j)), ai), aj));
+  double s = smul(smul(sc_logp(f, m, k, i - 1, j - 1), bi), bj);
+  s = sadd(s, smul(smul(sc_logp(f, m, k, i, j - 1), ai), bj));
+  s = sadd(s, smul(smul(sc_logp(f, m, k, i - 1, j), bi), aj));
+  return sadd(s, smul(smul(sc_logp(f, m, k, i, j), ai), aj));
+}
+
+// ln p of every grid point of every member
+__global__ void scale_lnp_kernel(ScaleFields f, double* lnp) {
+  const int64_t plane = (int64_t)f.nlath * f.nlonh * f.nlevh, n = plane * f.ne;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int m = (int)(t / plane);
+    const int64_t r = t - (int64_t)m * plane;
+    lnp[t] = log(f.v3d[(int64_t)m * f.mem3 + 5 * f.var3 + r]);
+  }
 }
 
 // phys2ijk (:969-1075): qc, and rk where it is good
@@ -223,10 +244,27 @@ extern "C" int letkf_scale_obsope(int nlonh, int nlath, int nlev, int khalo, int
   const int per = SOPE_NT / 32;
   const int need = (nobs + per - 1) / per;
   const int grid = need < nsm * 8 ? need : nsm * 8;
-  ScaleFields f{nlonh, nlath, nlev + 2 * khalo, nlev, khalo, ne, v3d, v3d_mem_stride, v3d_var_stride,
+  ScaleFields f{nlonh, nlath, nlev + 2 * khalo, nlev, khalo, ne, nullptr, v3d, v3d_mem_stride, v3d_var_stride,
                 v2d, v2d_mem_stride, v2d_var_stride};
-  scale_obsope_kernel<<<grid, SOPE_NT, 0, (cudaStream_t)stream>>>(f, nobs, elem, ri, rj, rlev, rotc, stggrd,
-                                                                  ps_adjust_thres, hx, qc_member, qc);
+  cudaStream_t s = (cudaStream_t)stream;
+  // ln p once per grid point where the observations would visit more (four
+  // columns, about half the levels each)
+  const int64_t plane = (int64_t)nlath * nlonh * f.nlevh;
+  double* lnp = nullptr;
+  if ((int64_t)nobs * 4 * (nlev / 2 + 1) > plane && cudaMallocAsync((void**)&lnp, sizeof(double) * plane * ne, s) ==
+                                                        cudaSuccess) {
+    const int64_t n = plane * ne;
+    const int64_t blocks = (n + 255) / 256;
+    scale_lnp_kernel<<<(unsigned)(blocks < (int64_t)nsm * 16 ? blocks : (int64_t)nsm * 16), 256, 0, s>>>(f, lnp);
+    note_launch();
+    f.lnp = lnp;
+  } else {
+    cudaGetLastError();  // an allocation that failed leaves the on-the-way logs
+  }
+  scale_obsope_kernel<<<grid, SOPE_NT, 0, s>>>(f, nobs, elem, ri, rj, rlev, rotc, stggrd, ps_adjust_thres, hx,
+                                               qc_member, qc);
   note_launch();
-  return cuda_status(cudaGetLastError());
+  const int st = cuda_status(cudaGetLastError());
+  if (lnp) cudaFreeAsync(lnp, s);
+  return st;
 }

@@ -248,7 +248,8 @@ def case_scale_obsope(dev):
     rj = 1 + (nlath - 1) * torch.rand(nobs, generator=g, device=dev, dtype=torch.float64)
     rlev = torch.exp(np.log(3e3) + (np.log(1e5) - np.log(3e3)) *
                      torch.rand(nobs, generator=g, device=dev, dtype=torch.float64))
-    rlev = torch.where(elem == SCALE_ELEM["ps"], 300.0 * torch.rand_like(rlev), rlev)
+    rlev = torch.where(elem == SCALE_ELEM["ps"],
+                       300.0 * torch.rand(nobs, generator=g, device=dev, dtype=torch.float64), rlev)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     hx, qc = scale_obsope(v3d, v2d, kh, elem, ri, rj, rlev)
