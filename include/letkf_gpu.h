@@ -458,7 +458,7 @@ int letkf_l96_obs_cell(int nx, int ny, const double* h, int* cell, void* stream)
 #define LETKF_OPT_GRID_SHARE 16    /* v >= 1: each persistent sweep launch takes 1/v of the CTAs its kernel can keep
                                       resident (the server's slots share the SMs this way); replaces a grid cap */
 #define LETKF_OPT_COLUMN_UNIT 17   /* where the points come in columns (equal ri, rj; the levels of a grid column), a
-                                      tensor-core CTA (ne <= 64) takes v consecutive order positions at a time and keeps
+                                      tensor-core CTA (ne <= 128) takes v consecutive order positions at a time and keeps
                                       the search's horizontal candidates of its column for the next levels, which apply
                                       only the vertical test (same lists, order and weights); v >= 1, or -1 (default):
                                       the mean column length of the points; 0: off */

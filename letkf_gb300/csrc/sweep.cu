@@ -827,8 +827,8 @@ static void build_args(letkf_sweep_t h, SweepArgs& a) {
   a.probe_rloc = h->probe_rloc;
   a.probe_count = h->probe_count;
   a.fault_wait_polls = h->fault_wait;
-  // the column cache serves the tensor-core sweep for ne <= 64
-  if (h->columns && h->col_ent && h->col_unit != 0 && h->d.ne <= 64) {
+  // the column cache serves the tensor-core sweeps (ne <= 128)
+  if (h->columns && h->col_ent && h->col_unit != 0 && h->d.ne <= 128) {
     a.col_ent = h->col_ent;
     a.col_cap = LETKF_COL_CAP;
     a.col_slots = h->col_slots;

@@ -69,8 +69,10 @@ struct T8Layout {
   static constexpr int MEAN = ((WCNT + 4 * 2 * (T8_NT / 32 + 1)) + 7) & ~7;  // double[16]
   static constexpr int MBAR = MEAN + 128;             // uint64[5]: Gram stages 0/1, products, rows, drain
   static constexpr int TMEMH = MBAR + 40;
-  static constexpr int CTRL = TMEMH + 8;              // int[4]
-  static constexpr int TOTAL = CTRL + 16;
+  static constexpr int CTRL = TMEMH + 8;              // int[4]: position, scratch
+  static constexpr int CKEY = CTRL + 16;              // double[2]: the column-cache point (ri, rj)
+  static constexpr int RUN = CKEY + 16;               // int[4]: run of positions [next, end), column-cache length
+  static constexpr int TOTAL = RUN + 16;
   static_assert(4 * PCAP >= 8 * 128, "background rows (nv <= 8, ne <= 128) fit the pending-list area");
 };
 
@@ -137,6 +139,11 @@ __global__ void __launch_bounds__(T8_NT, 1) sweep_tc128_kernel(SweepArgs a) {
   if (tid == 0) {
     for (int i = 0; i < 5; i++) tc::mbar_init(&mbar[i], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    int* rn = reinterpret_cast<int*>(sm + L::RUN);
+    rn[0] = rn[1] = 0;
+    rn[2] = -2;
+    double* ck = reinterpret_cast<double*>(sm + L::CKEY);
+    ck[0] = ck[1] = __longlong_as_double(0x7ff8000000000000ll);  // NaN: equal to no point
   }
   if (wid == 0) tc::tmem_alloc(tmem_holder, T8_TMEM_COLS);
   tc::fence_before_sync();
@@ -166,9 +173,25 @@ __global__ void __launch_bounds__(T8_NT, 1) sweep_tc128_kernel(SweepArgs a) {
   const bool skip_all = __syncthreads_or(tmo);
   if (skip_all) tmo = 1;
 
+  // runs of consecutive order positions and the column cache of the search,
+  // as in the k <= 64 sweep (sweep_tc.cu)
+  const bool col = a.col_ent != nullptr && !a.list_offs && (int)blockIdx.x < a.col_slots;
+  double* ckey = reinterpret_cast<double*>(sm + L::CKEY);
+  int* run = reinterpret_cast<int*>(sm + L::RUN);
   for (; !skip_all;) {
     __syncthreads();
-    if (tid == 0) ctrl[0] = atomicAdd(a.counter, 1);
+    if (tid == 0) {
+      if (run[0] >= run[1]) {
+        int len = a.col_unit > 1 ? a.col_unit : 1;
+        const int left = npts_work - *reinterpret_cast<volatile int*>(a.counter);
+        const int share = left / (4 * (int)gridDim.x);
+        if (share < len) len = share > 1 ? share : 1;
+        const int s0 = atomicAdd(a.counter, len);
+        run[0] = min(s0, npts_work);
+        run[1] = (int)min((int64_t)s0 + len, (int64_t)npts_work);
+      }
+      ctrl[0] = run[0]++;
+    }
     __syncthreads();
     const int q = ctrl[0];
     if (q >= npts_work) break;
@@ -245,8 +268,26 @@ __global__ void __launch_bounds__(T8_NT, 1) sweep_tc128_kernel(SweepArgs a) {
       chunk++;
     };
     const int probe = a.probe_slot ? a.probe_slot[pt] : -1;
-    const int Lp = a.list_offs ? sweep_list<T8_NT, T8_CH>(a, qq, ss, flush)
-                               : sweep_search<T8_NT, T8_CH, 1>(a, ri, rj, logr, rz, ss, probe, flush);
+    int Lp;
+    const bool same_col = col && ri == ckey[0] && rj == ckey[1];
+    const int cn = run[2];
+    if (a.list_offs) {
+      Lp = sweep_list<T8_NT, T8_CH>(a, qq, ss, flush);
+    } else if (same_col && cn >= 0) {
+      Lp = sweep_search_cached<T8_NT, T8_CH>(a, a.col_ent + (size_t)blockIdx.x * a.col_cap * 2, cn, ri, rj, logr,
+                                             rz, ss, probe, flush);
+    } else if (col && !same_col) {
+      int nsv = 0;
+      const SwCache cache{a.col_ent + (size_t)blockIdx.x * a.col_cap * 2, a.col_cap};
+      Lp = sweep_search<T8_NT, T8_CH, 1>(a, ri, rj, logr, rz, ss, probe, flush, cache, &nsv);
+      if (tid == 0) {  // read by the next point, after the barriers in between
+        ckey[0] = ri;
+        ckey[1] = rj;
+        run[2] = nsv <= a.col_cap ? nsv : -1;
+      }
+    } else {  // no cache, or this column's did not fit
+      Lp = sweep_search<T8_NT, T8_CH, 1>(a, ri, rj, logr, rz, ss, probe, flush);
+    }
     for (int b = 0; b < 2; b++)
       if ((outst >> b) & 1u) {
         wait_bar(b);
