@@ -21,6 +21,10 @@ one persistent CUDA launch (and the Jacobi pass over any deferred points).
             FP64 oracle on that sample, relative to the background spread
 
 ``--impl reference`` times the CPU oracle alone (the reference arm).
+``--decompose`` runs one regional domain as 2-D process tiles with their
+halo observations (one exchange_obs all-gather per rank before the timed
+region; ``--tiles K`` runs K tiles in turn on one GPU and compares the
+reassembled analysis with the single-domain sweep bit for bit).
 """
 from __future__ import annotations
 
