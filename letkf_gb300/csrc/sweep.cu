@@ -1325,6 +1325,17 @@ int letkf_sweep_footprint(const letkf_sweep_desc* d, int nobs, size_t* bytes) {
   b += n * (6 * 8 + 4 * 4 + 2 * 16 + 4 + ne * es);
   // set_obs staging (unsorted records, permutation, cell counts) while the above is live
   size_t stage = n * (6 * 8 + 4 * 4 + ne * 8) + ncell * 16 + 64;
+  if (d->precision == LETKF_PREC_MIXED && d->ne <= 128 && np > 1) {
+    // the tensor-core sweeps' column cache (allocated when the points come in
+    // columns): slots per SM times the SMs of this device (152 when there is none)
+    int dev = 0, nsm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm < 1) {
+      cudaGetLastError();
+      nsm = 152;
+    }
+    b += (size_t)nsm * LETKF_COL_SLOTS_PER_SM * LETKF_COL_CAP * 32;
+  }
   if (d->precision == LETKF_PREC_F64) {
     // run_f64 chunk buffers with the local lists of one chunk (L <= nobs per point)
     const size_t c = np < 16384 ? np : 16384;
