@@ -22,7 +22,7 @@ extern "C" {
 #define LETKF_ERR_ARG 1      /* bad argument (ne < 2, nobsl < 0, nobsl > nobs, NULL array) */
 #define LETKF_ERR_EIG 2      /* common/common_mtx.f90:61-64,75-78: rs ierr /= 0 or all eigenvalues <= 0 (STOP 2) */
 #define LETKF_ERR_CUDA 3     /* a CUDA runtime call failed */
-#define LETKF_ERR_CAPACITY 4 /* size beyond this build's limits (ne > LETKF_MAX_NE, local obs overflow) */
+#define LETKF_ERR_CAPACITY 4 /* size beyond the library's limits (ne > LETKF_MAX_NE, local obs overflow) */
 #define LETKF_ERR_NOGPU 5    /* no CUDA device */
 #define LETKF_ERR_TIMEOUT 6  /* a bounded device wait gave up */
 

@@ -55,7 +55,7 @@ const char* letkf_status_string(int s) {
     case LETKF_ERR_ARG: return "bad argument";
     case LETKF_ERR_EIG: return "eigensolver failure (rs ierr /= 0 or no positive eigenvalue)";
     case LETKF_ERR_CUDA: return "CUDA runtime error";
-    case LETKF_ERR_CAPACITY: return "size beyond this build's limits";
+    case LETKF_ERR_CAPACITY: return "size beyond the library's limits";
     case LETKF_ERR_NOGPU: return "no CUDA device";
     case LETKF_ERR_TIMEOUT: return "bounded device wait timed out";
     case LETKF_PENDING: return "job not finished";

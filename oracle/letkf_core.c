@@ -1,6 +1,6 @@
 /*
  * letkf_core.c -- CPU FP64 restatement of the reference numerics.
- * TEST INFRASTRUCTURE ONLY (the checker for the CUDA path; never shipped).
+ * TEST INFRASTRUCTURE ONLY (the oracle of the CUDA path; never shipped).
  * Parity unpinned against the Fortran itself (no Fortran compiler, no
  * reference golden data); pinned by the maths known-answer tests in tests/.
  *

@@ -1,7 +1,7 @@
 /*
  * letkf_oracle.h -- CPU FP64 restatement of the reference LETKF analysis path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA path:
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle of the CUDA path:
  * only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg / the
  * reference arm may load it.  The product path never calls into it.
  *

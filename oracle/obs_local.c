@@ -1,6 +1,6 @@
 /*
  * obs_local.c -- CPU restatement of the reference local-observation search.
- * TEST INFRASTRUCTURE ONLY (the checker for the CUDA search; never shipped).
+ * TEST INFRASTRUCTURE ONLY (the oracle of the CUDA search; never shipped).
  * Parity unpinned against the Fortran itself (no compiler, no golden data).
  *
  * Selected-observation lists and their order are the reference's; the CUDA

@@ -1,7 +1,7 @@
 /*
  * obs_operator.c -- CPU FP64 restatement of the SPEEDY observation operator
  * H(x) and of the driver rules around it.  TEST INFRASTRUCTURE ONLY (see
- * letkf_oracle.h): the checker for letkf_speedy_obsope.
+ * letkf_oracle.h): the oracle of letkf_speedy_obsope.
  *
  *   phys2ijk     speedy/common/common_obs_speedy.f90:137-206
  *   Trans_XtoY   speedy/common/common_obs_speedy.f90:29-80

@@ -1,7 +1,7 @@
 /*
  * obs_operator_scale.c -- CPU FP64 restatement of the SCALE observation
  * operator H(x) for conventional observations.  TEST INFRASTRUCTURE ONLY (see
- * letkf_oracle.h): the checker for letkf_scale_obsope.
+ * letkf_oracle.h): the oracle of letkf_scale_obsope.
  *
  *   obsope_cal   scale/obs/obsope_tools.f90:340-380 (OBS_IN_FORMAT 1: phys2ijk,
  *                then Trans_XtoY where it kept qc good), :602-608 (qc over

@@ -1,6 +1,6 @@
 """ctypes front end of the CPU oracle (test infrastructure only).
 
-This module is the checker: tests/, __graft_entry__.smoke() and bench.py's
+This module is the test oracle: tests/, __graft_entry__.smoke() and bench.py's
 CPU legs import it; the package ``letkf_gb300`` never does.  All arrays are
 float64 / int32 numpy arrays; column-major arrays are passed in Fortran order.
 """

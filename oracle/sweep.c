@@ -1,6 +1,6 @@
 /*
  * sweep.c -- CPU restatement of the SCALE-style das_letkf grid loop.
- * TEST INFRASTRUCTURE ONLY: the checker for the GPU sweep and the timed CPU
+ * TEST INFRASTRUCTURE ONLY: the oracle of the GPU sweep and the timed CPU
  * baseline.  Parity unpinned against the Fortran itself.
  *
  * Per grid point (scale/letkf/letkf_tools.f90:175-251, OpenMP
