@@ -10,6 +10,9 @@ the device path of this library (search -> gather -> batched core -> update).
 * ``speedy_cycle`` -- the letkf program (speedy/letkf/letkf.f90) from member grd
   files and an observation file to analysis files
 
+* ``scale_obs_setup`` -- set_letkf_obs of the SCALE driver for conventional
+  observations with H(x) of every member computed on the device (obsope_cal)
+
 The regional SCALE-style driver is the resident ``sweep.Sweep`` handle.  All
 compute runs in libletkf_gpu.so; torch only holds device memory and does
 layout transposes.
@@ -348,3 +351,45 @@ def l96_letkf_4d(xf, hxf, y, obs_cell, obserr=1.0, xlocal=3.0, tlocal=2.0, parm_
 
 __all__ = ["speedy_sort_obs", "var_local_n2n", "speedy_letkf", "l96_letkf", "l96_letkf_4d", "speedy_obs_setup",
            "speedy_cycle"]
+
+
+# ------------------------------------------------------------------------ SCALE
+SCALE_GROSS_ERROR = 5.0  # scale/common/common_nml.f90:83
+SCALE_IQC_GROSS_ERR = 5  # scale/common/common_obs_scale.f90:142
+SCALE_PS = 14593
+
+
+def scale_obs_setup(v3d, v2d, khalo, obs, rotc=None, stggrd=0, ps_adjust_thres=100.0, gross_error=SCALE_GROSS_ERROR,
+                    stream=None):
+    """set_letkf_obs of the SCALE driver for conventional observations
+    (scale/letkf/letkf_obs.f90:260-600) with H(x) of every member from the
+    device (letkf_scale_obsope, obsope_cal's conventional path) instead of
+    per-member obsda files: qc the maximum over members (:272), the member
+    mean (sequential sum, :562-566), Hdx and y - Hx (:574-577), the gross-error
+    check |y - Hx| > GROSS_ERROR err (qc 5, :586-630) and the selection of
+    qc 0.  v3d / v2d as core.scale_obsope takes them (device); obs: dict of
+    arrays elem, ri, rj, lev, dat, err (the halo-domain ri / rj obsope uses).
+    Returns (records, qc): records is a dict of host arrays for the selected
+    observations, ri, rj, lev, dat, err, dep, cls (1 for ps, whose vertical
+    coordinate in the search is the observed pressure; 0 otherwise) and hdxf
+    [n, ne] float32, ready for Sweep.set_obs; qc holds every observation's
+    SCALE code."""
+    import torch
+
+    dev = v3d.device
+    t = lambda a, dt=torch.float64: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
+    elem = t(obs["elem"], torch.int32)
+    rc = None if rotc is None else t(rotc)
+    hx, qc = K.scale_obsope(v3d, v2d, khalo, elem, t(obs["ri"]), t(obs["rj"]), t(obs["lev"]), rc, stggrd,
+                            ps_adjust_thres, stream=stream)
+    good = (qc == 0).to(torch.int32)  # the departure kernel takes 1 for a usable observation
+    hdxf, dep, ok = K.obs_departure(hx, t(obs["dat"]), t(obs["err"]), gross_error, good, stream)
+    qc_all = torch.where((good == 1) & (ok == 0), torch.full_like(qc, SCALE_IQC_GROSS_ERR), qc)
+    sel = torch.nonzero(ok == 1).flatten()
+    host = lambda a: a[sel].cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)[sel.cpu().numpy()]
+    el = host(elem)
+    rec = {"ri": host(obs["ri"]), "rj": host(obs["rj"]), "lev": host(obs["lev"]), "dat": host(obs["dat"]),
+           "err": host(obs["err"]), "dep": host(dep), "cls": (el == SCALE_PS).astype(np.int32),
+           "hdxf": hdxf[sel].to(torch.float32).cpu().numpy()}
+    return rec, qc_all.cpu().numpy()
+
