@@ -6,7 +6,7 @@ seeded inputs.  They pin the oracle against regressions (CPU tests) and give
 the CUDA path committed vectors to match (GPU tests).  Each case stores its
 inputs and outputs so the tests need no generator.
 
-    python tests/golden/make_golden.py        # rewrites tests/golden/*.npz
+    python tests/golden/make_golden.py [name.npz ...]   # rewrites tests/golden/*.npz
 """
 from __future__ import annotations
 
@@ -151,10 +151,56 @@ def l96_fixture():
             "idx": np.concatenate(idx_all).astype(np.int32), "rloc": np.concatenate(rloc_all)}
 
 
-def main():
+def scale_obsope_fixture():
+    """The SCALE conventional observation operator (scale/obs/obsope_tools.f90:
+    340-380) on 4 members of a 10 x 9 x (6 + 2 KHALO) domain with terrain
+    (levels below ground in some columns): 240 observations of every element
+    inside, outside, above and below the domain, rotated winds."""
+    rng = np.random.default_rng(31)
+    ne, nlonh, nlath, nlev, kh = 4, 10, 9, 6, 2
+    nlevh = nlev + 2 * kh
+    sig = np.exp(-0.45 * (np.arange(nlevh) - kh))
+    J, I = np.meshgrid(np.arange(1, nlath + 1), np.arange(1, nlonh + 1), indexing="ij")
+    zs = 300.0 * (1 + np.sin(I / 2.0) * np.cos(J / 3.0))
+    v3d = np.empty((ne, 6, nlath, nlonh, nlevh))
+    v2d = np.empty((ne, 4, nlath, nlonh))
+    for m in range(ne):
+        ps = 1.0e5 * np.exp(-zs / 8000.0) * (1 + 0.01 * rng.standard_normal((nlath, nlonh)))
+        p = ps[:, :, None] * sig[None, None, :]
+        v3d[m, 5] = np.where((zs > 450.0)[:, :, None] & (np.arange(nlevh) < kh + 2), -1.0, p)
+        for n, (sc, off) in enumerate([(5, 3), (5, -2), (8, 260), (0.002, 0.005), (0.1, 0.6)]):
+            v3d[m, n] = off + sc * rng.standard_normal((nlath, nlonh, nlevh))
+        v2d[m] = np.stack([ps, 285 + rng.standard_normal((nlath, nlonh)),
+                           0.008 + 0.001 * rng.standard_normal((nlath, nlonh)), zs])
+    nobs = 240
+    elem = rng.choice(np.array([2819, 2820, 3073, 3074, 3330, 3331, 14593, 4321], np.int32), nobs).astype(np.int32)
+    ri = rng.uniform(0.5, nlonh + 0.3, nobs)
+    rj = rng.uniform(0.5, nlath + 0.3, nobs)
+    rlev = np.exp(rng.uniform(np.log(3e3), np.log(1.2e5), nobs))
+    sfc = elem == 14593
+    rlev[sfc] = rng.uniform(0.0, 900.0, sfc.sum())
+    ang = rng.uniform(-0.6, 0.6, nobs)
+    rotc = np.stack([np.cos(ang), np.sin(ang)], -1)
+    hx, qc, qcm = O.scale_obsope(v3d, v2d, kh, elem, ri, rj, rlev, rotc)
+    assert {0, 10, 20, 21, 22, 90} <= set(np.unique(qcm).tolist())
+    return {"v3d": v3d, "v2d": v2d, "khalo": np.int32(kh), "elem": elem, "ri": ri, "rj": rj, "rlev": rlev,
+            "rotc": rotc, "hx": hx, "qc": qc, "qc_member": qcm}
+
+
+FIXTURES = {"core_cases.npz": lambda rng: core_fixture(rng), "scale_search.npz": lambda rng: scale_fixture(),
+            "speedy_search.npz": lambda rng: speedy_fixture(), "l96_analysis.npz": lambda rng: l96_fixture(),
+            "scale_obsope.npz": lambda rng: scale_obsope_fixture()}
+
+
+def main(names=None):
+    """Rewrite the named fixtures (all of them by default); the core cases
+    draw from one seeded generator, so they are made first in this order."""
     rng = np.random.default_rng(20240601)
-    files = {"core_cases.npz": core_fixture(rng), "scale_search.npz": scale_fixture(),
-             "speedy_search.npz": speedy_fixture(), "l96_analysis.npz": l96_fixture()}
+    files = {}
+    for name, make in FIXTURES.items():
+        d = make(rng)
+        if not names or name in names:
+            files[name] = d
     for name, d in files.items():
         path = os.path.join(HERE, name)
         np.savez_compressed(path, **d)
@@ -162,4 +208,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -162,3 +162,30 @@ def test_gpu_speedy_search_matches_fixture(cuda):
     np.testing.assert_array_equal(idx.cpu().numpy(), g["idx"])
     np.testing.assert_allclose(rloc.cpu().numpy(), g["rloc"], rtol=1e-13, atol=1e-300)
     np.testing.assert_array_equal(rdiag.cpu().numpy(), g["rdiag"])
+
+
+def test_oracle_reproduces_scale_obsope_fixture():
+    g = _load("scale_obsope.npz")
+    hx, qc, qcm = O.scale_obsope(g["v3d"], g["v2d"], int(g["khalo"]), g["elem"], g["ri"], g["rj"], g["rlev"],
+                                 g["rotc"])
+    np.testing.assert_array_equal(qcm, g["qc_member"])
+    np.testing.assert_array_equal(qc, g["qc"])
+    np.testing.assert_allclose(hx, g["hx"], rtol=1e-13, atol=0)
+
+
+@pytest.mark.gpu
+def test_gpu_scale_obsope_matches_fixture(cuda):
+    """Values within 1e-12 of each observation's largest magnitude over the
+    members (log and pow differ by an ulp from the host), qc equal."""
+    import torch
+
+    from letkf_gb300.core import scale_obsope
+
+    g = _load("scale_obsope.npz")
+    t = lambda a, dt=torch.float64: _t(a, dt, cuda)
+    hx, qc, qcm = scale_obsope(t(g["v3d"]), t(g["v2d"]), int(g["khalo"]), t(g["elem"], torch.int32), t(g["ri"]),
+                               t(g["rj"]), t(g["rlev"]), t(g["rotc"]), want_member_qc=True)
+    np.testing.assert_array_equal(qcm.cpu().numpy(), g["qc_member"])
+    np.testing.assert_array_equal(qc.cpu().numpy(), g["qc"])
+    scale = np.abs(g["hx"]).max(axis=1, keepdims=True)
+    assert (np.abs(hx.cpu().numpy() - g["hx"]) <= 1e-12 * scale).all()
